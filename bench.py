@@ -1,0 +1,396 @@
+"""Benchmark of the GB300 DIC hot path on the 2048x2048 / 41x41-subset workload.
+
+A step is one target frame through FFT-CC then IC-GN (155,236 POIs) with the
+reference image's precompute cached, as the reference's worker thread runs it
+(TW/TW_Core/fftcctworkerthread.cpp:399-481).  Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's CPU algorithm (the oracle restatement;
+the reference itself cannot be built here) on the host cores instead.
+Multi-GPU runs are independent replicas (the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "POIs/s at 2048², 41px subsets; p50/p99 frame latency vs plain FP32 GPU path"
+UNIT = "POIs/s"
+WORKLOAD = ("2048x2048 uint8 speckle pair (100k speckles, sinusoidal field u=3sin(2pi x/1024)+1.5, "
+            "v=2cos(2pi y/768)-0.8, noise sigma 2), ROI 2046x2046 at (1,1), 41x41 subsets (r=20), step 5, "
+            "margin 20 -> 155,236 POIs; FFT-CC + IC-GN (max 20 iterations, dP < 0.001) per frame, "
+            "reference precompute cached")
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+# --------------------------------------------------------------- clocks ----
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------- distributed ----
+def dist_setup(n_gpus):
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("TWDIC_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    """Max of a per-rank time over all ranks (the job ends with its slowest rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ workloads ----
+def workload():
+    from tw_gb300 import synth
+    return synth.scale_2048()
+
+
+def params_of(g, path):
+    from tw_gb300 import dic
+    return dic.make_params(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r,
+                           g.grid, g.grid, g.margin, g.margin, g.max_iter, g.delta_p, path)
+
+
+# ------------------------------------------------------------- CPU legs ----
+def cpu_rate(pair, g, poi, n_sample, nthreads=0):
+    """Oracle (restated reference CPU path) throughput, extrapolated to a full
+    frame: the reference recomputes the gradients and the target LUT of the
+    whole ROI once per ICGN2D_Algorithm call (TW_paDIC_ICGN2D_CPU.cpp:77-132),
+    timed here with an empty POI list, plus FFT-CC and IC-GN of the first
+    n_sample POIs scaled to all POIs.  Returns (POIs/s, seconds spent, threads)."""
+    from oracle import oracle as O
+    sp = np.ascontiguousarray(poi[:n_sample])
+    t0 = time.perf_counter()
+    O.icgn(pair.ref, pair.tar, g, sp[:0], np.zeros(0, np.float32), np.zeros(0, np.float32), nthreads=nthreads)
+    t_pre = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    u, v, z, st = O.fftcc(pair.ref, pair.tar, sp, g.subset_r, nthreads=nthreads)
+    O.icgn(pair.ref, pair.tar, g, sp, u, v, nthreads=nthreads)
+    t_sample = time.perf_counter() - t1
+    per_poi = max(t_sample - t_pre, 1e-9) / n_sample
+    frame_s = t_pre + per_poi * len(poi)
+    return len(poi) / frame_s, t_pre + t_sample, O.max_threads()
+
+
+def cpu_baseline(pair, g, poi, target_s=12.0):
+    rate, dt, thr = cpu_rate(pair, g, poi, 1500)
+    n = int(min(len(poi), max(1500, rate * target_s)))
+    rate, dt, thr = cpu_rate(pair, g, poi, n)
+    return {"value": round(rate, 1), "unit": UNIT, "cores": thr, "kind": "port",
+            "sample": f"first {n} POIs (row-major) of the workload, FFT-CC + IC-GN, plus the per-frame whole-ROI "
+                      f"gradient/LUT precompute, extrapolated to all {len(poi)} POIs ({dt:.1f} s of CPU work); OpenMP "
+                      "over POIs; oracle = C++ restatement of the reference CPU path (MKL/FFTW/LAPACKE not available)"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    pair, g = workload()
+    from tw_gb300 import synth  # noqa: F401
+    from oracle import oracle as O
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    rate, dt, thr = cpu_rate(pair, g, poi, 1000)
+    per_step = int(min(len(poi), max(1000, rate * 3.0)))  # about 3 s of CPU work per step
+    for _ in range(args.warmup):
+        cpu_rate(pair, g, poi, 500)
+    rates, spent = [], []
+    for _ in range(args.steps):
+        r, dt, thr = cpu_rate(pair, g, poi, per_step)
+        rates.append(r)
+        spent.append(dt)
+    value = len(rates) / sum(1.0 / r for r in rates)  # frames at the harmonic-mean rate
+    lat = sorted(1000.0 * len(poi) / r for r in rates)  # full-frame latency, extrapolated
+    times = [1000.0 * len(poi) / r / 1000.0 for r in rates]
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000.0 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": f"bounded sample of {per_step} POIs per step"},
+            "frame_latency_ms": {"p50": round(lat[len(lat) // 2], 1), "p99": round(lat[-1], 1),
+                                 "note": "full-frame latency extrapolated from the sample"},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": f"{per_step} POIs per step (+ whole-ROI precompute), extrapolated to "
+                                       f"{len(poi)} POIs; {sum(spent):.1f} s of CPU work over {args.steps} steps"},
+            "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------- GPU legs ----
+def time_frames(fr, tar_dev, outs, steps, warmup, flush, torch):
+    """Device-timed frames with device-resident inputs; L2 flushed between
+    frames outside the timed events."""
+    for i in range(warmup):
+        flush.fill_(i)
+        fr.process(tar_dev, **outs)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    phases = []
+    for i in range(steps):
+        flush.fill_(i)
+        evs[i][0].record(stream)
+        fr.process(tar_dev, **outs)
+        evs[i][1].record(stream)
+        phases.append(fr.phase_times())
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    return ms, phases
+
+
+def time_e2e(fr, tar_host, outs_host, steps, warmup, flush, torch):
+    for i in range(warmup):
+        flush.fill_(i)
+        torch.cuda.synchronize()
+        fr.process(tar_host, **outs_host)
+    ms = []
+    for i in range(steps):
+        flush.fill_(i)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fr.process(tar_host, **outs_host)  # synchronous: host outputs
+        ms.append(1000.0 * (time.perf_counter() - t0))
+    return ms
+
+
+def pct(xs, q):
+    s = sorted(xs)
+    return s[min(len(s) - 1, int(round(q / 100.0 * (len(s) - 1))))]
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    from tw_gb300 import PATH_FAST, PATH_PLAIN, dic
+    from tw_gb300.build import build
+    build()
+    torch.cuda.set_device(local)
+    pair, g = workload()
+    P = None
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    tar_dev = torch.from_numpy(pair.tar).cuda()
+    ref_dev = torch.from_numpy(pair.ref).cuda()
+
+    fr = dic.DICFrame(params_of(g, PATH_FAST))
+    P = fr.n
+    fr.set_stream(torch.cuda.current_stream())
+    fr.set_reference(ref_dev)
+    outs = fr.alloc_outputs(device="cuda")
+
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    ms, phases = time_frames(fr, tar_dev, outs, args.steps, args.warmup, flush, torch)
+    t_wall = time.perf_counter() - t_wall0
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    clk = clocks.stop()
+    total_ms = max_over_ranks(sum(ms), world)
+    value = P * args.steps * world / (total_ms / 1000.0)
+
+    # end-to-end through the public API with pinned host buffers
+    tar_pin = torch.from_numpy(pair.tar).pin_memory()
+    outs_h = {k: torch.from_numpy(v).pin_memory() for k, v in fr.alloc_outputs().items()}
+    e2e_ms = time_e2e(fr, tar_pin, outs_h, args.steps, args.warmup, flush, torch)
+    e2e_total = max_over_ranks(sum(e2e_ms), world)
+    e2e_value = P * args.steps * world / (e2e_total / 1000.0)
+    d2h = sum(int(v.numel() * v.element_size()) for v in outs_h.values())
+
+    # accuracy of the last frame vs the imposed field
+    from oracle import compare as C  # test infrastructure: truth error only
+    p6 = outs["p6"].cpu().numpy()
+    flags = outs["flags"].cpu().numpy()
+    iters = outs["iters"].cpu().numpy()
+    poi = fr.poi_positions()
+    acc = C.truth_error(pair, poi, p6, flags)
+    kbar = float(iters[flags == 0].mean())
+
+    # plain FP32 GPU path, same workload, same timing rules
+    frp = dic.DICFrame(params_of(g, PATH_PLAIN))
+    frp.set_stream(torch.cuda.current_stream())
+    frp.set_reference(ref_dev)
+    outs_p = frp.alloc_outputs(device="cuda")
+    psteps = max(3, min(args.steps, 10))
+    ms_p, phases_p = time_frames(frp, tar_dev, outs_p, psteps, min(args.warmup, 3), flush, torch)
+    plain_value = P * psteps / (sum(ms_p) / 1000.0)
+    del frp, outs_p
+    torch.cuda.empty_cache()
+
+    # roofline of the dominant phase
+    ph = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
+    roof = roofline(g, P, ph, kbar)
+
+    line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (IC-GN), fp16 tensor core / fp32 (FFT-CC), "
+                                                            "fp64 (6x6 solve)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "path": "fast", "pois": P, "l2": "flushed between steps (256 MB write, "
+                       "outside the timed events)", "parallelism": f"replicas x{world}"},
+            "frame_latency_ms": {"p50": round(pct(ms, 50), 4), "p99": round(pct(ms, 99), 4)},
+            "phases_ms": {k: round(v, 4) for k, v in ph.items()},
+            "plain_fp32": {"value": round(plain_value, 1), "ms_per_step": round(sum(ms_p) / psteps, 4),
+                           "p50_ms": round(pct(ms_p, 50), 4), "p99_ms": round(pct(ms_p, 99), 4),
+                           "phases_ms": {k: round(statistics.mean(p[k] for p in phases_p), 4)
+                                         for k in phases_p[0]}},
+            "speedup_vs_plain_fp32": round(value / (plain_value * world), 3),
+            "accuracy": {"vs_imposed_field": acc, "mean_iterations": round(kbar, 3),
+                         "success_fraction": float((flags == 0).mean())},
+            "roofline": roof,
+            "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(pair.tar.nbytes),
+                    "d2h_bytes_per_step": d2h, "p50_ms": round(pct(e2e_ms, 50), 4),
+                    "p99_ms": round(pct(e2e_ms, 99), 4)},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk,
+            "wall_s_timed_region": round(t_wall, 3)}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O  # noqa: F401  (CPU baseline leg)
+        line["cpu_baseline"] = cpu_baseline(pair, g, poi)
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def roofline(g, P, ph, kbar):
+    """Roofline of the dominant phase.  IC-GN (fast path) moves little DRAM
+    traffic: its algorithmic bytes per POI are the compulsory ones -- the
+    per-reference cache entry (184 B), u/v in and out (16 B), p6 (24 B),
+    iteration count and flag (5 B) -- plus both images once per frame.  Its
+    FP32 work per POI is k*S*64 flops (k = mean iterations)."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tc = peaks.get("bf16_tflops", 1900.0)
+    src = "measured" if peaks else "fallback"
+    S = (2 * g.subset_r + 1) ** 2
+    N = 2 * g.subset_r
+    if ph["icgn"] >= ph["fftcc"]:
+        bytes_per_launch = P * (184 + 16 + 24 + 5) + 2 * g.img_w * g.img_h
+        achieved = bytes_per_launch / (ph["icgn"] / 1000.0) / 1e9
+        fp32_flops = kbar * S * 64 * P
+        return {"kernel": "k_icgn_fast (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2),
+                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": None,
+                "peak_source": src, "algorithmic_bytes_per_launch": bytes_per_launch,
+                "fp32_tflops": round(fp32_flops / (ph["icgn"] / 1000.0) / 1e12, 2),
+                "note": "IC-GN is FP32/shared-memory bound; the HBM fraction shows it is not memory bound"}
+    flops = 48 * N ** 3 * P
+    achieved = flops / (ph["fftcc"] / 1000.0) / 1e12
+    return {"kernel": "FFT-CC", "bound": "tensor", "achieved": round(achieved, 2), "peak": tc, "unit": "TFLOP/s",
+            "frac": round(achieved / tc, 4), "traffic": None, "peak_source": src,
+            "algorithmic_flops_per_launch": flops}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank)
+    else:
+        rc = run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,191 @@
+/*
+ * tw_dic.h -- C ABI of the GB300 (sm_103a) 2D DIC hot path: integer-pixel
+ * FFT cross-correlation (FFT-CC) followed by first-order IC-GN sub-pixel
+ * registration with bicubic interpolation.
+ *
+ * Drop-in boundary for TW_Engine's FFT-CC and IC-GN classes.  Each entry
+ * point names the reference interface it replaces (paths relative to the
+ * TWANG006/TW project root).  Conventions:
+ *   - every function returns an int status, TWDIC_OK (0) on success and a
+ *     negative TWDIC_ERR_* value otherwise; nothing calls exit() or throws
+ *     across the ABI (the reference's checkCudaErrors exits the process,
+ *     TW/TW_Engine/helper_cuda.h:965-995);
+ *   - images are 8-bit gray, row-major, `stride` bytes per row (the reference
+ *     copies rows*cols bytes of a contiguous cv::Mat, so stride == width
+ *     there, TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:281-287);
+ *   - POI positions are int32 (y, x) pairs, x fastest, as the reference's
+ *     iPOIXY arrays (TW/TW_Engine/TW_utils.cpp:29-49);
+ *   - a `mem` argument says whether a pointer is host (TWDIC_MEM_HOST) or
+ *     device (TWDIC_MEM_DEVICE) memory; host buffers are staged through the
+ *     handle's device buffers on the handle's stream;
+ *   - caller-owned buffers throughout: handles never free memory they did
+ *     not allocate (the reference's cuICGN2D destructor frees borrowed
+ *     pointers, TW/TW_Engine/TW_paDIC_cuICGN2D.cu:719-729; this ABI does not).
+ *   - handles are not thread-safe (neither are the reference's objects);
+ *     distinct handles may be used from distinct threads.
+ */
+#ifndef TW_DIC_H
+#define TW_DIC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define TWDIC_API __attribute__((visibility("default")))
+#else
+#define TWDIC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TWDIC_ABI_VERSION 1
+
+/* status codes */
+#define TWDIC_OK 0
+#define TWDIC_ERR_INVALID_ARG (-1)  /* bad pointer, size or enum value */
+#define TWDIC_ERR_NO_POI (-2)       /* "Number of POIs is below 0!" (TW_paDIC_FFTCC2D.cpp:88-94 via cuFFTCC2D ctor) */
+#define TWDIC_ERR_BORDER (-3)       /* ROI leaves no one-pixel image border (TW_utils.cpp:254-257, :615-619) */
+#define TWDIC_ERR_STATE (-4)        /* call order: e.g. compute before a reference image was set */
+#define TWDIC_ERR_CUDA (-5)         /* a CUDA runtime call failed; see twdic_last_error() */
+#define TWDIC_ERR_NO_MEMORY (-6)    /* device allocation failed or the HBM budget would be exceeded */
+#define TWDIC_ERR_UNSUPPORTED (-7)  /* parameter outside this build's limits (e.g. subset radius > 31) */
+#define TWDIC_ERR_TIMEOUT (-8)      /* a bounded device-side wait gave up */
+
+#define TWDIC_MEM_HOST 0
+#define TWDIC_MEM_DEVICE 1
+
+/* Compute path.  PLAIN is the straightforward FP32 SIMT path (one CTA per
+ * POI, per-reference steepest-descent images and per-frame bicubic LUT in
+ * HBM).  FAST is the tensor-core / staged-window path (FP16 hi/lo DFT GEMMs on
+ * tcgen05, FP64 Cholesky, on-chip interpolation). */
+#define TWDIC_PATH_PLAIN 0
+#define TWDIC_PATH_FAST 1
+
+/* ICGN2DFlag (TW/TW_Engine/TW_paDIC.h:74-81) */
+#define TWDIC_ICGN_SUCCESS 0
+#define TWDIC_ICGN_DARK_SUBSET 1
+#define TWDIC_ICGN_SINGULAR_HESSIAN 2
+#define TWDIC_ICGN_SINGULAR_WARP 3
+#define TWDIC_ICGN_OUT_OF_ROI 4
+
+/* FFT-CC per-POI status */
+#define TWDIC_FFTCC_OK 0
+#define TWDIC_FFTCC_DARK_SUBSET 1 /* outputs of this POI are left untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275) */
+
+/* Constructor parameters.  Field meaning follows the reference constructors:
+ * Fftcc2D(imgW, imgH, startX, startY, roiW, roiH, subsetX, subsetY, gridX,
+ * gridY, marginX, marginY) (TW/TW_Engine/TW_paDIC_FFTCC2D.h:38-43) and
+ * ICGN2D_CPU/cuICGN2D(..., iNumIterations, fDeltaP, ...)
+ * (TW/TW_Engine/TW_paDIC_ICGN2D_CPU.h:23-44, TW_paDIC_cuICGN2D.h:14-22). */
+typedef struct twdic_params {
+  int32_t img_width, img_height;  /* whole image */
+  int32_t start_x, start_y;       /* ROI top-left */
+  int32_t roi_width, roi_height;
+  int32_t subset_x, subset_y;     /* half sizes r: FFT window 2r, IC-GN subset 2r+1 */
+  int32_t grid_space_x, grid_space_y;
+  int32_t margin_x, margin_y;
+  int32_t max_iterations;         /* IC-GN iteration cap (callers use 20) */
+  float delta_p;                  /* IC-GN convergence threshold on the scaled ||dP|| (callers use 0.001) */
+  int32_t path;                   /* TWDIC_PATH_* */
+} twdic_params;
+
+/* Last error message of the calling thread (never NULL). */
+TWDIC_API const char* twdic_last_error(void);
+TWDIC_API int twdic_abi_version(void);
+
+/* Number of POIs for a parameter set: NX = floor((roiW - 2 rX - 2 mX) / gX) + 1
+ * (Fftcc2D::recomputeNumPOI, TW/TW_Engine/TW_paDIC_FFTCC2D.cpp:88-94). */
+TWDIC_API int twdic_num_pois(const twdic_params* p, int32_t* num_x, int32_t* num_y);
+
+/* POI grid (ComputePOIPositions_s/_m, TW/TW_Engine/TW_utils.cpp:29-94;
+ * cuComputePOIPositions, TW/TW_Engine/TW_cuUtils.cu:83-134).  Host output,
+ * num_x*num_y (y, x) pairs. */
+TWDIC_API int twdic_poi_positions(const twdic_params* p, int32_t* poi_yx);
+
+/* ------------------------------------------------------------- FFT-CC --- */
+typedef struct twdic_fftcc twdic_fftcc;
+
+/* cuFFTCC2D(imgW, imgH, roiW, roiH, startX, startY, ...) / Fftcc2D_CPU ctor
+ * (TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:193-210, TW_paDIC_FFTCC2D_CPU.cpp:8-79)
+ * plus cuInitializeFFTCC's allocations (TW_paDIC_cuFFTCC2D.cu:464-548). */
+TWDIC_API int twdic_fftcc_create(const twdic_params* p, twdic_fftcc** out);
+/* GetNumPOIsX / GetNumPOIsY (TW/TW_Engine/TW_paDIC_FFTCC2D.h:99-101) */
+TWDIC_API int twdic_fftcc_num_pois(const twdic_fftcc* h, int32_t* num_x, int32_t* num_y);
+/* The handle's device POI array (g_cuHandle.m_d_iPOIXY): copies it out. */
+TWDIC_API int twdic_fftcc_poi_positions(const twdic_fftcc* h, int32_t* poi_yx, int mem);
+/* ResetRefImg (TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:679-685) */
+TWDIC_API int twdic_fftcc_reset_ref(twdic_fftcc* h, const uint8_t* img, int32_t stride, int mem);
+/* SetTarImg (TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:687-693) */
+TWDIC_API int twdic_fftcc_set_tar(twdic_fftcc* h, const uint8_t* img, int32_t stride, int mem);
+/* ComputeFFTCC / cuComputeFFTCC on the current target
+ * (TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:334-431, :550-647; CPU semantics of
+ * TW_paDIC_FFTCC2D_CPU.cpp:222-326).  u, v, zncc: num_pois floats each.
+ * status (may be NULL): num_pois bytes of TWDIC_FFTCC_*. */
+TWDIC_API int twdic_fftcc_compute(twdic_fftcc* h, float* u, float* v, float* zncc, uint8_t* status, int mem);
+/* DestroyFFTCC / cuDestroyFFTCC (TW/TW_Engine/TW_paDIC_cuFFTCC2D.cu:433-461, :649-677) */
+TWDIC_API int twdic_fftcc_destroy(twdic_fftcc* h);
+
+/* -------------------------------------------------------------- IC-GN --- */
+typedef struct twdic_icgn twdic_icgn;
+
+/* cuICGN2D(imgW, imgH, startX, startY, roiW, roiH, subsetX, subsetY,
+ * numberX, numberY, iNumIterations, fDeltaP, Iflag) + prepare()
+ * (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:694-768); ICGN2D_CPU ctor
+ * (TW_paDIC_ICGN2D_CPU.cpp:13-34).  num_x*num_y is the POI count of every
+ * compute call. */
+TWDIC_API int twdic_icgn_create(const twdic_params* p, int32_t num_x, int32_t num_y, twdic_icgn** out);
+/* ResetRefImg / cuInitialize (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:770-795;
+ * TW_paDIC_ICGN2D_CPU.cpp:66-70).  The per-reference precompute runs on the
+ * next compute call whose POIs differ from the cached ones. */
+TWDIC_API int twdic_icgn_reset_ref(twdic_icgn* h, const uint8_t* img, int32_t stride, int mem);
+/* cuCompute (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:811-968) with the CPU path's
+ * semantics ICGN2D_Algorithm (TW_paDIC_ICGN2D_CPU.cpp:77-132, :481-925).
+ *   tar     target image (mem_in)
+ *   poi_yx  num_pois (y, x) pairs (mem_in)
+ *   u, v    in/out: FFT-CC guesses in, sub-pixel displacements out (mem_out)
+ *   p6      out (may be NULL): num_pois x (u, ux, uy, v, vx, vy)
+ *   iters   in/out (may be NULL): iteration counter per POI; left unchanged
+ *           for POIs that stop before their first solve, as the reference
+ *   flags   out (may be NULL): TWDIC_ICGN_* per POI */
+TWDIC_API int twdic_icgn_compute(twdic_icgn* h, const uint8_t* tar, int32_t stride, const int32_t* poi_yx, int mem_in,
+                       float* u, float* v, float* p6, int32_t* iters, uint8_t* flags, int mem_out);
+/* cuFinalize + destructor (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:970-989) */
+TWDIC_API int twdic_icgn_destroy(twdic_icgn* h);
+
+/* --------------------------------------------------- fused frame path --- */
+/* One frame of FFTCCTWorkerThread::processFrameFFTCC_ICGN's DIC work
+ * (TW/TW_Core/fftcctworkerthread.cpp:399-481): cuComputeFFTCC then
+ * cuICGN2D::cuCompute on the same target, with the reference cached. */
+typedef struct twdic_frame twdic_frame;
+TWDIC_API int twdic_frame_create(const twdic_params* p, twdic_frame** out);
+TWDIC_API int twdic_frame_num_pois(const twdic_frame* h, int32_t* num_x, int32_t* num_y);
+TWDIC_API int twdic_frame_poi_positions(const twdic_frame* h, int32_t* poi_yx, int mem);
+TWDIC_API int twdic_frame_set_reference(twdic_frame* h, const uint8_t* img, int32_t stride, int mem);
+/* Outputs (any may be NULL except u, v): zncc from FFT-CC, the IC-GN
+ * deformation p6, iteration counts and flags. */
+TWDIC_API int twdic_frame_process(twdic_frame* h, const uint8_t* tar, int32_t stride, int mem_in, float* u, float* v,
+                        float* zncc, float* p6, int32_t* iters, uint8_t* flags, int mem_out);
+/* Bind a handle to a CUDA stream (cudaStream_t passed as void*; NULL = the
+ * handle's own stream).  All work of later calls is ordered on it. */
+TWDIC_API int twdic_frame_set_stream(twdic_frame* h, void* stream);
+/* Device time of the phases of the last process call, in milliseconds:
+ * t[0] target upload, t[1] FFT-CC, t[2] target preparation, t[3] IC-GN,
+ * t[4] result download, t[5] per-reference precompute (0 when cached). */
+TWDIC_API int twdic_frame_phase_times(const twdic_frame* h, float* t6);
+TWDIC_API int twdic_frame_destroy(twdic_frame* h);
+
+/* Launch-shape tuning of a frame handle (no counterpart in the reference;
+ * set by the autotuner).  icgn_threads: 128 or 256 threads per IC-GN CTA;
+ * icgn_ctas_per_sm: persistent CTAs per SM (0 = occupancy limit);
+ * icgn_use_lut: 1 = gather a per-frame bicubic LUT from HBM instead of the
+ * staged target window; fftcc_use_tc: 1 = tensor-core FFT-CC when available. */
+TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
+                                     int fftcc_use_tc);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TW_DIC_H */

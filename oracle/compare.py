@@ -1,0 +1,99 @@
+"""TEST INFRASTRUCTURE ONLY: parity checks of GPU results against the oracle.
+
+Parity definition (from the benchmark spec for this path):
+* integer FFT-CC displacements equal the oracle's, except at peaks that tie:
+  an exact tie is two shifts with equal exact (integer) correlation; a
+  rounding tie is a pair whose exact correlation values differ by less than
+  the FP32 DFT rounding bound (`tie_rtol` of the correlation range), where the
+  oracle's own FP32 arithmetic cannot decide the order.  Both are counted and
+  reported; any other mismatch is a failure;
+* sub-pixel u, v within 1e-3 px and displacement gradients within 1e-5 of
+  the oracle's FP32 restatement of the reference CPU path, on POIs both flag
+  Success; flags equal.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import oracle as O
+
+UV_TOL = 1e-3
+GRAD_TOL = 1e-5
+ZNCC_TOL = 1e-5
+
+
+@dataclasses.dataclass
+class FftccReport:
+    n: int
+    mismatches: int
+    exact_ties: int
+    rounding_ties: int
+    unexplained: int
+    max_zncc_err: float
+
+    def ok(self):
+        return self.unexplained == 0 and self.max_zncc_err <= ZNCC_TOL
+
+
+def fftcc_parity(ref, tar, poi, r, u, v, z, u_or, v_or, z_or, st_or, tie_rtol=1e-5) -> FftccReport:
+    ok = st_or == 0
+    mis = ok & ((u != u_or) | (v != v_or))
+    exact = rounding = unexplained = 0
+    n2 = 2 * r
+    for i in np.nonzero(mis)[0]:
+        c = O.exact_surface(ref, tar, poi[i, 0], poi[i, 1], r)
+        a = c[int(v[i]) % n2, int(u[i]) % n2]
+        b = c[int(v_or[i]) % n2, int(u_or[i]) % n2]
+        span = float(c.max() - c.min()) or 1.0
+        if a == b:
+            exact += 1
+        elif abs(float(a) - float(b)) <= tie_rtol * span:
+            rounding += 1
+        else:
+            unexplained += 1
+    same = ok & ~mis
+    zerr = float(np.abs(z[same] - z_or[same]).max()) if same.any() else 0.0
+    return FftccReport(int(ok.sum()), int(mis.sum()), exact, rounding, unexplained, zerr)
+
+
+@dataclasses.dataclass
+class IcgnReport:
+    n: int
+    compared: int
+    flag_mismatch: int
+    iter_mismatch: int
+    max_du: float
+    max_dv: float
+    max_dgrad: float
+    over_uv: int
+    over_grad: int
+
+    def ok(self, grad_tol=GRAD_TOL):
+        return self.flag_mismatch == 0 and self.over_uv == 0 and self.max_dgrad <= grad_tol
+
+
+def icgn_parity(p6, iters, flags, p6_or, iters_or, flags_or, mask=None) -> IcgnReport:
+    m = np.ones(len(flags), bool) if mask is None else mask.copy()
+    fm = int((m & (flags != flags_or)).sum())
+    both = m & (flags == 0) & (flags_or == 0)
+    d = np.abs(p6.astype(np.float64) - p6_or.astype(np.float64))
+    du = float(d[both, 0].max()) if both.any() else 0.0
+    dv = float(d[both, 3].max()) if both.any() else 0.0
+    dg = float(d[both][:, [1, 2, 4, 5]].max()) if both.any() else 0.0
+    over_uv = int(((d[:, 0] > UV_TOL) | (d[:, 3] > UV_TOL))[both].sum())
+    over_g = int((d[:, [1, 2, 4, 5]].max(axis=1) > GRAD_TOL)[both].sum())
+    im = int((both & (iters != iters_or)).sum())
+    return IcgnReport(int(m.sum()), int(both.sum()), fm, im, du, dv, dg, over_uv, over_g)
+
+
+def truth_error(pair, poi, p6, flags):
+    """Error of the sub-pixel result against the imposed synthetic field."""
+    X, Y = poi[:, 1].astype(np.float64), poi[:, 0].astype(np.float64)
+    uu, vv = pair.field(X, Y)
+    ok = flags == 0
+    eu = np.abs(p6[ok, 0] - uu[ok])
+    ev = np.abs(p6[ok, 3] - vv[ok])
+    return dict(mean_abs_u=float(eu.mean()), mean_abs_v=float(ev.mean()), max_abs_u=float(eu.max()),
+                max_abs_v=float(ev.max()), rms=float(np.sqrt(np.mean(eu ** 2 + ev ** 2))))

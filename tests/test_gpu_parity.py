@@ -1,0 +1,189 @@
+"""GPU parity of the C-ABI paths against the oracle (the FP32 restatement of
+the reference CPU path), at sizes the oracle finishes in seconds, plus
+size-independent properties at the full 2048x2048 workload."""
+import numpy as np
+import pytest
+
+from oracle import compare as C
+from oracle import oracle as O
+from tw_gb300 import PATH_FAST, PATH_PLAIN, synth
+from tw_gb300 import dic
+
+pytestmark = pytest.mark.gpu
+
+PATHS = [PATH_PLAIN, PATH_FAST]
+
+
+def params_of(g, path):
+    return dic.make_params(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r,
+                           g.grid, g.grid, g.margin, g.margin, g.max_iter, g.delta_p, path)
+
+
+def oracle_run(pair, g, poi):
+    u, v, z, st = O.fftcc(pair.ref, pair.tar, poi, g.subset_r)
+    p6, it, fl = O.icgn(pair.ref, pair.tar, g, poi, u, v)
+    return u, v, z, st, p6, it, fl
+
+
+@pytest.fixture(scope="module")
+def small():
+    pair, g = synth.small_case()
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    return pair, g, poi, oracle_run(pair, g, poi)
+
+
+@pytest.fixture(scope="module")
+def plain512():
+    pair, g = synth.plain_512()
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    return pair, g, poi, oracle_run(pair, g, poi)
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_fftcc_parity(small, path):
+    pair, g, poi, (u_or, v_or, z_or, st_or, *_rest) = small
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                      g.grid, g.margin, g.margin, path=path)
+    np.testing.assert_array_equal(f.POIPositions(), poi)
+    U, V, Z = f.InitializeFFTCC(pair.ref)
+    st = np.zeros(f.GetNumPOIs(), np.uint8)
+    f.ComputeFFTCC(U, V, Z, pair.tar, status=st)
+    rep = C.fftcc_parity(pair.ref, pair.tar, poi, g.subset_r, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or,
+                         st_or)
+    assert (st == st_or).all()
+    assert rep.ok(), rep
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("case", ["small", "plain512"])
+def test_frame_parity(request, case, path):
+    pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = request.getfixturevalue(case)
+    fr = dic.DICFrame(params_of(g, path))
+    np.testing.assert_array_equal(fr.poi_positions(), poi)
+    fr.set_reference(pair.ref)
+    out = fr.alloc_outputs()
+    fr.process(pair.tar, **out)
+    # compare IC-GN where the GPU's FFT-CC guess equals the oracle's (ties
+    # excepted by the FFT-CC parity test)
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                      g.grid, g.margin, g.margin, path=path)
+    U, V, Z = f.InitializeFFTCC(pair.ref)
+    f.ComputeFFTCC(U, V, Z, pair.tar)
+    same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
+    assert same_start.mean() > 0.99
+    rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start)
+    print(case, path, rep)
+    assert rep.ok(), rep
+    np.testing.assert_array_equal(out["u"], out["p6"][:, 0])
+    np.testing.assert_array_equal(out["v"], out["p6"][:, 3])
+    err = C.truth_error(pair, poi, out["p6"], out["flags"])
+    assert err["max_abs_u"] < 0.05 and err["max_abs_v"] < 0.05, err
+    # second frame with the cached reference gives identical results
+    out2 = fr.alloc_outputs()
+    fr.process(pair.tar, **out2)
+    for k in out:
+        np.testing.assert_array_equal(out[k], out2[k])
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_device_buffers_match_host(small, path):
+    import torch
+    pair, g, poi, _ = small
+    fr = dic.DICFrame(params_of(g, path))
+    fr.set_reference(torch.from_numpy(pair.ref).cuda())
+    host = fr.alloc_outputs()
+    fr.process(pair.tar, **host)
+    dev = fr.alloc_outputs(device="cuda")
+    fr.process(torch.from_numpy(pair.tar).cuda(), **dev)
+    torch.cuda.synchronize()
+    for k in host:
+        np.testing.assert_array_equal(host[k], dev[k].cpu().numpy())
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_icgn_api_with_oracle_guesses(small, path):
+    pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = small
+    n = len(poi)
+    ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r, n, 1,
+                      g.max_iter, g.delta_p, path=path)
+    ic.ResetRefImg(pair.ref)
+    u, v = u_or.copy(), v_or.copy()
+    iters = np.zeros(n, np.int32)
+    p6, fl = ic.ICGN2D_Algorithm(u, v, iters, poi, pair.tar)
+    rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or)
+    assert rep.ok(), rep
+
+
+@pytest.mark.parametrize("path", PATHS)
+def test_icgn_flags_and_counters(small, path):
+    """OutofROI before the first solve leaves the counter untouched; a dark
+    reference flags DarkSubset; a subset outside the ROI is OutofROI."""
+    pair, g, _, _ = small
+    poi = np.array([[80, 96], [80, 96], [80, 96], [5, 5]], np.int32)
+    u0 = np.array([0.0, 200.0, 1.6, 0.0], np.float32)
+    v0 = np.array([0.0, 0.0, -2.4, 0.0], np.float32)
+    ref = pair.ref.copy()
+    ref[60:101, 66:127] = 0  # dark reference subset around POI 2
+    ref2 = ref.copy()
+    ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r, 4, 1,
+                      g.max_iter, g.delta_p, path=path)
+    ic.ResetRefImg(ref2)
+    u, v = u0.copy(), v0.copy()
+    iters = np.full(4, -1, np.int32)
+    p6, fl = ic.ICGN2D_Algorithm(u, v, iters, poi, pair.tar)
+    p6_or, it_or, fl_or = O.icgn(ref2, pair.tar, g, poi, u0, v0, iters_init=-1)
+    np.testing.assert_array_equal(fl, fl_or)
+    np.testing.assert_array_equal(iters, it_or)
+    assert fl[1] == 4 and iters[1] == -1 and u[1] == 200.0
+    assert fl[3] == 4
+
+
+def test_fftcc_dark_subset_untouched(small):
+    pair, g, _, _ = small
+    ref = np.full_like(pair.ref, 50)
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                      g.grid, g.margin, g.margin)
+    U, V, Z = f.InitializeFFTCC(ref)
+    U[:] = -3
+    st = np.zeros(f.GetNumPOIs(), np.uint8)
+    f.ComputeFFTCC(U, V, Z, pair.tar, status=st)
+    assert (st == 1).all() and (U == -3).all()
+
+
+def test_full_size_properties():
+    """2048x2048, 41x41 subsets, step 5 (155,236 POIs): fast vs plain path,
+    fast vs imposed field, and a POI sample against the oracle."""
+    pair, g = synth.scale_2048()
+    res = {}
+    for path in PATHS:
+        fr = dic.DICFrame(params_of(g, path))
+        assert fr.n == 155236
+        fr.set_reference(pair.ref)
+        out = fr.alloc_outputs()
+        fr.process(pair.tar, **out)
+        res[path] = out
+        poi = fr.poi_positions()
+    a, b = res[PATH_FAST], res[PATH_PLAIN]
+    both = (a["flags"] == 0) & (b["flags"] == 0)
+    assert both.mean() > 0.99
+    d = np.abs(a["p6"][both] - b["p6"][both])
+    assert d[:, [0, 3]].max() < 1e-3
+    err = C.truth_error(pair, poi, a["p6"], a["flags"])
+    assert err["rms"] < 0.02, err
+    # oracle on a sample of POIs (its FFT-CC guesses), through the IC-GN API
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(len(poi), 3000, replace=False))
+    sp = poi[idx]
+    u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, sp, g.subset_r)
+    p6_or, it_or, fl_or = O.icgn(pair.ref, pair.tar, g, sp, u_or, v_or)
+    for path in PATHS:
+        ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r,
+                          len(sp), 1, g.max_iter, g.delta_p, path=path)
+        ic.ResetRefImg(pair.ref)
+        u, v = u_or.copy(), v_or.copy()
+        iters = np.zeros(len(sp), np.int32)
+        p6, fl = ic.ICGN2D_Algorithm(u, v, iters, sp, pair.tar)
+        rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or)
+        assert rep.ok(), (path, rep)

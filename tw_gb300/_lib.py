@@ -1,0 +1,117 @@
+"""ctypes binding of libtwdic.so (the C ABI declared in include/tw_dic.h).
+
+Loading fails loudly when the library has not been built: there is no
+CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtwdic.so")
+
+OK = 0
+ERR = {
+    -1: "TWDIC_ERR_INVALID_ARG",
+    -2: "TWDIC_ERR_NO_POI",
+    -3: "TWDIC_ERR_BORDER",
+    -4: "TWDIC_ERR_STATE",
+    -5: "TWDIC_ERR_CUDA",
+    -6: "TWDIC_ERR_NO_MEMORY",
+    -7: "TWDIC_ERR_UNSUPPORTED",
+    -8: "TWDIC_ERR_TIMEOUT",
+}
+MEM_HOST = 0
+MEM_DEVICE = 1
+PATH_PLAIN = 0
+PATH_FAST = 1
+
+# every symbol include/tw_dic.h declares
+EXPORTED = (
+    "twdic_last_error", "twdic_abi_version", "twdic_num_pois", "twdic_poi_positions",
+    "twdic_fftcc_create", "twdic_fftcc_num_pois", "twdic_fftcc_poi_positions", "twdic_fftcc_reset_ref",
+    "twdic_fftcc_set_tar", "twdic_fftcc_compute", "twdic_fftcc_destroy",
+    "twdic_icgn_create", "twdic_icgn_reset_ref", "twdic_icgn_compute", "twdic_icgn_destroy",
+    "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
+    "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
+    "twdic_frame_set_tuning",
+)
+
+
+class TWDICError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERR.get(code, code)}: {message}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("img_width", ctypes.c_int32), ("img_height", ctypes.c_int32),
+        ("start_x", ctypes.c_int32), ("start_y", ctypes.c_int32),
+        ("roi_width", ctypes.c_int32), ("roi_height", ctypes.c_int32),
+        ("subset_x", ctypes.c_int32), ("subset_y", ctypes.c_int32),
+        ("grid_space_x", ctypes.c_int32), ("grid_space_y", ctypes.c_int32),
+        ("margin_x", ctypes.c_int32), ("margin_y", ctypes.c_int32),
+        ("max_iterations", ctypes.c_int32),
+        ("delta_p", ctypes.c_float),
+        ("path", ctypes.c_int32),
+    ]
+
+
+_lib = None
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_I32P = ctypes.POINTER(ctypes.c_int32)
+
+
+def load():
+    """Load libtwdic.so; raises if it is missing (build it with tw_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER(Params)
+    sig = {
+        "twdic_last_error": ([], ctypes.c_char_p),
+        "twdic_abi_version": ([], _I),
+        "twdic_num_pois": ([P, _I32P, _I32P], _I),
+        "twdic_poi_positions": ([P, _VP], _I),
+        "twdic_fftcc_create": ([P, ctypes.POINTER(_VP)], _I),
+        "twdic_fftcc_num_pois": ([_VP, _I32P, _I32P], _I),
+        "twdic_fftcc_poi_positions": ([_VP, _VP, _I], _I),
+        "twdic_fftcc_reset_ref": ([_VP, _VP, ctypes.c_int32, _I], _I),
+        "twdic_fftcc_set_tar": ([_VP, _VP, ctypes.c_int32, _I], _I),
+        "twdic_fftcc_compute": ([_VP, _VP, _VP, _VP, _VP, _I], _I),
+        "twdic_fftcc_destroy": ([_VP], _I),
+        "twdic_icgn_create": ([P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)], _I),
+        "twdic_icgn_reset_ref": ([_VP, _VP, ctypes.c_int32, _I], _I),
+        "twdic_icgn_compute": ([_VP, _VP, ctypes.c_int32, _VP, _I, _VP, _VP, _VP, _VP, _VP, _I], _I),
+        "twdic_icgn_destroy": ([_VP], _I),
+        "twdic_frame_create": ([P, ctypes.POINTER(_VP)], _I),
+        "twdic_frame_num_pois": ([_VP, _I32P, _I32P], _I),
+        "twdic_frame_poi_positions": ([_VP, _VP, _I], _I),
+        "twdic_frame_set_reference": ([_VP, _VP, ctypes.c_int32, _I], _I),
+        "twdic_frame_process": ([_VP, _VP, ctypes.c_int32, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I], _I),
+        "twdic_frame_set_stream": ([_VP, _VP], _I),
+        "twdic_frame_phase_times": ([_VP, _VP], _I),
+        "twdic_frame_destroy": ([_VP], _I),
+        "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(rc: int):
+    if rc != OK:
+        msg = load().twdic_last_error()
+        raise TWDICError(rc, msg.decode() if msg else "")
+    return rc

@@ -1,0 +1,596 @@
+// C ABI of the GB300 DIC hot path (declared in include/tw_dic.h).
+//
+// Host orchestration in C++: parameter validation with the reference's error
+// conditions turned into status codes, device buffers owned by the handles,
+// host<->device staging on the handle's stream, and the per-reference cache.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dic_common.cuh"
+#include "dic_kernels.h"
+#include "../../include/tw_dic.h"
+
+namespace twdic {
+namespace {
+
+thread_local std::string g_last_error = "no error";
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define TW_CUDA(call)                                                                                   \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(e_ == cudaErrorMemoryAllocation ? TWDIC_ERR_NO_MEMORY : TWDIC_ERR_CUDA,         \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
+    } while (0)
+
+#define TW_TRY(expr)                 \
+    do {                             \
+        int r_ = (expr);             \
+        if (r_ != TWDIC_OK) return r_; \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t b) {
+        if (b <= bytes && p) return TWDIC_OK;
+        release();
+        if (b == 0) return TWDIC_OK;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && b + (size_t(256) << 20) > free_b)
+            return fail(TWDIC_ERR_NO_MEMORY, "device budget: %zu bytes requested, %zu free", b, free_b);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(TWDIC_ERR_NO_MEMORY, "cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+        }
+        bytes = b;
+        return TWDIC_OK;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+int num_pois_of(const twdic_params& p, int* nx, int* ny) {
+    // Fftcc2D::recomputeNumPOI (TW_paDIC_FFTCC2D.cpp:88-94)
+    *nx = int(std::floor((p.roi_width - p.subset_x * 2 - p.margin_x * 2) / float(p.grid_space_x))) + 1;
+    *ny = int(std::floor((p.roi_height - p.subset_y * 2 - p.margin_y * 2) / float(p.grid_space_y))) + 1;
+    return (*nx > 0 && *ny > 0) ? TWDIC_OK : fail(TWDIC_ERR_NO_POI, "Number of POIs is below 0!");
+}
+
+int validate(const twdic_params* p, bool need_grid, bool need_border) {
+    if (!p) return fail(TWDIC_ERR_INVALID_ARG, "params is NULL");
+    if (p->img_width <= 0 || p->img_height <= 0) return fail(TWDIC_ERR_INVALID_ARG, "image size must be positive");
+    if (p->roi_width <= 0 || p->roi_height <= 0) return fail(TWDIC_ERR_INVALID_ARG, "ROI size must be positive");
+    if (p->start_x < 0 || p->start_y < 0 || p->start_x + p->roi_width > p->img_width ||
+        p->start_y + p->roi_height > p->img_height)
+        return fail(TWDIC_ERR_INVALID_ARG, "ROI lies outside the image");
+    if (p->subset_x < 1 || p->subset_y < 1) return fail(TWDIC_ERR_INVALID_ARG, "subset half size must be >= 1");
+    if (p->subset_x > 31 || p->subset_y > 31)
+        return fail(TWDIC_ERR_UNSUPPORTED, "subset half size %d x %d exceeds 31", p->subset_x, p->subset_y);
+    if (p->path != TWDIC_PATH_PLAIN && p->path != TWDIC_PATH_FAST)
+        return fail(TWDIC_ERR_INVALID_ARG, "unknown path %d", p->path);
+    if (need_grid) {
+        if (p->grid_space_x < 1 || p->grid_space_y < 1) return fail(TWDIC_ERR_INVALID_ARG, "grid space must be >= 1");
+        if (p->margin_x < 0 || p->margin_y < 0) return fail(TWDIC_ERR_INVALID_ARG, "margin must be >= 0");
+    }
+    if (need_border) {
+        if (p->max_iterations < 1) return fail(TWDIC_ERR_INVALID_ARG, "max_iterations must be >= 1");
+        if (!(p->delta_p >= 0.f)) return fail(TWDIC_ERR_INVALID_ARG, "delta_p must be >= 0");
+        // GradientXY_2Images / BicubicCoefficients (TW_utils.cpp:254-257, :615-619)
+        if (p->start_x < 1 || p->start_y < 1 || p->start_x + p->roi_width + 1 > p->img_width ||
+            p->start_y + p->roi_height + 1 > p->img_height)
+            return fail(TWDIC_ERR_BORDER, "Not enough boundary pixels for gradients!");
+    }
+    return TWDIC_OK;
+}
+
+Geom make_geom(const twdic_params& p) {
+    Geom g;
+    g.img_w = p.img_width; g.img_h = p.img_height; g.pitch = p.img_width;
+    g.sx = p.start_x; g.sy = p.start_y; g.rw = p.roi_width; g.rh = p.roi_height;
+    g.rx = p.subset_x; g.ry = p.subset_y;
+    g.max_iter = p.max_iterations; g.delta_p = p.delta_p;
+    return g;
+}
+
+void grid_positions(const twdic_params& p, int nx, int ny, int32_t* yx) {
+    // ComputePOIPositions_s (TW_utils.cpp:29-49)
+    for (int i = 0; i < ny; ++i)
+        for (int j = 0; j < nx; ++j) {
+            yx[2 * ((size_t)i * nx + j) + 0] = p.start_y + p.margin_y + p.subset_y + i * p.grid_space_y;
+            yx[2 * ((size_t)i * nx + j) + 1] = p.start_x + p.margin_x + p.subset_x + j * p.grid_space_x;
+        }
+}
+
+// -------------------------------------------------------------- Engine ----
+struct Engine {
+    twdic_params prm{};
+    Geom g{};
+    int n = 0;  // POIs of the handle
+    int nx = 0, ny = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    bool have_ref = false, have_tar = false;
+    IcgnTune icgn_tune;
+    FftccTune fftcc_tune;
+
+    DevBuf d_ref, d_tar, d_poi;
+    DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work;
+    // per-reference cache
+    bool cache_valid = false;
+    const void* cache_poi_key = nullptr;
+    std::vector<int32_t> cache_poi_host;
+    DevBuf c_subR, c_sd, c_chol, c_norm, c_flag;  // plain
+    DevBuf c_stat, c_chol64, c_flag64;            // fast
+    DevBuf d_lut;
+    cudaEvent_t ev[7] = {};
+    float last_times[6] = {0, 0, 0, 0, 0, 0};
+    bool times_pending = false;
+
+    ~Engine() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+
+    int init(const twdic_params& p, int num_pois) {
+        prm = p;
+        g = make_geom(p);
+        n = num_pois;
+        TW_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
+        stream = own_stream;
+        for (auto& e : ev) TW_CUDA(cudaEventCreate(&e));
+        const size_t img = (size_t)p.img_width * p.img_height;
+        TW_TRY(d_ref.ensure(img));
+        TW_TRY(d_tar.ensure(img));
+        TW_TRY(d_poi.ensure(sizeof(int2) * (size_t)n));
+        TW_TRY(d_u.ensure(sizeof(float) * (size_t)n));
+        TW_TRY(d_v.ensure(sizeof(float) * (size_t)n));
+        TW_TRY(d_zncc.ensure(sizeof(float) * (size_t)n));
+        TW_TRY(d_fst.ensure((size_t)n));
+        TW_TRY(d_p6.ensure(sizeof(float) * 6 * (size_t)n));
+        TW_TRY(d_iters.ensure(sizeof(int) * (size_t)n));
+        TW_TRY(d_flags.ensure((size_t)n));
+        TW_TRY(d_err.ensure(sizeof(unsigned)));
+        TW_TRY(d_work.ensure(sizeof(int) * 4));
+        TW_CUDA(cudaMemsetAsync(d_err.p, 0, sizeof(unsigned), stream));
+        return TWDIC_OK;
+    }
+
+    int upload_image(DevBuf& dst, const uint8_t* img, int32_t stride, int mem) {
+        if (!img) return fail(TWDIC_ERR_INVALID_ARG, "image pointer is NULL");
+        if (stride == 0) stride = prm.img_width;
+        if (stride < prm.img_width) return fail(TWDIC_ERR_INVALID_ARG, "stride %d < width %d", stride, prm.img_width);
+        if (mem != TWDIC_MEM_HOST && mem != TWDIC_MEM_DEVICE) return fail(TWDIC_ERR_INVALID_ARG, "bad mem kind");
+        TW_CUDA(cudaMemcpy2DAsync(dst.p, prm.img_width, img, stride, prm.img_width, prm.img_height,
+                                  mem == TWDIC_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, stream));
+        return TWDIC_OK;
+    }
+
+    int set_ref(const uint8_t* img, int32_t stride, int mem) {
+        TW_TRY(upload_image(d_ref, img, stride, mem));
+        have_ref = true;
+        cache_valid = false;
+        return TWDIC_OK;
+    }
+
+    int set_tar(const uint8_t* img, int32_t stride, int mem) {
+        TW_TRY(upload_image(d_tar, img, stride, mem));
+        have_tar = true;
+        return TWDIC_OK;
+    }
+
+    int check_err() {
+        unsigned h = 0;
+        TW_CUDA(cudaMemcpyAsync(&h, d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+        TW_CUDA(cudaStreamSynchronize(stream));
+        if (h & kErrTimeout) {
+            cudaMemsetAsync(d_err.p, 0, sizeof(unsigned), stream);
+            return fail(TWDIC_ERR_TIMEOUT, "a bounded device-side wait gave up");
+        }
+        return TWDIC_OK;
+    }
+
+    // FFT-CC of all POIs into device arrays.
+    int fftcc(float* u, float* v, float* z, uint8_t* st) {
+        if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "FFT-CC needs a reference and a target image");
+        const int2* poi = d_poi.as<int2>();
+        if (prm.path == TWDIC_PATH_FAST && fftcc_tune.use_tc && fftcc_tc_supported(g)) {
+            TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st,
+                                    d_err.as<unsigned>(), stream));
+        } else {
+            TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st, stream));
+        }
+        return TWDIC_OK;
+    }
+
+    int ensure_cache(float* t_pre) {
+        if (cache_valid) return TWDIC_OK;
+        const int S = (2 * g.rx + 1) * (2 * g.ry + 1);
+        if (prm.path == TWDIC_PATH_PLAIN) {
+            TW_TRY(c_subR.ensure(sizeof(float) * (size_t)n * S));
+            TW_TRY(c_sd.ensure(sizeof(float2) * 3 * (size_t)n * S));
+            TW_TRY(c_chol.ensure(sizeof(float) * 36 * (size_t)n));
+            TW_TRY(c_norm.ensure(sizeof(float) * (size_t)n));
+            TW_TRY(c_flag.ensure((size_t)n));
+            TW_CUDA(launch_ref_precompute_plain(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_subR.as<float>(),
+                                                c_sd.as<float2>(), c_chol.as<float>(), c_norm.as<float>(),
+                                                c_flag.as<uint8_t>(), stream));
+        } else {
+            TW_TRY(c_stat.ensure(sizeof(float2) * (size_t)n));
+            TW_TRY(c_chol64.ensure(sizeof(double) * 21 * (size_t)n));
+            TW_TRY(c_flag64.ensure((size_t)n));
+            TW_CUDA(launch_ref_precompute_fast(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_stat.as<float2>(),
+                                               c_chol64.as<double>(), c_flag64.as<uint8_t>(), stream));
+        }
+        cache_valid = true;
+        if (t_pre) *t_pre = 1.f;
+        return TWDIC_OK;
+    }
+
+    // IC-GN of all POIs; u, v in/out device arrays.
+    int icgn(float* u, float* v, float* p6, int* iters, uint8_t* flags) {
+        if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
+        TW_TRY(ensure_cache(nullptr));
+        const int2* poi = d_poi.as<int2>();
+        if (prm.path == TWDIC_PATH_PLAIN) {
+            TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
+            TW_CUDA(launch_icgn_plain(g, d_tar.as<uint8_t>(), poi, n, c_subR.as<float>(), c_sd.as<float2>(),
+                                      c_chol.as<float>(), c_norm.as<float>(), c_flag.as<uint8_t>(),
+                                      d_lut.as<float4>(), u, v, p6, iters, flags, stream));
+        } else {
+            if (icgn_tune.use_lut) {
+                TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
+                TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
+            }
+            TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float2>(),
+                                     c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.as<float4>(),
+                                     d_work.as<int>(), u, v, p6, iters, flags, icgn_tune, stream));
+        }
+        return TWDIC_OK;
+    }
+};
+
+int copy_in(void* dst, const void* src, size_t bytes, int mem, cudaStream_t st) {
+    if (!src || bytes == 0) return TWDIC_OK;
+    TW_CUDA(cudaMemcpyAsync(dst, src, bytes, mem == TWDIC_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                            st));
+    return TWDIC_OK;
+}
+int copy_out(void* dst, const void* src, size_t bytes, int mem, cudaStream_t st) {
+    if (!dst || bytes == 0) return TWDIC_OK;
+    TW_CUDA(cudaMemcpyAsync(dst, src, bytes, mem == TWDIC_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                            st));
+    return TWDIC_OK;
+}
+int check_mem(int mem) {
+    return (mem == TWDIC_MEM_HOST || mem == TWDIC_MEM_DEVICE) ? TWDIC_OK
+                                                               : fail(TWDIC_ERR_INVALID_ARG, "bad mem kind %d", mem);
+}
+
+}  // namespace
+}  // namespace twdic
+
+using namespace twdic;
+
+struct twdic_fftcc { Engine e; };
+struct twdic_icgn { Engine e; };
+struct twdic_frame { Engine e; };
+
+extern "C" {
+
+const char* twdic_last_error(void) { return g_last_error.c_str(); }
+int twdic_abi_version(void) { return TWDIC_ABI_VERSION; }
+
+int twdic_num_pois(const twdic_params* p, int32_t* num_x, int32_t* num_y) {
+    TW_TRY(validate(p, true, false));
+    if (!num_x || !num_y) return fail(TWDIC_ERR_INVALID_ARG, "NULL output");
+    int nx, ny;
+    TW_TRY(num_pois_of(*p, &nx, &ny));
+    *num_x = nx;
+    *num_y = ny;
+    return TWDIC_OK;
+}
+
+int twdic_poi_positions(const twdic_params* p, int32_t* poi_yx) {
+    int32_t nx, ny;
+    TW_TRY(twdic_num_pois(p, &nx, &ny));
+    if (!poi_yx) return fail(TWDIC_ERR_INVALID_ARG, "NULL output");
+    grid_positions(*p, nx, ny, poi_yx);
+    return TWDIC_OK;
+}
+
+static int engine_grid_init(Engine& e, const twdic_params* p, bool border) {
+    TW_TRY(validate(p, true, border));
+    int nx, ny;
+    TW_TRY(num_pois_of(*p, &nx, &ny));
+    if ((size_t)nx * ny > (size_t)1 << 30) return fail(TWDIC_ERR_UNSUPPORTED, "too many POIs");
+    e.nx = nx;
+    e.ny = ny;
+    TW_TRY(e.init(*p, nx * ny));
+    std::vector<int32_t> yx(2 * (size_t)nx * ny);
+    grid_positions(*p, nx, ny, yx.data());
+    TW_CUDA(cudaMemcpyAsync(e.d_poi.p, yx.data(), yx.size() * 4, cudaMemcpyHostToDevice, e.stream));
+    TW_CUDA(cudaStreamSynchronize(e.stream));
+    return TWDIC_OK;
+}
+
+// ------------------------------------------------------------ FFT-CC ABI --
+int twdic_fftcc_create(const twdic_params* p, twdic_fftcc** out) {
+    if (!out) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle output");
+    *out = nullptr;
+    auto* h = new (std::nothrow) twdic_fftcc;
+    if (!h) return fail(TWDIC_ERR_NO_MEMORY, "host allocation failed");
+    int r = engine_grid_init(h->e, p, false);
+    if (r != TWDIC_OK) { delete h; return r; }
+    *out = h;
+    return TWDIC_OK;
+}
+int twdic_fftcc_num_pois(const twdic_fftcc* h, int32_t* num_x, int32_t* num_y) {
+    if (!h || !num_x || !num_y) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    *num_x = h->e.nx;
+    *num_y = h->e.ny;
+    return TWDIC_OK;
+}
+int twdic_fftcc_poi_positions(const twdic_fftcc* h, int32_t* poi_yx, int mem) {
+    if (!h || !poi_yx) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem));
+    TW_TRY(copy_out(poi_yx, h->e.d_poi.p, sizeof(int2) * (size_t)h->e.n, mem, h->e.stream));
+    TW_CUDA(cudaStreamSynchronize(h->e.stream));
+    return TWDIC_OK;
+}
+int twdic_fftcc_reset_ref(twdic_fftcc* h, const uint8_t* img, int32_t stride, int mem) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return h->e.set_ref(img, stride, mem);
+}
+int twdic_fftcc_set_tar(twdic_fftcc* h, const uint8_t* img, int32_t stride, int mem) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return h->e.set_tar(img, stride, mem);
+}
+int twdic_fftcc_compute(twdic_fftcc* h, float* u, float* v, float* zncc, uint8_t* status, int mem) {
+    if (!h || !u || !v || !zncc) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem));
+    Engine& e = h->e;
+    const size_t fb = sizeof(float) * (size_t)e.n;
+    float *du = u, *dv = v, *dz = zncc;
+    uint8_t* ds = (mem == TWDIC_MEM_DEVICE && status) ? status : e.d_fst.as<uint8_t>();
+    if (mem == TWDIC_MEM_HOST) {
+        // dark subsets leave their outputs untouched: stage the caller's values
+        du = e.d_u.as<float>(); dv = e.d_v.as<float>(); dz = e.d_zncc.as<float>();
+        TW_TRY(copy_in(du, u, fb, mem, e.stream));
+        TW_TRY(copy_in(dv, v, fb, mem, e.stream));
+        TW_TRY(copy_in(dz, zncc, fb, mem, e.stream));
+    }
+    TW_TRY(e.fftcc(du, dv, dz, ds));
+    if (mem == TWDIC_MEM_HOST) {
+        TW_TRY(copy_out(u, du, fb, mem, e.stream));
+        TW_TRY(copy_out(v, dv, fb, mem, e.stream));
+        TW_TRY(copy_out(zncc, dz, fb, mem, e.stream));
+        TW_TRY(copy_out(status, ds, (size_t)e.n, mem, e.stream));
+    }
+    return e.check_err();
+}
+int twdic_fftcc_destroy(twdic_fftcc* h) {
+    delete h;
+    return TWDIC_OK;
+}
+
+// ------------------------------------------------------------- IC-GN ABI --
+int twdic_icgn_create(const twdic_params* p, int32_t num_x, int32_t num_y, twdic_icgn** out) {
+    if (!out) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle output");
+    *out = nullptr;
+    TW_TRY(validate(p, false, true));
+    if (num_x <= 0 || num_y <= 0) return fail(TWDIC_ERR_NO_POI, "Number of POIs is below 0!");
+    if ((size_t)num_x * num_y > (size_t)1 << 30) return fail(TWDIC_ERR_UNSUPPORTED, "too many POIs");
+    auto* h = new (std::nothrow) twdic_icgn;
+    if (!h) return fail(TWDIC_ERR_NO_MEMORY, "host allocation failed");
+    h->e.nx = num_x;
+    h->e.ny = num_y;
+    int r = h->e.init(*p, num_x * num_y);
+    if (r != TWDIC_OK) { delete h; return r; }
+    *out = h;
+    return TWDIC_OK;
+}
+int twdic_icgn_reset_ref(twdic_icgn* h, const uint8_t* img, int32_t stride, int mem) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return h->e.set_ref(img, stride, mem);
+}
+int twdic_icgn_compute(twdic_icgn* h, const uint8_t* tar, int32_t stride, const int32_t* poi_yx, int mem_in,
+                       float* u, float* v, float* p6, int32_t* iters, uint8_t* flags, int mem_out) {
+    if (!h || !tar || !poi_yx || !u || !v) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem_in));
+    TW_TRY(check_mem(mem_out));
+    Engine& e = h->e;
+    const size_t n = (size_t)e.n;
+    TW_TRY(e.set_tar(tar, stride, mem_in));
+    // POIs: the per-reference cache is keyed on their contents (host) or on
+    // the array's address (device).
+    if (mem_in == TWDIC_MEM_HOST) {
+        if (e.cache_poi_host.size() != 2 * n || std::memcmp(e.cache_poi_host.data(), poi_yx, 8 * n) != 0) {
+            e.cache_poi_host.assign(poi_yx, poi_yx + 2 * n);
+            TW_TRY(copy_in(e.d_poi.p, poi_yx, 8 * n, mem_in, e.stream));
+            e.cache_valid = false;
+        }
+    } else if (e.cache_poi_key != poi_yx) {
+        TW_TRY(copy_in(e.d_poi.p, poi_yx, 8 * n, mem_in, e.stream));
+        e.cache_poi_key = poi_yx;
+        e.cache_poi_host.clear();
+        e.cache_valid = false;
+    }
+    float *du = u, *dv = v, *dp6 = p6 ? p6 : e.d_p6.as<float>();
+    int* dit = iters;
+    uint8_t* dfl = flags ? flags : e.d_flags.as<uint8_t>();
+    if (mem_out == TWDIC_MEM_HOST) {
+        du = e.d_u.as<float>(); dv = e.d_v.as<float>(); dp6 = e.d_p6.as<float>();
+        dit = e.d_iters.as<int>(); dfl = e.d_flags.as<uint8_t>();
+        TW_TRY(copy_in(du, u, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_in(dv, v, 4 * n, mem_out, e.stream));
+        if (iters) TW_TRY(copy_in(dit, iters, 4 * n, mem_out, e.stream));
+        else TW_CUDA(cudaMemsetAsync(dit, 0, 4 * n, e.stream));
+    } else if (!iters) {
+        dit = e.d_iters.as<int>();
+        TW_CUDA(cudaMemsetAsync(dit, 0, 4 * n, e.stream));
+    }
+    TW_TRY(e.icgn(du, dv, dp6, dit, dfl));
+    if (mem_out == TWDIC_MEM_HOST) {
+        TW_TRY(copy_out(u, du, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(v, dv, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(p6, dp6, 24 * n, mem_out, e.stream));
+        TW_TRY(copy_out(iters, dit, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(flags, dfl, n, mem_out, e.stream));
+    }
+    return e.check_err();
+}
+int twdic_icgn_destroy(twdic_icgn* h) {
+    delete h;
+    return TWDIC_OK;
+}
+
+// ------------------------------------------------------------- frame ABI --
+int twdic_frame_create(const twdic_params* p, twdic_frame** out) {
+    if (!out) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle output");
+    *out = nullptr;
+    auto* h = new (std::nothrow) twdic_frame;
+    if (!h) return fail(TWDIC_ERR_NO_MEMORY, "host allocation failed");
+    int r = engine_grid_init(h->e, p, true);
+    if (r != TWDIC_OK) { delete h; return r; }
+    *out = h;
+    return TWDIC_OK;
+}
+int twdic_frame_num_pois(const twdic_frame* h, int32_t* num_x, int32_t* num_y) {
+    if (!h || !num_x || !num_y) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    *num_x = h->e.nx;
+    *num_y = h->e.ny;
+    return TWDIC_OK;
+}
+int twdic_frame_poi_positions(const twdic_frame* h, int32_t* poi_yx, int mem) {
+    if (!h || !poi_yx) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem));
+    TW_TRY(copy_out(poi_yx, h->e.d_poi.p, sizeof(int2) * (size_t)h->e.n, mem, h->e.stream));
+    TW_CUDA(cudaStreamSynchronize(h->e.stream));
+    return TWDIC_OK;
+}
+int twdic_frame_set_reference(twdic_frame* h, const uint8_t* img, int32_t stride, int mem) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return h->e.set_ref(img, stride, mem);
+}
+int twdic_frame_set_stream(twdic_frame* h, void* stream) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    h->e.stream = stream ? static_cast<cudaStream_t>(stream) : h->e.own_stream;
+    return TWDIC_OK;
+}
+int twdic_frame_process(twdic_frame* h, const uint8_t* tar, int32_t stride, int mem_in, float* u, float* v,
+                        float* zncc, float* p6, int32_t* iters, uint8_t* flags, int mem_out) {
+    if (!h || !tar || !u || !v) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem_in));
+    TW_TRY(check_mem(mem_out));
+    Engine& e = h->e;
+    if (!e.have_ref) return fail(TWDIC_ERR_STATE, "no reference image set");
+    const size_t n = (size_t)e.n;
+    const bool dev = mem_out == TWDIC_MEM_DEVICE;
+    float* du = dev ? u : e.d_u.as<float>();
+    float* dv = dev ? v : e.d_v.as<float>();
+    float* dz = (dev && zncc) ? zncc : e.d_zncc.as<float>();
+    float* dp6 = (dev && p6) ? p6 : e.d_p6.as<float>();
+    int* dit = (dev && iters) ? iters : e.d_iters.as<int>();
+    uint8_t* dfl = (dev && flags) ? flags : e.d_flags.as<uint8_t>();
+    TW_CUDA(cudaEventRecord(e.ev[0], e.stream));
+    TW_TRY(e.set_tar(tar, stride, mem_in));
+    TW_CUDA(cudaEventRecord(e.ev[1], e.stream));
+    const bool cached = e.cache_valid;
+    TW_TRY(e.ensure_cache(nullptr));
+    TW_CUDA(cudaEventRecord(e.ev[2], e.stream));
+    // a frame starts from zero displacements for dark FFT-CC subsets and a
+    // zero iteration count, as a freshly calloc'd reference buffer would
+    TW_CUDA(cudaMemsetAsync(du, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(dv, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(dz, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(dit, 0, 4 * n, e.stream));
+    TW_TRY(e.fftcc(du, dv, dz, e.d_fst.as<uint8_t>()));
+    TW_CUDA(cudaEventRecord(e.ev[3], e.stream));
+    TW_TRY(e.icgn(du, dv, dp6, dit, dfl));
+    TW_CUDA(cudaEventRecord(e.ev[4], e.stream));
+    if (!dev) {
+        TW_TRY(copy_out(u, du, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(v, dv, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(zncc, dz, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(p6, dp6, 24 * n, mem_out, e.stream));
+        TW_TRY(copy_out(iters, dit, 4 * n, mem_out, e.stream));
+        TW_TRY(copy_out(flags, dfl, n, mem_out, e.stream));
+    }
+    TW_CUDA(cudaEventRecord(e.ev[5], e.stream));
+    e.times_pending = true;
+    e.last_times[5] = cached ? -1.f : 0.f;
+    if (!dev) return e.check_err();
+    return TWDIC_OK;
+}
+int twdic_frame_phase_times(const twdic_frame* hc, float* t6) {
+    if (!hc || !t6) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    auto* h = const_cast<twdic_frame*>(hc);
+    Engine& e = h->e;
+    if (e.times_pending) {
+        TW_CUDA(cudaEventSynchronize(e.ev[5]));
+        float a = 0, b = 0, c = 0, d = 0, f = 0;
+        TW_CUDA(cudaEventElapsedTime(&a, e.ev[0], e.ev[1]));
+        TW_CUDA(cudaEventElapsedTime(&f, e.ev[1], e.ev[2]));
+        TW_CUDA(cudaEventElapsedTime(&b, e.ev[2], e.ev[3]));
+        TW_CUDA(cudaEventElapsedTime(&c, e.ev[3], e.ev[4]));
+        TW_CUDA(cudaEventElapsedTime(&d, e.ev[4], e.ev[5]));
+        const bool cached = e.last_times[5] < 0.f;
+        e.last_times[0] = a;
+        e.last_times[1] = b;
+        e.last_times[2] = 0.f;  // target preparation is inside the IC-GN phase
+        e.last_times[3] = c;
+        e.last_times[4] = d;
+        e.last_times[5] = cached ? 0.f : f;
+        e.times_pending = false;
+    }
+    for (int i = 0; i < 6; ++i) t6[i] = e.last_times[i];
+    return TWDIC_OK;
+}
+int twdic_frame_destroy(twdic_frame* h) {
+    delete h;
+    return TWDIC_OK;
+}
+
+// Tuning (internal to the Python autotuner; not part of the reference interface).
+int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
+                           int fftcc_use_tc) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (icgn_threads != 128 && icgn_threads != 256) return fail(TWDIC_ERR_INVALID_ARG, "threads must be 128 or 256");
+    h->e.icgn_tune.threads = icgn_threads;
+    h->e.icgn_tune.ctas_per_sm = icgn_ctas_per_sm;
+    h->e.icgn_tune.use_lut = icgn_use_lut;
+    h->e.fftcc_tune.use_tc = fftcc_use_tc;
+    return TWDIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,48 @@
+// Kernel launchers of the DIC hot path (internal to libtwdic).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "dic_common.cuh"
+
+namespace twdic {
+
+// Launch shape of the fast IC-GN kernel, chosen by the autotuner.
+struct IcgnTune {
+    int threads = 128;    // 128 or 256 threads per CTA (one POI per CTA at a time)
+    int ctas_per_sm = 0;  // persistent CTAs per SM (0 = occupancy limit)
+    int use_lut = 0;      // 1: gather the per-frame LUT from HBM instead of the staged window
+};
+
+// Launch shape of the tensor-core FFT-CC kernel.
+struct FftccTune {
+    int use_tc = 1;       // 0: FP32 SIMT DFT kernel
+};
+
+// ---- plain FP32 path (kernels_plain.cu)
+cudaError_t launch_fftcc_plain(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
+                               float* u, float* v, float* zncc, uint8_t* status, cudaStream_t st);
+cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* subR,
+                                        float2* sd, float* chol, float* refnorm, uint8_t* rflag, cudaStream_t st);
+cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
+cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi, int n, const float* subR,
+                              const float2* sd, const float* chol, const float* refnorm, const uint8_t* rflag,
+                              const float4* lut, float* u, float* v, float* p6, int* iters, uint8_t* flags,
+                              cudaStream_t st);
+
+// ---- fast IC-GN (kernels_icgn_fast.cu)
+cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float2* refstat,
+                                       double* chol, uint8_t* rflag, cudaStream_t st);
+cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
+                             const float2* refstat, const double* chol, const uint8_t* rflag, const float4* lut,
+                             int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
+                             const IcgnTune& tune, cudaStream_t st);
+int icgn_fast_window(const Geom& g);
+
+// ---- tensor-core FFT-CC (kernels_fftcc_tc.cu)
+cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st);
+bool fftcc_tc_supported(const Geom& g);
+
+}  // namespace twdic

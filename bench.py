@@ -248,10 +248,18 @@ def pct(xs, q):
 
 def run_gpu(args, world, rank, local):
     import torch
-    from tw_gb300 import PATH_FAST, PATH_PLAIN, dic
     from tw_gb300.build import build
     build()
     torch.cuda.set_device(local)
+    # every launch of the run (L2 flush, frames, CUDA events) goes to one
+    # non-default stream that the DIC handles are bound to
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        return _run_gpu(args, world, rank, local, torch)
+
+
+def _run_gpu(args, world, rank, local, torch):
+    from tw_gb300 import PATH_FAST, PATH_PLAIN, dic
     pair, g = workload()
     P = None
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2

@@ -121,12 +121,11 @@ def test_icgn_flags_and_counters(small, path):
     """OutofROI before the first solve leaves the counter untouched; a dark
     reference flags DarkSubset; a subset outside the ROI is OutofROI."""
     pair, g, _, _ = small
-    poi = np.array([[80, 96], [80, 96], [80, 96], [5, 5]], np.int32)
-    u0 = np.array([0.0, 200.0, 1.6, 0.0], np.float32)
-    v0 = np.array([0.0, 0.0, -2.4, 0.0], np.float32)
-    ref = pair.ref.copy()
-    ref[60:101, 66:127] = 0  # dark reference subset around POI 2
-    ref2 = ref.copy()
+    poi = np.array([[80, 96], [80, 96], [40, 150], [5, 5]], np.int32)
+    u0 = np.array([1.6, 200.0, 1.6, 0.0], np.float32)
+    v0 = np.array([-2.4, 0.0, -2.4, 0.0], np.float32)
+    ref2 = pair.ref.copy()
+    ref2[25:56, 135:166] = 0  # dark reference subset around POI 2
     ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r, 4, 1,
                       g.max_iter, g.delta_p, path=path)
     ic.ResetRefImg(ref2)
@@ -136,7 +135,9 @@ def test_icgn_flags_and_counters(small, path):
     p6_or, it_or, fl_or = O.icgn(ref2, pair.tar, g, poi, u0, v0, iters_init=-1)
     np.testing.assert_array_equal(fl, fl_or)
     np.testing.assert_array_equal(iters, it_or)
+    assert fl[0] == 0 and iters[0] >= 1
     assert fl[1] == 4 and iters[1] == -1 and u[1] == 200.0
+    assert fl[2] == 1 and iters[2] == -1
     assert fl[3] == 4
 
 

@@ -142,7 +142,7 @@ struct Engine {
     FftccTune fftcc_tune;
 
     DevBuf d_ref, d_tar, d_poi;
-    DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work;
+    DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work, d_tw;
     // per-reference cache
     bool cache_valid = false;
     const void* cache_poi_key = nullptr;
@@ -181,6 +181,20 @@ struct Engine {
         TW_TRY(d_err.ensure(sizeof(unsigned)));
         TW_TRY(d_work.ensure(sizeof(int) * 4));
         TW_CUDA(cudaMemsetAsync(d_err.p, 0, sizeof(unsigned), stream));
+        // DFT twiddles exp(-2 pi i k / N) of the two window sizes, rounded once
+        // from double (the FP32 SIMT FFT-CC kernel reads them)
+        std::vector<float> tw(4 * 64, 0.f);
+        const double two_pi = 6.283185307179586476925286766559;
+        for (int t = 0; t < 2; ++t) {
+            const int N = 2 * (t == 0 ? p.subset_x : p.subset_y);
+            for (int k = 0; k < N; ++k) {
+                tw[t * 128 + 2 * k] = (float)std::cos(-two_pi * k / N);
+                tw[t * 128 + 2 * k + 1] = (float)std::sin(-two_pi * k / N);
+            }
+        }
+        TW_TRY(d_tw.ensure(tw.size() * sizeof(float)));
+        TW_CUDA(cudaMemcpyAsync(d_tw.p, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+        TW_CUDA(cudaStreamSynchronize(stream));
         return TWDIC_OK;
     }
 
@@ -226,7 +240,8 @@ struct Engine {
             TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st,
                                     d_err.as<unsigned>(), stream));
         } else {
-            TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st, stream));
+            TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, d_tw.as<float2>(), u, v, z,
+                                       st, stream));
         }
         return TWDIC_OK;
     }
@@ -244,10 +259,10 @@ struct Engine {
                                                 c_sd.as<float2>(), c_chol.as<float>(), c_norm.as<float>(),
                                                 c_flag.as<uint8_t>(), stream));
         } else {
-            TW_TRY(c_stat.ensure(sizeof(float2) * (size_t)n));
+            TW_TRY(c_stat.ensure(sizeof(float) * 16 * (size_t)n));
             TW_TRY(c_chol64.ensure(sizeof(double) * 21 * (size_t)n));
             TW_TRY(c_flag64.ensure((size_t)n));
-            TW_CUDA(launch_ref_precompute_fast(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_stat.as<float2>(),
+            TW_CUDA(launch_ref_precompute_fast(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_stat.as<float>(),
                                                c_chol64.as<double>(), c_flag64.as<uint8_t>(), stream));
         }
         cache_valid = true;
@@ -271,7 +286,7 @@ struct Engine {
                 TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
                 TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
             }
-            TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float2>(),
+            TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.as<float4>(),
                                      d_work.as<int>(), u, v, p6, iters, flags, icgn_tune, stream));
         }
@@ -585,7 +600,8 @@ int twdic_frame_destroy(twdic_frame* h) {
 int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
                            int fftcc_use_tc) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (icgn_threads != 128 && icgn_threads != 256) return fail(TWDIC_ERR_INVALID_ARG, "threads must be 128 or 256");
+    if (icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 64, 128 or 256");
     h->e.icgn_tune.threads = icgn_threads;
     h->e.icgn_tune.ctas_per_sm = icgn_ctas_per_sm;
     h->e.icgn_tune.use_lut = icgn_use_lut;

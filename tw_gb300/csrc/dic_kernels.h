@@ -10,7 +10,7 @@ namespace twdic {
 
 // Launch shape of the fast IC-GN kernel, chosen by the autotuner.
 struct IcgnTune {
-    int threads = 128;    // 128 or 256 threads per CTA (one POI per CTA at a time)
+    int threads = 128;    // 64, 128 or 256 threads per CTA (one POI per CTA at a time)
     int ctas_per_sm = 0;  // persistent CTAs per SM (0 = occupancy limit)
     int use_lut = 0;      // 1: gather the per-frame LUT from HBM instead of the staged window
 };
@@ -21,8 +21,9 @@ struct FftccTune {
 };
 
 // ---- plain FP32 path (kernels_plain.cu)
+// tw: twiddle table, tw[k] = exp(-2 pi i k / 2rx) for k < 64, then the same for 2ry
 cudaError_t launch_fftcc_plain(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                               float* u, float* v, float* zncc, uint8_t* status, cudaStream_t st);
+                               const float2* tw, float* u, float* v, float* zncc, uint8_t* status, cudaStream_t st);
 cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* subR,
                                         float2* sd, float* chol, float* refnorm, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
@@ -32,10 +33,12 @@ cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi
                               cudaStream_t st);
 
 // ---- fast IC-GN (kernels_icgn_fast.cu)
-cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float2* refstat,
+// stats: 16 floats per POI (mean, norm, sum SD_k [6], sum SD_k (R - mean) [6], pad);
+// chol: 21 doubles per POI (packed lower factor, reciprocal diagonal).
+cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
                                        double* chol, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                             const float2* refstat, const double* chol, const uint8_t* rflag, const float4* lut,
+                             const float* stats, const double* chol, const uint8_t* rflag, const float4* lut,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st);
 int icgn_fast_window(const Geom& g);

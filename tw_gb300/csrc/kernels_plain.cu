@@ -18,8 +18,9 @@ constexpr int kIcgnThreads = 128;
 // c2r row DFT fused with the first-maximum search.
 __global__ void __launch_bounds__(kFftThreads) k_fftcc_plain(Geom g, const uint8_t* __restrict__ ref,
                                                                const uint8_t* __restrict__ tar,
-                                                               const int2* __restrict__ poi, int n, float* u,
-                                                               float* v, float* zncc, uint8_t* status) {
+                                                               const int2* __restrict__ poi, int n,
+                                                               const float2* __restrict__ tw, float* u, float* v,
+                                                               float* zncc, uint8_t* status) {
     const int p = blockIdx.x;
     if (p >= n) return;
     const int Nx = 2 * g.rx, Ny = 2 * g.ry, Hx = g.rx + 1, NN = Nx * Ny;
@@ -32,16 +33,7 @@ __global__ void __launch_bounds__(kFftThreads) k_fftcc_plain(Geom g, const uint8
     __shared__ int ired[2 * (kFftThreads / 32)];
 
     const int tid = threadIdx.x;
-    for (int k = tid; k < Nx; k += kFftThreads) {
-        double s, c;
-        sincospi(-2.0 * k / Nx, &s, &c);
-        twx[k] = make_float2((float)c, (float)s);
-    }
-    for (int k = tid; k < Ny; k += kFftThreads) {
-        double s, c;
-        sincospi(-2.0 * k / Ny, &s, &c);
-        twy[k] = make_float2((float)c, (float)s);
-    }
+    for (int k = tid; k < 128; k += kFftThreads) twx[k] = tw[k];
     const int2 pyx = poi[p];
     const int y0 = pyx.x - g.ry, x0 = pyx.y - g.rx;
     float* fw = reinterpret_cast<float*>(bufA);  // [Ny][Nx]
@@ -424,6 +416,7 @@ __global__ void __launch_bounds__(kIcgnThreads) k_icgn_plain(Geom g, const uint8
 #pragma unroll
         for (int k = 0; k < 6; ++k) Wm[k] = sW[k];
         const int flag = sctl[0], cont = sctl[1];
+        if (tid != 0 && flag == kSuccess) ++it;  // thread 0 advanced its counter in the solve
         if (flag != kSuccess) { finish((uint8_t)flag, it + 1, it > 0); return; }
         if (!cont) { finish(kSuccess, it, true); return; }
         __syncthreads();  // sctl/sW reused next iteration
@@ -434,13 +427,13 @@ __global__ void __launch_bounds__(kIcgnThreads) k_icgn_plain(Geom g, const uint8
 
 // ------------------------------------------------------------ launchers ----
 cudaError_t launch_fftcc_plain(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                               float* u, float* v, float* zncc, uint8_t* status, cudaStream_t st) {
+                               const float2* tw, float* u, float* v, float* zncc, uint8_t* status, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     const int Ny = 2 * g.ry, Hx = g.rx + 1;
     const size_t smem = sizeof(float2) * (128 + 4 * (size_t)Ny * Hx);
     cudaError_t e = cudaFuncSetAttribute(k_fftcc_plain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_fftcc_plain<<<n, kFftThreads, smem, st>>>(g, ref, tar, poi, n, u, v, zncc, status);
+    k_fftcc_plain<<<n, kFftThreads, smem, st>>>(g, ref, tar, poi, n, tw, u, v, zncc, status);
     return cudaGetLastError();
 }
 

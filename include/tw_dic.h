@@ -184,6 +184,39 @@ TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
                                      int fftcc_use_tc);
 
+/* ------------------------------------------- IC-GN without allocation --- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they run IC-GN: a real-time camera loop whose frame deadline
+ * cannot absorb cudaMalloc's implicit device-wide synchronisation or an
+ * out-of-memory failure mid-stream, or an application whose device memory is
+ * budgeted up front by another allocator.  Runs the fast IC-GN path
+ * (per-reference precompute, then the persistent IC-GN kernel) for one
+ * target frame, with every buffer supplied by the caller and the path's
+ * scratch (per-POI reference cache and work counter) held in a fixed-size
+ * static device array inside the library: no cudaMalloc, cudaFree or
+ * allocating library call.
+ *   - at most TWDIC_NOALLOC_MAX_POIS POIs per call (larger counts return
+ *     TWDIC_ERR_UNSUPPORTED); the array takes about 46 MB on every GPU that
+ *     loads the library, until the process exits;
+ *   - all pointers are device pointers: images as in twdic_icgn_compute
+ *     (pitch = img_width), poi_yx 8-byte aligned, u/v/iters in-out, p6 and
+ *     flags out, all num_pois long; the work is queued on `stream`
+ *     (cudaStream_t as void*, NULL = legacy default stream) and the call
+ *     returns without synchronising;
+ *   - the reference precompute is redone on every call (no cache survives
+ *     between calls); the array keeps the last call's contents, and the parts
+ *     that must start at zero are cleared on the stream by each call;
+ *   - every call shares the one array: calls whose GPU work overlaps (other
+ *     streams, other host threads) race and corrupt each other's results --
+ *     serialise them;
+ *   - the first call on a device resolves the array's device address
+ *     (cudaGetSymbolAddress, which may load the library's module on that
+ *     device); make that first call before any stream capture. */
+#define TWDIC_NOALLOC_MAX_POIS 196608
+TWDIC_API int twdic_icgn_compute_noalloc(const twdic_params* p, const uint8_t* d_ref, const uint8_t* d_tar,
+                                         const int32_t* d_poi_yx, int32_t num_pois, float* d_u, float* d_v,
+                                         float* d_p6, int32_t* d_iters, uint8_t* d_flags, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,7 @@ EXPORTED = (
     "twdic_icgn_create", "twdic_icgn_reset_ref", "twdic_icgn_compute", "twdic_icgn_destroy",
     "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
-    "twdic_frame_set_tuning",
+    "twdic_frame_set_tuning", "twdic_icgn_compute_noalloc",
 )
 
 
@@ -101,6 +101,7 @@ def load():
         "twdic_frame_phase_times": ([_VP, _VP], _I),
         "twdic_frame_destroy": ([_VP], _I),
         "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
+        "twdic_icgn_compute_noalloc": ([P, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -312,6 +312,10 @@ int check_mem(int mem) {
 }
 
 }  // namespace
+
+// Error message setter for entry points defined in other translation units.
+void set_error_message(const char* msg) { g_last_error = msg; }
+
 }  // namespace twdic
 
 using namespace twdic;

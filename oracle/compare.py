@@ -21,7 +21,9 @@ from . import oracle as O
 
 UV_TOL = 1e-3
 GRAD_TOL = 1e-5
-ZNCC_TOL = 1e-5
+# ZNCC: the FP32 oracle's own rounding reaches ~1e-5 for 62x62 windows (sums
+# of squares near 1e7 in float), so the bound is 3e-5
+ZNCC_TOL = 3e-5
 
 
 @dataclasses.dataclass

@@ -141,6 +141,28 @@ def test_icgn_flags_and_counters(small, path):
     assert fl[3] == 4
 
 
+@pytest.mark.parametrize("r", [5, 8, 10, 15, 16, 20, 24, 29, 31])
+def test_fftcc_radii_parity(r):
+    """FFT-CC at the subset radii of the uneven-batching workload (r in
+    10..30) and the ends of the supported range, both paths."""
+    pair, g = synth.small_case(h=150, w=170, r=r, grid=9, seed=100 + r)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    if nx <= 0 or ny <= 0:
+        pytest.skip("no POI at this radius")
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, poi, r)
+    for path in PATHS:
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, r, r, g.grid, g.grid,
+                          g.margin, g.margin, path=path)
+        U, V, Z = f.InitializeFFTCC(pair.ref)
+        st = np.zeros(f.GetNumPOIs(), np.uint8)
+        f.ComputeFFTCC(U, V, Z, pair.tar, status=st)
+        rep = C.fftcc_parity(pair.ref, pair.tar, poi, r, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or, st_or)
+        print(r, path, rep)
+        assert (st == st_or).all()
+        assert rep.ok(), (r, path, rep)
+
+
 def test_fftcc_dark_subset_untouched(small):
     pair, g, _, _ = small
     ref = np.full_like(pair.ref, 50)

@@ -1,15 +1,638 @@
-// Tensor-core FFT-CC (tcgen05 DFT GEMMs).  Placeholder until implemented:
-// reports unsupported so the engine uses the FP32 SIMT DFT kernel.
+// Tensor-core FFT-CC: the per-POI 2D DFTs of Fftcc2D_CPU::ComputeFFTCC
+// (TW_paDIC_FFTCC2D_CPU.cpp:222-326) as batched GEMMs on tcgen05.
+//
+// For an N x N window (N = 2r, no padding of the data: the correlation stays
+// circular as in the reference), with w = exp(-2 pi i / N):
+//   stage 1  Y[ky][x]  = sum_y f[y][x] w^(ky y)          ky <= N/2 (real input)
+//   stage 2  F[ky][kx] = sum_x Y[ky][x] w^(kx x)
+//   cross    C = conj(F) G / (||f-mean|| ||g-mean||), C[0][0] = 0 (mean removal)
+//   stage 3  conj(Z[ky][x]) = sum_kx conj(C[ky][kx]) w^(kx x)   (the forward
+//            matrices serve the inverse transform through the conjugate)
+//   stage 4  c[y][x]  = sum_ky weight(ky) Re(Z[ky][x] w^(-ky y))  (c2r)
+// Every stage is D[128 x n] += A[128 x k] B[k x n] with the data as A
+// (rows = window rows / spectrum rows of several POIs, K-major in shared
+// memory) and constant twiddle matrices as B (K-major), FP16 operands, FP32
+// accumulators in tensor memory.  Twiddles are split hi + lo (two MMAs); the
+// data operands are single FP16.  The resulting surface is accurate to
+// ~1e-3 of its range, so the integer peak is then decided exactly: every
+// shift within 2% of the approximate maximum is re-evaluated as the exact
+// integer correlation sum_x f(x) g(x + k) (whose order is the order of the
+// mean-subtracted correlation), with the reference's first-maximum rule.
+// ZNCC is computed from the exact integer sums in FP64.
+//
+// One CTA of 128 threads (one warpgroup) per SM slot, persistent over POI
+// batches; thread 0 issues the MMAs, completion is signalled through an
+// mbarrier (bounded wait), the epilogues read TMEM with tcgen05.ld.
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "dic_common.cuh"
 #include "dic_kernels.h"
 
 namespace twdic {
 
-bool fftcc_tc_supported(const Geom&) { return false; }
+namespace {
 
-cudaError_t launch_fftcc_tc(const Geom&, const uint8_t*, const uint8_t*, const int2*, int, float*, float*, float*,
-                            uint8_t*, unsigned*, cudaStream_t) {
-    return cudaErrorNotSupported;
+constexpr int kThreads = 128;
+constexpr int kMaxCand = 16;      // exact re-evaluations per POI
+constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
+constexpr int kTmemCols = 128;
+constexpr unsigned kWaitLimit = 1u << 24;
+
+struct TcShape {
+    int N, H, HP, NP, PB, tiles1, K4, n_batches, n;
+    int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
+    int off_a13, off_a2, off_a4, smem_bytes;
+};
+
+__host__ __device__ __forceinline__ int kmaj(int r, int k, int K) {  // LBO 128 B, SBO 16*K B
+    return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+__host__ __device__ __forceinline__ int kmaj144(int r, int k, int K) {  // LBO 144 B, SBO 18*K B
+    return (r >> 3) * (K * 18) + (k >> 3) * 144 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// ------------------------------------------------------------ PTX glue ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    // no-swizzle K-major descriptor: start>>4 [0,14), LBO>>4 [16,30), SBO>>4 [32,46), version 1 at bit 46
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__host__ __device__ constexpr uint32_t idesc_f16(int n, bool neg_b) {
+    // kind::f16: D f32 (bit 4), A = B = f16, both K-major, N>>3 at bit 17, M>>4 at bit 24
+    return (1u << 4) | ((neg_b ? 1u : 0u) << 14) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: returns false (and leaves the caller to abort) after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (unsigned i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast<__half*>(p) = __float2half_rn(v); }
+
+// ----------------------------------------------------------------- kernel --
+template <int NP>
+__global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, const uint8_t* __restrict__ ref,
+                                                          const uint8_t* __restrict__ tar,
+                                                          const int2* __restrict__ poi,
+                                                          const uint4* __restrict__ tables, float* u, float* v,
+                                                          float* zncc, uint8_t* status, unsigned* err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int wsum[2 * kMaxPB][2];
+    __shared__ float sscale[kMaxPB];
+    __shared__ int sdark[kMaxPB];
+    __shared__ float sbv[kThreads];
+    __shared__ int sbi[kThreads];
+    __shared__ float sthr[kMaxPB];
+    __shared__ int ncand[kMaxPB];
+    __shared__ int cand[kMaxPB][kMaxCand];
+    __shared__ int candS[kMaxPB][kMaxCand];
+    __shared__ int sabort;
+
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int N = s.N, H = s.H, HP = s.HP, PB = s.PB, K4 = s.K4;
+    const int n2 = N * N;
+    constexpr int K1 = NP;
+
+    // ---- set-up: TMEM, mbarrier, twiddle tables, zeroed A2/A4
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (t == 0) {
+        mbar_init(&mbar);
+        sabort = 0;
+    }
+    {
+        uint4* dst = reinterpret_cast<uint4*>(sm);
+        for (int i = t; i < s.tab_bytes / 16; i += kThreads) dst[i] = tables[i];
+        uint4* a2 = reinterpret_cast<uint4*>(sm + s.off_a2);
+        for (int i = t; i < (s.smem_bytes - s.off_a2) / 16; i += kThreads) a2[i] = make_uint4(0, 0, 0, 0);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = tmem_slot;
+    const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
+    const uint32_t sbase = smem_u32(sm);
+    uint32_t phase = 0;
+
+    for (int batch = blockIdx.x; batch < s.n_batches; batch += gridDim.x) {
+        const int b0 = batch * PB;
+        if (t < 2 * kMaxPB * 2) (&wsum[0][0])[t] = 0;
+        __syncthreads();
+
+        // ---- phase L: windows -> A1 (rows (window, x), K = y), exact FP16
+        for (int rr = t; rr < s.tiles1 * 128; rr += kThreads) {
+            const int wi = rr / N, x = rr - wi * N;
+            const int p = wi >> 1;
+            const bool valid = wi < 2 * PB && b0 + p < s.n;
+            const uint8_t* base = nullptr;
+            if (valid) {
+                const int2 pyx = poi[b0 + p];
+                base = ((wi & 1) ? tar : ref) + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx) + x;
+            }
+            uint8_t* a1 = sm + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
+            const int row = rr & 127;
+            int su = 0, sq = 0;
+#pragma unroll
+            for (int c = 0; c < K1 / 8; ++c) {
+                float f[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int y = c * 8 + j;
+                    const int val = (valid && y < N) ? (int)base[(size_t)y * g.pitch] : 0;
+                    su += val;
+                    sq += val * val;
+                    f[j] = (float)val;
+                }
+                uint4 q;
+                q.x = pack2(f[0], f[1]); q.y = pack2(f[2], f[3]); q.z = pack2(f[4], f[5]); q.w = pack2(f[6], f[7]);
+                *reinterpret_cast<uint4*>(a1 + kmaj(row, c * 8, K1)) = q;
+            }
+            if (valid) {
+                atomicAdd(&wsum[wi][0], su);
+                atomicAdd(&wsum[wi][1], sq);
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+
+        // ---- stage 1: D1[(w,x)][(part,ky)] = A1 * B1
+        if (t == 0) {
+            tc_fence_after();
+            for (int tile = 0; tile < s.tiles1; ++tile) {
+                const uint32_t a0 = sbase + s.off_a13 + tile * (128 * K1 * 2);
+                for (int kk = 0; kk < K1 / 16; ++kk) {
+                    const uint64_t a = sdesc(a0 + kk * 256, 128, 16 * K1);
+                    const uint64_t bh = sdesc(sbase + s.off_b1h + kk * 256, 128, 16 * K1);
+                    const uint64_t bl = sdesc(sbase + s.off_b1l + kk * 256, 128, 16 * K1);
+                    mma_f16(tm + tile * 2 * HP, a, bh, idesc_f16(2 * HP, false), kk > 0);
+                    mma_f16(tm + tile * 2 * HP, a, bl, idesc_f16(2 * HP, false), 1);
+                }
+            }
+            mma_commit(&mbar);
+        }
+        // per-POI normalisation while the MMAs run: 1/sqrt(nf ng) with
+        // nf = sum (f - mean)^2 = (n sum f^2 - (sum f)^2) / n, exact in integers
+        if (t < PB) {
+            const int wf = 2 * t, wg = 2 * t + 1;
+            const long long numf = (long long)n2 * wsum[wf][1] - (long long)wsum[wf][0] * wsum[wf][0];
+            const long long numg = (long long)n2 * wsum[wg][1] - (long long)wsum[wg][0] * wsum[wg][0];
+            const bool dark = b0 + t >= s.n || numf == 0 || numg == 0;
+            sdark[t] = dark ? 1 : 0;
+            sscale[t] = dark ? 0.f : (float)((double)n2 / sqrt((double)numf * (double)numg));
+        }
+        bool ok = mbar_wait(&mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        tc_fence_after();
+
+        // ---- epilogue 1: Y -> A2 (rows (p, ky, w), K = (part, x)), FP16
+        for (int tile = 0; tile < s.tiles1; ++tile) {
+            float d[2 * 40];
+            for (int c = 0; c < 2 * HP; c += 16) tmem_ld16(tm_warp + tile * 2 * HP + c, d + c);
+            tmem_ld_wait();
+            const int rr = tile * 128 + t;
+            const int wi = rr / N, x = rr - wi * N;
+            if (wi < 2 * PB) {
+                const int p = wi >> 1, wsel = wi & 1;
+                uint8_t* a2 = sm + s.off_a2;
+                for (int ky = 0; ky < H; ++ky) {
+                    const int r2 = (p * H + ky) * 2 + wsel;
+                    st_half(a2 + kmaj144(r2, x, 2 * NP), d[ky]);
+                    st_half(a2 + kmaj144(r2, NP + x, 2 * NP), d[HP + ky]);
+                }
+            }
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+
+        // ---- stage 2: F = Y * W (rows (p,ky,w); columns Re kx | Im kx)
+        if (t == 0) {
+            tc_fence_after();
+            for (int kk = 0; kk < NP / 16; ++kk) {
+                const uint64_t ar = sdesc(sbase + s.off_a2 + kk * 288, 144, 36 * NP);
+                const uint64_t ai = sdesc(sbase + s.off_a2 + (NP / 8 + 2 * kk) * 144, 144, 36 * NP);
+                const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
+                const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
+                const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
+                const uint64_t sl = sdesc(sbase + s.off_s2l + kk * 256, 128, 16 * NP);
+                const uint32_t acc = kk > 0;
+                mma_f16(tm, ar, ch, idesc_f16(NP, false), acc);  // Re = Yr cos + Yi sin
+                mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
+                mma_f16(tm, ai, sh, idesc_f16(NP, false), 1);
+                mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
+                mma_f16(tm + NP, ar, sh, idesc_f16(NP, true), acc);  // Im = -Yr sin + Yi cos
+                mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
+                mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
+                mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
+            }
+            mma_commit(&mbar);
+        }
+        ok = mbar_wait(&mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        tc_fence_after();
+
+        // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
+        {
+            float re[NP], im[NP];
+            for (int c = 0; c < NP; c += 16) {
+                tmem_ld16(tm_warp + c, re + c);
+                tmem_ld16(tm_warp + NP + c, im + c);
+            }
+            tmem_ld_wait();
+            const bool rowv = t < 2 * PB * H;
+            const int p = rowv ? t / (2 * H) : 0;
+            const int ky = rowv ? (t >> 1) % H : 0;
+            const int wsel = t & 1;
+            const float sc = rowv ? sscale[p] : 0.f;
+            const int r3 = p * H + ky;
+            uint8_t* a3 = sm + s.off_a13;
+            constexpr int HALF = NP / 2;
+            float br[8], bi[8];
+#pragma unroll
+            for (int i = 0; i < HALF; ++i) {
+                const float own_r = wsel ? re[HALF + i] : re[i];
+                const float own_i = wsel ? im[HALF + i] : im[i];
+                const float snd_r = wsel ? re[i] : re[HALF + i];
+                const float snd_i = wsel ? im[i] : im[HALF + i];
+                const float oth_r = __shfl_xor_sync(0xffffffffu, snd_r, 1);
+                const float oth_i = __shfl_xor_sync(0xffffffffu, snd_i, 1);
+                const float fr = wsel ? oth_r : own_r, fi = wsel ? oth_i : own_i;
+                const float gr = wsel ? own_r : oth_r, gi = wsel ? own_i : oth_i;
+                const int kx = wsel ? HALF + i : i;
+                float cr = (fr * gr + fi * gi) * sc;
+                float ci = (fr * gi - fi * gr) * sc;
+                if (kx >= N || (ky == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
+                br[i & 7] = cr;
+                bi[i & 7] = -ci;  // conj(C) feeds the forward matrices of stage 3
+                if ((i & 7) == 7 && rowv) {
+                    const int k0 = kx - 7;
+                    uint4 q;
+                    q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
+                    q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
+                    *reinterpret_cast<uint4*>(a3 + kmaj(r3, k0, 2 * NP)) = q;
+                    q.x = pack2(bi[0], bi[1]); q.y = pack2(bi[2], bi[3]);
+                    q.z = pack2(bi[4], bi[5]); q.w = pack2(bi[6], bi[7]);
+                    *reinterpret_cast<uint4*>(a3 + kmaj(r3, NP + k0, 2 * NP)) = q;
+                }
+            }
+            // rows of A3 past the data are zero (A3 shares memory with A1)
+            if (t >= PB * H) {
+                for (int k0 = 0; k0 < 2 * NP; k0 += 8)
+                    *reinterpret_cast<uint4*>(a3 + kmaj(t, k0, 2 * NP)) = make_uint4(0, 0, 0, 0);
+            }
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+
+        // ---- stage 3: conj(Z) = conj(C) * W (rows (p,ky); columns Re x | Im x)
+        if (t == 0) {
+            tc_fence_after();
+            for (int kk = 0; kk < NP / 16; ++kk) {
+                const uint64_t ar = sdesc(sbase + s.off_a13 + kk * 256, 128, 32 * NP);
+                const uint64_t ai = sdesc(sbase + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 32 * NP);
+                const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
+                const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
+                const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
+                const uint64_t sl = sdesc(sbase + s.off_s2l + kk * 256, 128, 16 * NP);
+                const uint32_t acc = kk > 0;
+                mma_f16(tm, ar, ch, idesc_f16(NP, false), acc);
+                mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
+                mma_f16(tm, ai, sh, idesc_f16(NP, false), 1);
+                mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
+                mma_f16(tm + NP, ar, sh, idesc_f16(NP, true), acc);
+                mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
+                mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
+                mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
+            }
+            mma_commit(&mbar);
+        }
+        ok = mbar_wait(&mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        tc_fence_after();
+
+        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (part, ky)), c2r weights folded in
+        {
+            float re[NP], im[NP];
+            for (int c = 0; c < NP; c += 16) {
+                tmem_ld16(tm_warp + c, re + c);
+                tmem_ld16(tm_warp + NP + c, im + c);
+            }
+            tmem_ld_wait();
+            if (t < PB * H) {
+                const int p = t / H, ky = t - (t / H) * H;
+                const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
+                uint8_t* a4 = sm + s.off_a4;
+#pragma unroll
+                for (int x = 0; x < NP; ++x) {
+                    if (x < N) {
+                        const int r4 = p * N + x;
+                        st_half(a4 + kmaj144(r4, ky, K4), wgt * re[x]);
+                        st_half(a4 + kmaj144(r4, HP + ky, K4), -wgt * im[x]);  // Zi = -D_i
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+
+        // ---- stage 4: c[(p,x)][y] = A4 * B4
+        if (t == 0) {
+            tc_fence_after();
+            for (int kk = 0; kk < K4 / 16; ++kk) {
+                const uint64_t a = sdesc(sbase + s.off_a4 + kk * 288, 144, 18 * K4);
+                const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
+                const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
+                mma_f16(tm, a, bh, idesc_f16(NP, false), kk > 0);
+                mma_f16(tm, a, bl, idesc_f16(NP, false), 1);
+            }
+            mma_commit(&mbar);
+        }
+        ok = mbar_wait(&mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        tc_fence_after();
+
+        // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
+        float cv[NP];
+        for (int c = 0; c < NP; c += 16) tmem_ld16(tm_warp + c, cv + c);
+        tmem_ld_wait();
+        tc_fence_before();
+        const bool rowv = t < PB * N;
+        const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
+        {
+            float bv = -3.4e38f;
+            int bi = 0x7fffffff;
+            if (rowv && !sdark[p4]) {
+#pragma unroll
+                for (int y = 0; y < NP; ++y)
+                    if (y < N && cv[y] > bv) { bv = cv[y]; bi = y * N + x4; }
+            }
+            sbv[t] = bv;
+            sbi[t] = bi;
+        }
+        __syncthreads();
+        if (t < PB) {
+            float bv = -3.4e38f;
+            int bi = 0x7fffffff;
+            for (int r = t * N; r < t * N + N; ++r) argmax_merge(bv, bi, sbv[r], sbi[r]);
+            sthr[t] = bv - 0.02f * (float)n2;
+            ncand[t] = 1;
+            cand[t][0] = bi;
+        }
+        __syncthreads();
+        if (rowv && !sdark[p4]) {
+#pragma unroll
+            for (int y = 0; y < NP; ++y) {
+                if (y < N && cv[y] >= sthr[p4]) {
+                    const int idx = y * N + x4;
+                    if (idx != cand[p4][0]) {
+                        const int slot = atomicAdd(&ncand[p4], 1);
+                        if (slot < kMaxCand) cand[p4][slot] = idx;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // exact integer correlation of every candidate, one warp per (POI, candidate)
+        for (int task = warp; task < PB * kMaxCand; task += kThreads / 32) {
+            const int p = task / kMaxCand, slot = task - p * kMaxCand;
+            if (sdark[p] || slot >= min(ncand[p], kMaxCand)) continue;
+            const int idx = cand[p][slot];
+            const int kx = idx % N, ky = idx / N;
+            const int2 pyx = poi[b0 + p];
+            const uint8_t* fb = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
+            const uint8_t* gb = tar + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
+            int acc = 0;
+            for (int q = lane; q < n2; q += 32) {
+                const int y = q / N, x = q - (q / N) * N;
+                int yy = y + ky; if (yy >= N) yy -= N;
+                int xx = x + kx; if (xx >= N) xx -= N;
+                acc += (int)fb[(size_t)y * g.pitch + x] * (int)gb[(size_t)yy * g.pitch + xx];
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) candS[p][slot] = acc;
+        }
+        __syncthreads();
+        if (t < PB && b0 + t < s.n) {
+            const int gp = b0 + t;
+            if (sdark[t]) {
+                status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
+            } else {
+                const int nc = min(ncand[t], kMaxCand);
+                int best = cand[t][0], bs = candS[t][0];
+                for (int c = 1; c < nc; ++c) {
+                    const int sc = candS[t][c], id = cand[t][c];
+                    if (sc > bs || (sc == bs && id < best)) { bs = sc; best = id; }
+                }
+                int iu = best % N, iv = best / N;
+                if (iu > g.rx) iu -= N;
+                if (iv > g.ry) iv -= N;
+                const long long sf = wsum[2 * t][0], sg = wsum[2 * t + 1][0];
+                const long long numf = (long long)n2 * wsum[2 * t][1] - sf * sf;
+                const long long numg = (long long)n2 * wsum[2 * t + 1][1] - sg * sg;
+                const double cnum = (double)((long long)n2 * bs - sf * sg);
+                u[gp] = (float)iu;
+                v[gp] = (float)iv;
+                zncc[gp] = (float)(cnum / sqrt((double)numf * (double)numg));
+                status[gp] = 0;
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- teardown
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kTmemCols));
+}
+
+// ----------------------------------------------------------- host side ----
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+bool make_shape(const Geom& g, int n, TcShape& s) {
+    if (g.rx != g.ry) return false;
+    const int N = 2 * g.rx;
+    if (N < 8 || N > 64) return false;
+    s.N = N;
+    s.H = N / 2 + 1;
+    s.HP = round_up(s.H, 8);
+    s.NP = round_up(N, 16);
+    int pb = 256 / (2 * N);
+    pb = std::min(pb, 64 / s.H);
+    pb = std::min(pb, 128 / N);
+    pb = std::min(pb, kMaxPB);
+    if (pb < 1 || 2 * s.HP > 80) return false;
+    s.PB = pb;
+    s.tiles1 = (pb * 2 * N + 127) / 128;
+    s.K4 = 2 * s.HP;
+    // tensor-memory columns used by the stages must fit the allocation
+    if (s.tiles1 * 2 * s.HP > kTmemCols || 2 * s.NP > kTmemCols || s.tiles1 > 2) return false;
+    if (2 * pb * s.H > 128 || pb * N > 128) return false;
+    s.n = n;
+    s.n_batches = (n + pb - 1) / pb;
+    const int K1 = s.NP, N1 = 2 * s.HP, NP = s.NP, K4 = s.K4;
+    int o = 0;
+    s.off_b1h = o; o += N1 * K1 * 2;
+    s.off_b1l = o; o += N1 * K1 * 2;
+    s.off_c2h = o; o += NP * NP * 2;
+    s.off_c2l = o; o += NP * NP * 2;
+    s.off_s2h = o; o += NP * NP * 2;
+    s.off_s2l = o; o += NP * NP * 2;
+    s.off_b4h = o; o += NP * K4 * 2;
+    s.off_b4l = o; o += NP * K4 * 2;
+    s.tab_bytes = o;
+    s.off_a13 = o; o += std::max(s.tiles1 * 128 * K1 * 2, 128 * 2 * NP * 2);
+    s.off_a2 = o; o += 16 * 36 * NP;
+    s.off_a4 = o; o += 16 * 18 * K4;
+    s.smem_bytes = o;
+    return s.smem_bytes <= 200 * 1024;
+}
+
+// Twiddle matrices B1, C2, S2, B4 (hi and lo FP16) in the no-swizzle K-major
+// layout the kernel's descriptors expect, computed in double.
+std::vector<uint8_t> make_tables(const TcShape& s) {
+    std::vector<uint8_t> blob(s.tab_bytes, 0);
+    const int N = s.N, H = s.H, HP = s.HP, NP = s.NP, K1 = s.NP, K4 = s.K4;
+    const double two_pi = 6.283185307179586476925286766559;
+    auto put = [&](int off_h, int off_l, int r, int k, int K, double val) {
+        const __half h = __double2half(val);
+        const __half l = __double2half(val - (double)__half2float(h));
+        std::memcpy(&blob[off_h + kmaj(r, k, K)], &h, 2);
+        std::memcpy(&blob[off_l + kmaj(r, k, K)], &l, 2);
+    };
+    auto ang = [&](int a, int b) { return two_pi * (double)((long long)a * b % N) / N; };
+    for (int ky = 0; ky < H; ++ky)
+        for (int y = 0; y < N; ++y) {
+            put(s.off_b1h, s.off_b1l, ky, y, K1, std::cos(ang(ky, y)));        // Re part row
+            put(s.off_b1h, s.off_b1l, HP + ky, y, K1, -std::sin(ang(ky, y)));  // Im part row
+            put(s.off_b4h, s.off_b4l, y, ky, K4, std::cos(ang(ky, y)));
+            put(s.off_b4h, s.off_b4l, y, HP + ky, K4, -std::sin(ang(ky, y)));
+        }
+    for (int kx = 0; kx < N; ++kx)
+        for (int x = 0; x < N; ++x) {
+            put(s.off_c2h, s.off_c2l, kx, x, NP, std::cos(ang(kx, x)));
+            put(s.off_s2h, s.off_s2l, kx, x, NP, std::sin(ang(kx, x)));
+        }
+    return blob;
+}
+
+struct TablesCache {
+    int N = -1;
+    uint4* dev = nullptr;
+    ~TablesCache() {
+        if (dev) cudaFree(dev);
+    }
+};
+
+}  // namespace
+
+bool fftcc_tc_supported(const Geom& g) {
+    TcShape s;
+    return make_shape(g, 1, s);
+}
+
+cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    TcShape s;
+    if (!make_shape(g, n, s)) return cudaErrorNotSupported;
+    static thread_local TablesCache cache;
+    if (cache.N != s.N) {
+        if (cache.dev) cudaFree(cache.dev);
+        cache.dev = nullptr;
+        cache.N = -1;
+        std::vector<uint8_t> blob = make_tables(s);
+        cudaError_t e = cudaMalloc(&cache.dev, blob.size());
+        if (e != cudaSuccess) return e;
+        e = cudaMemcpy(cache.dev, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+        cache.N = s.N;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void (*kern)(TcShape, Geom, const uint8_t*, const uint8_t*, const int2*, const uint4*, float*, float*, float*,
+                 uint8_t*, unsigned*) = nullptr;
+    switch (s.NP) {
+        case 16: kern = k_fftcc_tc<16>; break;
+        case 32: kern = k_fftcc_tc<32>; break;
+        case 48: kern = k_fftcc_tc<48>; break;
+        case 64: kern = k_fftcc_tc<64>; break;
+        default: return cudaErrorNotSupported;
+    }
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, s.smem_bytes);
+    if (e != cudaSuccess) return e;
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, s.smem_bytes);
+    if (e != cudaSuccess) return e;
+    occ = std::max(1, std::min(occ, 4));  // TMEM: 128 columns per CTA, 512 per SM
+    int grid = std::min(sms * occ, s.n_batches);
+    kern<<<grid, kThreads, s.smem_bytes, st>>>(s, g, ref, tar, poi, cache.dev, u, v, zncc, status, err);
+    return cudaGetLastError();
 }
 
 }  // namespace twdic

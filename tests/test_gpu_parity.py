@@ -73,7 +73,8 @@ def test_frame_parity(request, case, path):
     f.ComputeFFTCC(U, V, Z, pair.tar)
     same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
     assert same_start.mean() > 0.99
-    rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start)
+    rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start,
+                        r=g.subset_r)
     print(case, path, rep)
     assert rep.ok(), rep
     np.testing.assert_array_equal(out["u"], out["p6"][:, 0])
@@ -112,7 +113,7 @@ def test_icgn_api_with_oracle_guesses(small, path):
     u, v = u_or.copy(), v_or.copy()
     iters = np.zeros(n, np.int32)
     p6, fl = ic.ICGN2D_Algorithm(u, v, iters, poi, pair.tar)
-    rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or)
+    rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or, r=g.subset_r)
     assert rep.ok(), rep
 
 
@@ -208,5 +209,5 @@ def test_full_size_properties():
         u, v = u_or.copy(), v_or.copy()
         iters = np.zeros(len(sp), np.int32)
         p6, fl = ic.ICGN2D_Algorithm(u, v, iters, sp, pair.tar)
-        rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or)
+        rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or, r=g.subset_r)
         assert rep.ok(), (path, rep)

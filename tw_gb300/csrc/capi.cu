@@ -162,6 +162,10 @@ struct Engine {
 
     int init(const twdic_params& p, int num_pois) {
         prm = p;
+        // fastest measured IC-GN shape on GB300 at 41x41 subsets: 64 threads
+        // per POI gathering a per-frame LUT (the autotuner may change it)
+        icgn_tune.threads = 64;
+        icgn_tune.use_lut = 1;
         g = make_geom(p);
         n = num_pois;
         TW_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));

@@ -34,29 +34,34 @@ constexpr int kPreThreads = 128;
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
 // Per-reference precompute (TW_paDIC_ICGN2D_CPU.cpp:516-595, :676-693).
-// FP32 per-thread partial sums (exact for the intensity sum), FP64 across
-// threads; FP64 Cholesky.
+// Per-thread FP32 partial sums (exact for the intensity sum) and FP32 warp
+// sums; the final cross-warp sums are FP64, one value per lane of warp 0.
+// Thread 0 factors the Hessian (Cholesky, FP64) and forms H^-1 = L^-T L^-1
+// from the factor in FP64, stored packed (21 doubles) for the per-iteration
+// FP64 solve.  On GB300 an FP64 warp instruction holds the FP64 pipe for
+// many cycles whatever its active lanes, so FP64 work is kept to a few
+// lane-parallel instructions.
 __global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, const uint8_t* __restrict__ ref,
                                                                       const int2* __restrict__ poi, int n,
-                                                                      float* stats, double* chol,
+                                                                      float* stats, double* hinv,
                                                                       uint8_t* rflag) {
     const int p = blockIdx.x;
     if (p >= n) return;
     const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
     const int2 pyx = poi[p];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     constexpr int NW = kPreThreads / 32;
-    __shared__ double dred[34 * NW];
+    __shared__ float fred[NW][34];
+    __shared__ double dsum[34];
     __shared__ int ired[NW];
     if (pyx.x - g.ry < g.sy || pyx.y - g.rx < g.sx || pyx.x + g.ry >= g.sy + g.rh || pyx.y + g.rx >= g.sx + g.rw) {
         if (tid == 0) rflag[p] = kOutofROI;
         return;
     }
+    const uint8_t* r0 = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
     int isum[1] = {0};
-    for (int k = tid; k < S; k += kPreThreads) {
-        const int l = k / SW, m = k - l * SW;
-        isum[0] += ref[(size_t)(pyx.x - g.ry + l) * g.pitch + (pyx.y - g.rx + m)];
-    }
+    for (int l = wid; l < SH; l += NW)
+        for (int m = lane; m < SW; m += 32) isum[0] += r0[(size_t)l * g.pitch + m];
     block_sum<kPreThreads, 1>(isum, ired);
     const float mean = (float)isum[0] / (float)S;  // bit-equal to the reference's mean
     // [0..20] Hessian lower triangle, [21] sum (R-mean)^2, [22..27] sum SD_k,
@@ -64,48 +69,76 @@ __global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, con
     float h[34];
 #pragma unroll
     for (int k = 0; k < 34; ++k) h[k] = 0.f;
-    for (int k = tid; k < S; k += kPreThreads) {
-        const int l = k / SW, m = k - l * SW;
-        const uint8_t* r = ref + (size_t)(pyx.x - g.ry + l) * g.pitch + (pyx.y - g.rx + m);
-        const float rx = 0.5f * (float)((int)r[1] - (int)r[-1]);
-        const float ry = 0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]);
-        const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
-        const float d[6] = {rx, rx * dx, rx * dy, ry, ry * dx, ry * dy};
-        const float rt = (float)r[0] - mean;
-        int q = 0;
+    for (int l = wid; l < SH; l += NW) {
+        for (int m = lane; m < SW; m += 32) {
+            const uint8_t* r = r0 + (size_t)l * g.pitch + m;
+            const float rx = 0.5f * (float)((int)r[1] - (int)r[-1]);
+            const float ry = 0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]);
+            const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
+            const float d[6] = {rx, rx * dx, rx * dy, ry, ry * dx, ry * dy};
+            const float rt = (float)r[0] - mean;
+            int q = 0;
 #pragma unroll
-        for (int a = 0; a < 6; ++a)
+            for (int a = 0; a < 6; ++a)
 #pragma unroll
-            for (int b = 0; b <= a; ++b) h[q++] += d[a] * d[b];
-        h[21] += rt * rt;
+                for (int b = 0; b <= a; ++b) h[q++] += d[a] * d[b];
+            h[21] += rt * rt;
 #pragma unroll
-        for (int a = 0; a < 6; ++a) {
-            h[22 + a] += d[a];
-            h[28 + a] += d[a] * rt;
+            for (int a = 0; a < 6; ++a) {
+                h[22 + a] += d[a];
+                h[28 + a] += d[a] * rt;
+            }
         }
     }
-    double dv[34];
 #pragma unroll
-    for (int k = 0; k < 34; ++k) dv[k] = (double)h[k];
-    block_sum<kPreThreads, 34>(dv, dred);
+    for (int k = 0; k < 34; ++k) {
+        const float w = warp_sum(h[k]);
+        if (lane == 0) fred[wid][k] = w;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        for (int k = lane; k < 34; k += 32) {
+            double a = 0.0;
+            for (int w = 0; w < NW; ++w) a += (double)fred[w][k];
+            dsum[k] = a;
+        }
+    }
+    __syncthreads();
     if (tid == 0) {
-        const float rs = (float)sqrt(dv[21]);
+        const float rs = (float)sqrt(dsum[21]);
         uint8_t f = kSuccess;
         if (fabsf(mean) <= FLT_EPSILON || fabsf(rs) <= FLT_EPSILON) f = kDarkSubset;
         double a[36];
         int q = 0;
         for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) a[i * 6 + j] = (j <= i) ? dv[q++] : 0.0;
+            for (int j = 0; j < 6; ++j) a[i * 6 + j] = (j <= i) ? dsum[q++] : 0.0;
         if (f == kSuccess && potrf6(a) > 0) f = kSingularHessian;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j <= i; ++j)
-                chol[(size_t)p * 21 + tri(i, j)] = (i == j) ? 1.0 / a[i * 6 + i] : a[i * 6 + j];
+        double* hi = hinv + (size_t)p * 21;
+        if (f == kSuccess) {
+            // H^-1 column by column: L y = e_j, then L^T x = y
+            for (int j = 0; j < 6; ++j) {
+                double x[6];
+                for (int k = 0; k < 6; ++k) {
+                    double acc = (k == j) ? 1.0 : 0.0;
+                    for (int i = 0; i < k; ++i) acc -= a[k * 6 + i] * x[i];
+                    x[k] = acc / a[k * 6 + k];
+                }
+                for (int k = 5; k >= 0; --k) {
+                    double acc = x[k];
+                    for (int i = k + 1; i < 6; ++i) acc -= a[i * 6 + k] * x[i];
+                    x[k] = acc / a[k * 6 + k];
+                }
+                for (int k = j; k < 6; ++k) hi[tri(k, j)] = x[k];
+            }
+        } else {
+            for (int k = 0; k < 21; ++k) hi[k] = 0.0;
+        }
         float* st = stats + (size_t)p * 16;
         st[0] = mean;
         st[1] = rs;
         for (int k = 0; k < 6; ++k) {
-            st[2 + k] = (float)dv[22 + k];
-            st[8 + k] = (float)dv[28 + k];
+            st[2 + k] = (float)dsum[22 + k];
+            st[8 + k] = (float)dsum[28 + k];
         }
         st[14] = 0.f;
         st[15] = 0.f;
@@ -127,11 +160,12 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
                                                        const uint8_t* __restrict__ tar,
                                                        const int2* __restrict__ poi, int n,
                                                        const float* __restrict__ stats,
-                                                       const double* __restrict__ chol,
+                                                       const double* __restrict__ hinv,
                                                        const uint8_t* __restrict__ rflag,
                                                        const float4* __restrict__ lut, int* work, float* u,
                                                        float* v, float* p6, int* iters, uint8_t* flags, int ws) {
     constexpr int NW = THREADS / 32;
+    constexpr unsigned FULL = 0xffffffffu;
     // dynamic shared memory: [S] float2 reference gradients (R_x, R_y), then
     // the [ws][ws] target window
     extern __shared__ __align__(16) float smem_f[];
@@ -143,6 +177,7 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
     float2* grad = reinterpret_cast<float2*>(smem_f);
     float* win = smem_f + 2 * ((S + 1) & ~1);
     const size_t plane = (size_t)g.rw * g.rh;
+    const float inv_s = 1.0f / (float)S;
     // sample k = tid + j*THREADS sits at row l, column m of the subset;
     // stepping j advances (l, m) by (dl, dm) with carry
     const int l_first = tid / SW, m_first = tid - (tid / SW) * SW;
@@ -164,24 +199,45 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
             flags[p] = rf;
             for (int k = 0; k < 6; ++k) p6[(size_t)p * 6 + k] = P[k];
         }
-        // ---- stage the target window and the reference gradients
+        // ---- stage the target window and the reference gradients (rows by
+        // warps, columns by lanes)
         const int wx0 = px + (int)floorf(u0) - g.rx - 4;
         const int wy0 = py + (int)floorf(v0) - g.ry - 4;
         if (!done) {
             if (!USE_LUT) {
-                for (int k = tid; k < ws * ws; k += THREADS) {
-                    const int yy = wy0 + k / ws, xx = wx0 + k % ws;
-                    float t = 0.f;
-                    if (yy >= 0 && yy < g.img_h && xx >= 0 && xx < g.img_w)
-                        t = (float)tar[(size_t)yy * g.pitch + xx];
-                    win[k] = t;
+                for (int yy = wid; yy < ws; yy += NW) {
+                    const int gy = wy0 + yy;
+                    const bool rowok = gy >= 0 && gy < g.img_h;
+                    const uint8_t* trow = tar + (size_t)(rowok ? gy : 0) * g.pitch;
+                    for (int xx = lane; xx < ws; xx += 32) {
+                        const int gx = wx0 + xx;
+                        win[yy * ws + xx] = (rowok && gx >= 0 && gx < g.img_w) ? (float)trow[gx] : 0.f;
+                    }
                 }
             }
-            for (int k = tid; k < S; k += THREADS) {
-                const int l = k / SW, m = k - l * SW;
-                const uint8_t* r = ref + (size_t)(py - g.ry + l) * g.pitch + (px - g.rx + m);
-                grad[k] = make_float2(0.5f * (float)((int)r[1] - (int)r[-1]),
-                                      0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
+            const uint8_t* r0 = ref + (size_t)(py - g.ry) * g.pitch + (px - g.rx);
+            for (int l = wid; l < SH; l += NW) {
+                for (int m = lane; m < SW; m += 32) {
+                    const uint8_t* r = r0 + (size_t)l * g.pitch + m;
+                    grad[l * SW + m] = make_float2(0.5f * (float)((int)r[1] - (int)r[-1]),
+                                                   0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
+                }
+            }
+        }
+        // warp 0, lane k < 6: row k of H^-1 (FP64), sum SD_k and sum SD_k (R - mean)
+        double hrow[6];
+        float sumsd = 0.f, qk = 0.f, rs = 0.f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) hrow[j] = 0.0;
+        if (wid == 0 && !done) {
+            const float* st = stats + (size_t)p * 16;
+            rs = st[1];
+            if (lane < 6) {
+                sumsd = st[2 + lane];
+                qk = st[8 + lane];
+                const double* hi = hinv + (size_t)p * 21;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) hrow[j] = hi[lane >= j ? tri(lane, j) : tri(j, lane)];
             }
         }
         const float c = done ? 0.f : stats[(size_t)p * 16];  // shift: mean(R)
@@ -191,13 +247,19 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
             float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             int oor = 0;
             int l = l_first, m = m_first;
+            // x = px + W00 dx + W01 dy + W02 as two FMAs (the reference rounds
+            // each operation; the difference is an ulp, which moves a
+            // truncated coordinate only at an exact integer, where the
+            // bicubic patch is continuous)
+            const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
 #pragma unroll 2
             for (int k = tid; k < S; k += THREADS) {
-                const float wx = warp_coord(px, Wm[0], m - g.rx, Wm[1], l - g.ry, Wm[2]);
-                const float wy = warp_coord(py, Wm[3], m - g.rx, Wm[4], l - g.ry, Wm[5]);
+                const float dxf = (float)(m - g.rx), dyf = (float)(l - g.ry);
+                const float wx = fmaf(Wm[0], dxf, fmaf(Wm[1], dyf, bx));
+                const float wy = fmaf(Wm[3], dxf, fmaf(Wm[4], dyf, by));
                 const int ix = (int)wx, iy = (int)wy;
                 float t = 0.f;
-                if (ix >= g.sx && iy >= g.sy && ix < g.sx + g.rw && iy < g.sy + g.rh) {
+                if ((unsigned)(ix - g.sx) < (unsigned)g.rw && (unsigned)(iy - g.sy) < (unsigned)g.rh) {
                     const int lx = ix - wx0, ly = iy - wy0;
                     if (it == 0) {  // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
                         t = (!USE_LUT && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
@@ -245,7 +307,7 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
                 }
                 const float2 gr = grad[k];
                 const float tp = t - c;
-                const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
+                const float dx = dxf, dy = dyf;
                 const float a = gr.x * tp, b = gr.y * tp;
                 s[0] += tp;
                 s[1] += tp * tp;
@@ -255,74 +317,74 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
                 m += dm;
                 if (m >= SW) { m -= SW; ++l; }
             }
-            // ---- one reduction (FP32 in warps), then thread 0 finishes the iteration
+            // ---- one reduction (FP32), then warp 0 finishes the iteration:
+            // FP32 scalars, FP64 H^-1 b on lanes 0-5, warp update on lane 0
 #pragma unroll
             for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
-            oor = __any_sync(0xffffffffu, oor);
+            oor = __any_sync(FULL, oor);
             if (lane == 0) {
 #pragma unroll
                 for (int k = 0; k < 8; ++k) red[wid][k] = s[k];
                 red[wid][8] = (float)oor;
             }
             __syncthreads();
-            if (tid == 0) {
-                // final sums in FP64
-                double d[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                float any_oor = 0.f;
-                for (int w = 0; w < NW; ++w) {
-                    for (int k = 0; k < 8; ++k) d[k] += (double)red[w][k];
-                    any_oor += red[w][8];
-                }
-                int flag = kSuccess, cont = 0, set_it = 0;
-                const float* st = stats + (size_t)p * 16;
-                const double Sd = (double)S;
-                const double mean_t = (double)c + d[0] / Sd;
-                const double var = d[1] - d[0] * d[0] / Sd;
-                const float ts = (float)sqrt(var > 0.0 ? var : 0.0);
+            if (wid == 0) {
+                float tot = 0.f;
+                if (lane < 9)
+                    for (int w = 0; w < NW; ++w) tot += red[w][lane];
+                const float S0 = __shfl_sync(FULL, tot, 0), S1 = __shfl_sync(FULL, tot, 1);
+                const float any_oor = __shfl_sync(FULL, tot, 8);
+                const float Ak = __shfl_sync(FULL, tot, 2 + (lane < 6 ? lane : 0));
+                const float m0 = S0 * inv_s;
+                const float mean_t = c + m0;
+                const float var = S1 - S0 * m0;
+                const float ts = sqrtf(var > 0.f ? var : 0.f);
+                int flag = kSuccess, cont = 0;
                 if (any_oor > 0.f) {
                     flag = kOutofROI;
-                } else if (fabs(mean_t) <= (double)FLT_EPSILON || fabsf(ts) <= FLT_EPSILON) {
+                } else if (fabsf(mean_t) <= FLT_EPSILON || fabsf(ts) <= FLT_EPSILON) {
                     flag = kDarkSubset;
                 } else if (it == 0 && rf == kSingularHessian) {
                     flag = kSingularHessian;
-                } else {
-                    const double q = (double)st[1] / (double)ts;
-                    const double m0 = d[0] / Sd;
-                    double b[6];
-                    for (int k = 0; k < 6; ++k) b[k] = q * (d[2 + k] - m0 * (double)st[2 + k]) - (double)st[8 + k];
-                    // FP64 Cholesky solve with the cached factor (reciprocal diagonal)
-                    const double* L = chol + (size_t)p * 21;
-                    for (int k = 0; k < 6; ++k) {
-                        double acc = b[k];
-                        for (int i = 0; i < k; ++i) acc -= L[tri(k, i)] * b[i];
-                        b[k] = acc * L[tri(k, k)];
+                }
+                float dpk = 0.f;
+                if (flag == kSuccess) {
+                    const float q = rs / ts;
+                    const float bk = (lane < 6) ? q * (Ak - m0 * sumsd) - qk : 0.f;
+                    const double bd = (double)bk;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 6; ++j) acc = fma(hrow[j], __shfl_sync(FULL, bd, j), acc);
+                    dpk = (float)acc;
+                }
+                float dp[6];
+#pragma unroll
+                for (int j = 0; j < 6; ++j) dp[j] = __shfl_sync(FULL, dpk, j);
+                if (lane == 0) {
+                    if (flag == kSuccess) {
+                        if (!update_warp(P, dp, Wm)) {
+                            flag = kSingularWarp;
+                        } else {
+                            // scaled ||dP|| >= delta_p, squared, FP32
+                            const float a1 = dp[1] * (float)g.rx, a2 = dp[2] * (float)g.ry;
+                            const float a4 = dp[4] * (float)g.rx, a5 = dp[5] * (float)g.ry;
+                            const float nrm2 = dp[0] * dp[0] + a1 * a1 + a2 * a2 + dp[3] * dp[3] + a4 * a4 + a5 * a5;
+                            cont = (it + 1 < g.max_iter && nrm2 >= g.delta_p * g.delta_p) ? 1 : 0;
+                        }
                     }
-                    for (int k = 5; k >= 0; --k) {
-                        double acc = b[k];
-                        for (int i = k + 1; i < 6; ++i) acc -= L[tri(i, k)] * b[i];
-                        b[k] = acc * L[tri(k, k)];
-                    }
-                    float dp[6];
-                    for (int k = 0; k < 6; ++k) dp[k] = (float)b[k];
-                    if (!update_warp(P, dp, Wm)) {
-                        flag = kSingularWarp;
+                    if (flag == kSuccess && cont) {
+                        for (int k = 0; k < 6; ++k) sW[k] = Wm[k];
                     } else {
-                        cont = (it + 1 < g.max_iter && dp_norm(dp, g.rx, g.ry) >= (double)g.delta_p) ? 1 : 0;
+                        // finish: the counter is it+1 after a solve or an abort in a
+                        // later pass; an abort in the first pass leaves it untouched
+                        flags[p] = (uint8_t)flag;
+                        for (int k = 0; k < 6; ++k) p6[(size_t)p * 6 + k] = P[k];
+                        u[p] = P[0];
+                        v[p] = P[3];
+                        if (flag == kSuccess || it > 0) iters[p] = it + 1;
                     }
+                    sctl[0] = (flag == kSuccess && cont) ? 1 : 0;
                 }
-                if (flag == kSuccess && cont) {
-                    for (int k = 0; k < 6; ++k) sW[k] = Wm[k];
-                } else {
-                    // finish: counter is it+1 after a solve or an abort in a later pass;
-                    // an abort in the first pass leaves it untouched
-                    set_it = (flag == kSuccess) || it > 0;
-                    flags[p] = (uint8_t)flag;
-                    for (int k = 0; k < 6; ++k) p6[(size_t)p * 6 + k] = P[k];
-                    u[p] = P[0];
-                    v[p] = P[3];
-                    if (set_it) iters[p] = it + 1;
-                }
-                sctl[0] = (flag == kSuccess && cont) ? 1 : 0;
             }
             __syncthreads();
             if (!sctl[0]) break;
@@ -355,6 +417,8 @@ static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const u
     const size_t smem = sizeof(float) * (2 * (size_t)((S + 1) & ~1) + (LUT ? 0 : (size_t)ws * ws));
     auto kern = k_icgn_fast<THREADS, LUT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);

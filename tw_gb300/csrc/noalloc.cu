@@ -30,7 +30,7 @@ constexpr size_t kAlign = 256;
 constexpr size_t round_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 // Scratch carving, per POI: 16 floats of reference statistics (64 B), the
-// packed FP64 Cholesky factor (21 doubles, 168 B) and a flag byte; then one
+// packed FP64 inverse Hessian (21 doubles, 168 B) and a flag byte; then one
 // work counter.
 constexpr size_t kStatsOff = 0;
 constexpr size_t kCholOff = kStatsOff + round_up(size_t(TWDIC_NOALLOC_MAX_POIS) * 64);

@@ -113,7 +113,10 @@ int validate(const twdic_params* p, bool need_grid, bool need_border) {
 
 Geom make_geom(const twdic_params& p) {
     Geom g;
-    g.img_w = p.img_width; g.img_h = p.img_height; g.pitch = p.img_width;
+    g.img_w = p.img_width; g.img_h = p.img_height;
+    // engine-owned image rows are padded to 16 bytes: the tensor-memory-access
+    // (TMA) loads of the tensor-core FFT-CC need 16-byte-multiple row strides
+    g.pitch = (p.img_width + 15) & ~15;
     g.sx = p.start_x; g.sy = p.start_y; g.rw = p.roi_width; g.rh = p.roi_height;
     g.rx = p.subset_x; g.ry = p.subset_y;
     g.max_iter = p.max_iterations; g.delta_p = p.delta_p;
@@ -171,7 +174,7 @@ struct Engine {
         TW_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
         stream = own_stream;
         for (auto& e : ev) TW_CUDA(cudaEventCreate(&e));
-        const size_t img = (size_t)p.img_width * p.img_height;
+        const size_t img = (size_t)g.pitch * p.img_height;
         TW_TRY(d_ref.ensure(img));
         TW_TRY(d_tar.ensure(img));
         TW_TRY(d_poi.ensure(sizeof(int2) * (size_t)n));
@@ -207,7 +210,7 @@ struct Engine {
         if (stride == 0) stride = prm.img_width;
         if (stride < prm.img_width) return fail(TWDIC_ERR_INVALID_ARG, "stride %d < width %d", stride, prm.img_width);
         if (mem != TWDIC_MEM_HOST && mem != TWDIC_MEM_DEVICE) return fail(TWDIC_ERR_INVALID_ARG, "bad mem kind");
-        TW_CUDA(cudaMemcpy2DAsync(dst.p, prm.img_width, img, stride, prm.img_width, prm.img_height,
+        TW_CUDA(cudaMemcpy2DAsync(dst.p, g.pitch, img, stride, prm.img_width, prm.img_height,
                                   mem == TWDIC_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, stream));
         return TWDIC_OK;
     }

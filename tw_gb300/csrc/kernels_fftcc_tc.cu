@@ -23,6 +23,8 @@
 // One CTA of 128 threads (one warpgroup) per SM slot, persistent over POI
 // batches; thread 0 issues the MMAs, completion is signalled through an
 // mbarrier (bounded wait), the epilogues read TMEM with tcgen05.ld.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include <cmath>
@@ -39,13 +41,25 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kMaxCand = 16;      // exact re-evaluations per POI
 constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
+constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
 
 struct TcShape {
-    int N, H, HP, NP, PB, tiles1, K4, n_batches, n;
+    int N, H, HP, NP, PB, tiles1, K4, BW, WS, n_batches, n, groups;
+    // shared twiddle tables
     int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
-    int off_a13, off_a2, off_a4, smem_bytes;
+    // per-group operand regions, relative to the group's base
+    int off_a13, off_a2, off_a4, off_win, group_bytes;
+    int smem_bytes;
+};
+
+// Epilogue-4 scratch, placed in the A1/A3 region once stage 3 has read A3.
+struct PeakScratch {
+    float bv[kThreads];
+    int bi[kThreads];
+    int cand[kMaxPB][kMaxCand];
+    int candS[kMaxPB][kMaxCand];
 };
 
 __host__ __device__ __forceinline__ int kmaj(int r, int k, int K) {  // LBO 128 B, SBO 16*K B
@@ -115,79 +129,159 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 2D TMA box load (x must be a multiple of 16 bytes) completing on `bar`
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+// named barrier over the 128 threads of one group
+__device__ __forceinline__ void group_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ int group_sync_or(int id, int v) {
+    int r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.s32 p, %2, 0;\n bar.red.or.pred q, %1, 128, p;\n selp.s32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r) : "r"(id), "r"(v) : "memory");
+    return r;
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 __device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast<__half*>(p) = __float2half_rn(v); }
 
-// ----------------------------------------------------------------- kernel --
-template <int NP>
-__global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, const uint8_t* __restrict__ ref,
-                                                          const uint8_t* __restrict__ tar,
-                                                          const int2* __restrict__ poi,
-                                                          const uint4* __restrict__ tables, float* u, float* v,
-                                                          float* zncc, uint8_t* status, unsigned* err) {
-    extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t tmem_slot;
-    __shared__ int wsum[2 * kMaxPB][2];
-    __shared__ float sscale[kMaxPB];
-    __shared__ int sdark[kMaxPB];
-    __shared__ float sbv[kThreads];
-    __shared__ int sbi[kThreads];
-    __shared__ float sthr[kMaxPB];
-    __shared__ int ncand[kMaxPB];
-    __shared__ int cand[kMaxPB][kMaxCand];
-    __shared__ int candS[kMaxPB][kMaxCand];
-    __shared__ int sabort;
+// Optional phase timing (compiled only with -DTWDIC_TC_TRACE): thread 0 of
+// every group adds the clock64() cycles of each phase of each batch.
+#ifdef TWDIC_TC_TRACE
+__device__ unsigned long long g_tc_trace[16];
+#define TC_MARK(i)                                                           \
+    do {                                                                     \
+        if (t == 0) {                                                        \
+            const long long now_ = clock64();                                \
+            atomicAdd(&g_tc_trace[i], (unsigned long long)(now_ - tmark_));  \
+            tmark_ = now_;                                                   \
+        }                                                                    \
+    } while (0)
+#else
+#define TC_MARK(i) \
+    do {           \
+    } while (0)
+#endif
 
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int N = s.N, H = s.H, HP = s.HP, PB = s.PB, K4 = s.K4;
+// ----------------------------------------------------------------- kernel --
+// blockDim = 128 * s.groups.  Each 128-thread group runs its own batches
+// (own operand buffers, TMEM columns, mbarriers and named barrier) and the
+// groups share the twiddle tables, so one group's load and MMA latency
+// overlaps another's epilogues.
+template <int NP, int HP>
+__global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUtensorMap map_ref,
+                                                     const __grid_constant__ CUtensorMap map_tar, TcShape s, Geom g,
+                                                     const int2* __restrict__ poi,
+                                                     const uint4* __restrict__ tables, float* u, float* v,
+                                                     float* zncc, uint8_t* status, unsigned* err) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ __align__(8) uint64_t mbar_mma[2];
+    __shared__ __align__(8) uint64_t mbar_tma[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int wsum[2][2 * kMaxPB][2];
+    __shared__ float sscale[2][kMaxPB];
+    __shared__ int sdark[2][kMaxPB];
+    __shared__ float sthr[2][kMaxPB];
+    __shared__ int ncand[2][kMaxPB];
+    __shared__ int2 spoi[2][kMaxPB];
+    __shared__ int smis[2][2 * kMaxPB];
+
+    const int grp = threadIdx.x >> 7;
+    const int t = threadIdx.x & 127, warp = t >> 5, lane = t & 31;
+    const int bar_id = 1 + grp;
+    const int N = s.N, H = s.H, PB = s.PB, K4 = s.K4, BW = s.BW, WS = s.WS;
     const int n2 = N * N;
     constexpr int K1 = NP;
+    uint8_t* gbase = sm + s.tab_bytes + grp * s.group_bytes;
+    uint8_t* wwin = gbase + s.off_win;  // [2 PB] TMA boxes of N rows x BW bytes, stride WS
+    PeakScratch* ps = reinterpret_cast<PeakScratch*>(gbase + s.off_a13);
+    uint64_t* mbar = &mbar_mma[grp];
+    uint64_t* tbar = &mbar_tma[grp];
 
-    // ---- set-up: TMEM, mbarrier, twiddle tables, zeroed A2/A4
-    if (warp == 0) {
+    // ---- set-up: TMEM (128 columns per group), mbarriers, tables, zeroed A2/A4
+    if (threadIdx.x < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(kTmemCols));
+                     "r"(kTmemCols * s.groups));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (t == 0) {
-        mbar_init(&mbar);
-        sabort = 0;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < s.groups; ++k) {
+            mbar_init(&mbar_mma[k]);
+            mbar_init(&mbar_tma[k]);
+        }
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_ref)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_tar)) : "memory");
     }
     {
         uint4* dst = reinterpret_cast<uint4*>(sm);
-        for (int i = t; i < s.tab_bytes / 16; i += kThreads) dst[i] = tables[i];
-        uint4* a2 = reinterpret_cast<uint4*>(sm + s.off_a2);
-        for (int i = t; i < (s.smem_bytes - s.off_a2) / 16; i += kThreads) a2[i] = make_uint4(0, 0, 0, 0);
+        for (int i = threadIdx.x; i < s.tab_bytes / 16; i += blockDim.x) dst[i] = tables[i];
+        uint4* a2 = reinterpret_cast<uint4*>(gbase + s.off_a2);
+        for (int i = t; i < (s.off_win - s.off_a2) / 16; i += 128) a2[i] = make_uint4(0, 0, 0, 0);
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tm = tmem_slot;
+    // TMA destinations need 128-byte alignment of the dynamic shared memory
+    if (smem_u32(sm) & 127u) {
+        if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+        if (threadIdx.x < 32)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
+                         "r"(kTmemCols * s.groups));
+        return;
+    }
+    const uint32_t tm = tmem_slot + grp * kTmemCols;
     const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
+    const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
-    uint32_t phase = 0;
+    uint32_t phase = 0, tphase = 0;
+#ifdef TWDIC_TC_TRACE
+    long long tmark_ = clock64();
+#endif
 
-    for (int batch = blockIdx.x; batch < s.n_batches; batch += gridDim.x) {
+    for (int batch = blockIdx.x * s.groups + grp; batch < s.n_batches; batch += gridDim.x * s.groups) {
         const int b0 = batch * PB;
-        if (t < 2 * kMaxPB * 2) (&wsum[0][0])[t] = 0;
-        __syncthreads();
+        if (t < 2 * kMaxPB * 2) (&wsum[grp][0][0])[t] = 0;
+        if (t < PB) spoi[grp][t] = (b0 + t < s.n) ? poi[b0 + t] : make_int2(-1, -1);
+        group_sync(bar_id);
 
-        // ---- phase L: windows -> A1 (rows (window, x), K = y), exact FP16
-        for (int rr = t; rr < s.tiles1 * 128; rr += kThreads) {
-            const int wi = rr / N, x = rr - wi * N;
-            const int p = wi >> 1;
-            const bool valid = wi < 2 * PB && b0 + p < s.n;
-            const uint8_t* base = nullptr;
-            if (valid) {
-                const int2 pyx = poi[b0 + p];
-                base = ((wi & 1) ? tar : ref) + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx) + x;
+        // ---- phase L1: one TMA box per window ([N rows][BW bytes], x aligned
+        // down to 16 bytes; out-of-bounds parts are zero-filled)
+        if (t == 0) {
+            fence_async_smem();  // the previous batch's generic reads of the windows come first
+            int nload = 0;
+            for (int wi = 0; wi < 2 * PB; ++wi) nload += spoi[grp][wi >> 1].x >= 0;
+            mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
+            for (int wi = 0; wi < 2 * PB; ++wi) {
+                const int2 pyx = spoi[grp][wi >> 1];
+                if (pyx.x < 0) continue;
+                const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
+                const int xa = x0 & ~15;
+                smis[grp][wi] = x0 - xa;
+                tma_load_2d(wwin + wi * WS, (wi & 1) ? &map_tar : &map_ref, xa, y0, tbar);
             }
-            uint8_t* a1 = sm + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
+        }
+        bool ok = mbar_wait(tbar, tphase);
+        tphase ^= 1u;
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        TC_MARK(0);
+
+        // ---- phase L2: windows -> A1 (rows (window, x), K = y), exact FP16;
+        // integer sums per window by segmented warp reductions
+        for (int rr = t; rr < s.tiles1 * 128; rr += 128) {
+            const int wi = rr / N, x = rr - wi * N;
+            const bool data = wi < 2 * PB && spoi[grp][wi >> 1].x >= 0;
+            const uint8_t* col = wwin + (data ? wi : 0) * WS + (data ? smis[grp][wi] : 0) + x;
+            uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
             const int row = rr & 127;
             int su = 0, sq = 0;
 #pragma unroll
@@ -196,7 +290,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int y = c * 8 + j;
-                    const int val = (valid && y < N) ? (int)base[(size_t)y * g.pitch] : 0;
+                    const int val = (data && y < N) ? (int)col[y * BW] : 0;
                     su += val;
                     sq += val * val;
                     f[j] = (float)val;
@@ -205,19 +299,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                 q.x = pack2(f[0], f[1]); q.y = pack2(f[2], f[3]); q.z = pack2(f[4], f[5]); q.w = pack2(f[6], f[7]);
                 *reinterpret_cast<uint4*>(a1 + kmaj(row, c * 8, K1)) = q;
             }
-            if (valid) {
-                atomicAdd(&wsum[wi][0], su);
-                atomicAdd(&wsum[wi][1], sq);
+            const int key = data ? wi : -1;
+            const unsigned seg = __match_any_sync(kFull, key);
+            const int gs = __reduce_add_sync(seg, su), gq = __reduce_add_sync(seg, sq);
+            if (data && lane == __ffs(seg) - 1) {
+                atomicAdd(&wsum[grp][wi][0], gs);
+                atomicAdd(&wsum[grp][wi][1], gq);
             }
         }
         fence_async_smem();
-        __syncthreads();
+        group_sync(bar_id);
+        TC_MARK(1);
 
         // ---- stage 1: D1[(w,x)][(part,ky)] = A1 * B1
         if (t == 0) {
             tc_fence_after();
             for (int tile = 0; tile < s.tiles1; ++tile) {
-                const uint32_t a0 = sbase + s.off_a13 + tile * (128 * K1 * 2);
+                const uint32_t a0 = gaddr + s.off_a13 + tile * (128 * K1 * 2);
                 for (int kk = 0; kk < K1 / 16; ++kk) {
                     const uint64_t a = sdesc(a0 + kk * 256, 128, 16 * K1);
                     const uint64_t bh = sdesc(sbase + s.off_b1h + kk * 256, 128, 16 * K1);
@@ -226,50 +324,63 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                     mma_f16(tm + tile * 2 * HP, a, bl, idesc_f16(2 * HP, false), 1);
                 }
             }
-            mma_commit(&mbar);
+            mma_commit(mbar);
         }
         // per-POI normalisation while the MMAs run: 1/sqrt(nf ng) with
         // nf = sum (f - mean)^2 = (n sum f^2 - (sum f)^2) / n, exact in integers
         if (t < PB) {
             const int wf = 2 * t, wg = 2 * t + 1;
-            const long long numf = (long long)n2 * wsum[wf][1] - (long long)wsum[wf][0] * wsum[wf][0];
-            const long long numg = (long long)n2 * wsum[wg][1] - (long long)wsum[wg][0] * wsum[wg][0];
+            const long long numf = (long long)n2 * wsum[grp][wf][1] - (long long)wsum[grp][wf][0] * wsum[grp][wf][0];
+            const long long numg = (long long)n2 * wsum[grp][wg][1] - (long long)wsum[grp][wg][0] * wsum[grp][wg][0];
             const bool dark = b0 + t >= s.n || numf == 0 || numg == 0;
-            sdark[t] = dark ? 1 : 0;
-            sscale[t] = dark ? 0.f : (float)((double)n2 / sqrt((double)numf * (double)numg));
+            sdark[grp][t] = dark ? 1 : 0;
+            sscale[grp][t] = dark ? 0.f : (float)((double)n2 / sqrt((double)numf * (double)numg));
         }
-        bool ok = mbar_wait(&mbar, phase);
+        ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
+        TC_MARK(2);
 
         // ---- epilogue 1: Y -> A2 (rows (p, ky, w), K = (part, x)), FP16
         for (int tile = 0; tile < s.tiles1; ++tile) {
-            float d[2 * 40];
+            float d[2 * HP];
+#pragma unroll
             for (int c = 0; c < 2 * HP; c += 16) tmem_ld16(tm_warp + tile * 2 * HP + c, d + c);
             tmem_ld_wait();
             const int rr = tile * 128 + t;
             const int wi = rr / N, x = rr - wi * N;
             if (wi < 2 * PB) {
                 const int p = wi >> 1, wsel = wi & 1;
-                uint8_t* a2 = sm + s.off_a2;
-                for (int ky = 0; ky < H; ++ky) {
-                    const int r2 = (p * H + ky) * 2 + wsel;
-                    st_half(a2 + kmaj144(r2, x, 2 * NP), d[ky]);
-                    st_half(a2 + kmaj144(r2, NP + x, 2 * NP), d[HP + ky]);
+                // rows r2 = (p H + ky) 2 + wsel step by 2: +32 B inside an 8-row
+                // group, +SBO - 96 B when the step crosses into the next group
+                int r2 = (p * H) * 2 + wsel;
+                uint8_t* rowp = gbase + s.off_a2 + kmaj144(r2, 0, 2 * NP);
+                const int kre = (x >> 3) * 144 + (x & 7) * 2;
+                const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
+                const int sbo = 36 * NP;
+#pragma unroll
+                for (int ky = 0; ky < HP; ++ky) {
+                    if (ky < H) {
+                        st_half(rowp + kre, d[ky]);
+                        st_half(rowp + kim, d[HP + ky]);
+                        r2 += 2;
+                        rowp += ((r2 & 7) < 2) ? (sbo - 96) : 32;
+                    }
                 }
             }
         }
         tc_fence_before();
         fence_async_smem();
-        __syncthreads();
+        group_sync(bar_id);
+        TC_MARK(3);
 
         // ---- stage 2: F = Y * W (rows (p,ky,w); columns Re kx | Im kx)
         if (t == 0) {
             tc_fence_after();
             for (int kk = 0; kk < NP / 16; ++kk) {
-                const uint64_t ar = sdesc(sbase + s.off_a2 + kk * 288, 144, 36 * NP);
-                const uint64_t ai = sdesc(sbase + s.off_a2 + (NP / 8 + 2 * kk) * 144, 144, 36 * NP);
+                const uint64_t ar = sdesc(gaddr + s.off_a2 + kk * 288, 144, 36 * NP);
+                const uint64_t ai = sdesc(gaddr + s.off_a2 + (NP / 8 + 2 * kk) * 144, 144, 36 * NP);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
                 const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
                 const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
@@ -284,16 +395,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                 mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
                 mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
             }
-            mma_commit(&mbar);
+            mma_commit(mbar);
         }
-        ok = mbar_wait(&mbar, phase);
+        ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
+        TC_MARK(4);
 
         // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
         {
             float re[NP], im[NP];
+#pragma unroll
             for (int c = 0; c < NP; c += 16) {
                 tmem_ld16(tm_warp + c, re + c);
                 tmem_ld16(tm_warp + NP + c, im + c);
@@ -303,9 +416,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
             const int p = rowv ? t / (2 * H) : 0;
             const int ky = rowv ? (t >> 1) % H : 0;
             const int wsel = t & 1;
-            const float sc = rowv ? sscale[p] : 0.f;
+            const float sc = rowv ? sscale[grp][p] : 0.f;
             const int r3 = p * H + ky;
-            uint8_t* a3 = sm + s.off_a13;
+            uint8_t* a3 = gbase + s.off_a13;
             constexpr int HALF = NP / 2;
             float br[8], bi[8];
 #pragma unroll
@@ -314,8 +427,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                 const float own_i = wsel ? im[HALF + i] : im[i];
                 const float snd_r = wsel ? re[i] : re[HALF + i];
                 const float snd_i = wsel ? im[i] : im[HALF + i];
-                const float oth_r = __shfl_xor_sync(0xffffffffu, snd_r, 1);
-                const float oth_i = __shfl_xor_sync(0xffffffffu, snd_i, 1);
+                const float oth_r = __shfl_xor_sync(kFull, snd_r, 1);
+                const float oth_i = __shfl_xor_sync(kFull, snd_i, 1);
                 const float fr = wsel ? oth_r : own_r, fi = wsel ? oth_i : own_i;
                 const float gr = wsel ? own_r : oth_r, gi = wsel ? own_i : oth_i;
                 const int kx = wsel ? HALF + i : i;
@@ -343,14 +456,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
         }
         tc_fence_before();
         fence_async_smem();
-        __syncthreads();
+        group_sync(bar_id);
+        TC_MARK(5);
 
         // ---- stage 3: conj(Z) = conj(C) * W (rows (p,ky); columns Re x | Im x)
         if (t == 0) {
             tc_fence_after();
             for (int kk = 0; kk < NP / 16; ++kk) {
-                const uint64_t ar = sdesc(sbase + s.off_a13 + kk * 256, 128, 32 * NP);
-                const uint64_t ai = sdesc(sbase + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 32 * NP);
+                const uint64_t ar = sdesc(gaddr + s.off_a13 + kk * 256, 128, 32 * NP);
+                const uint64_t ai = sdesc(gaddr + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 32 * NP);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
                 const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
                 const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
@@ -365,16 +479,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                 mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
                 mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
             }
-            mma_commit(&mbar);
+            mma_commit(mbar);
         }
-        ok = mbar_wait(&mbar, phase);
+        ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
+        TC_MARK(6);
 
         // ---- epilogue 3: Z -> A4 (rows (p, x), K = (part, ky)), c2r weights folded in
         {
             float re[NP], im[NP];
+#pragma unroll
             for (int c = 0; c < NP; c += 16) {
                 tmem_ld16(tm_warp + c, re + c);
                 tmem_ld16(tm_warp + NP + c, im + c);
@@ -383,116 +499,137 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
             if (t < PB * H) {
                 const int p = t / H, ky = t - (t / H) * H;
                 const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
-                uint8_t* a4 = sm + s.off_a4;
+                // rows r4 = p N + x step by 1: +16 B inside an 8-row group,
+                // +SBO - 112 B when the step crosses into the next group
+                int r4 = p * N;
+                uint8_t* rowp = gbase + s.off_a4 + kmaj(r4, 0, K4);
+                const int kre = (ky >> 3) * 128 + (ky & 7) * 2;
+                const int kim = ((HP + ky) >> 3) * 128 + ((HP + ky) & 7) * 2;
+                const int sbo = 16 * K4;
 #pragma unroll
                 for (int x = 0; x < NP; ++x) {
                     if (x < N) {
-                        const int r4 = p * N + x;
-                        st_half(a4 + kmaj144(r4, ky, K4), wgt * re[x]);
-                        st_half(a4 + kmaj144(r4, HP + ky, K4), -wgt * im[x]);  // Zi = -D_i
+                        st_half(rowp + kre, wgt * re[x]);
+                        st_half(rowp + kim, -wgt * im[x]);  // Zi = -D_i
+                        ++r4;
+                        rowp += ((r4 & 7) == 0) ? (sbo - 112) : 16;
                     }
                 }
             }
         }
         tc_fence_before();
         fence_async_smem();
-        __syncthreads();
+        group_sync(bar_id);
+        TC_MARK(7);
 
         // ---- stage 4: c[(p,x)][y] = A4 * B4
         if (t == 0) {
             tc_fence_after();
             for (int kk = 0; kk < K4 / 16; ++kk) {
-                const uint64_t a = sdesc(sbase + s.off_a4 + kk * 288, 144, 18 * K4);
+                const uint64_t a = sdesc(gaddr + s.off_a4 + kk * 256, 128, 16 * K4);
                 const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
                 const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
                 mma_f16(tm, a, bh, idesc_f16(NP, false), kk > 0);
                 mma_f16(tm, a, bl, idesc_f16(NP, false), 1);
             }
-            mma_commit(&mbar);
+            mma_commit(mbar);
         }
-        ok = mbar_wait(&mbar, phase);
+        ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (__syncthreads_or(!ok)) { if (t == 0) { sabort = 1; atomicOr(err, kErrTimeout); } break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
+        TC_MARK(8);
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
+        // (scratch in the A1/A3 region, which stage 3 has finished reading)
         float cv[NP];
+#pragma unroll
         for (int c = 0; c < NP; c += 16) tmem_ld16(tm_warp + c, cv + c);
         tmem_ld_wait();
         tc_fence_before();
         const bool rowv = t < PB * N;
         const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
+        const bool live = rowv && !sdark[grp][p4];
         {
             float bv = -3.4e38f;
             int bi = 0x7fffffff;
-            if (rowv && !sdark[p4]) {
+            if (live) {
 #pragma unroll
                 for (int y = 0; y < NP; ++y)
                     if (y < N && cv[y] > bv) { bv = cv[y]; bi = y * N + x4; }
             }
-            sbv[t] = bv;
-            sbi[t] = bi;
+            ps->bv[t] = bv;
+            ps->bi[t] = bi;
         }
-        __syncthreads();
+        group_sync(bar_id);
         if (t < PB) {
             float bv = -3.4e38f;
             int bi = 0x7fffffff;
-            for (int r = t * N; r < t * N + N; ++r) argmax_merge(bv, bi, sbv[r], sbi[r]);
-            sthr[t] = bv - 0.02f * (float)n2;
-            ncand[t] = 1;
-            cand[t][0] = bi;
+            for (int r = t * N; r < t * N + N; ++r) argmax_merge(bv, bi, ps->bv[r], ps->bi[r]);
+            sthr[grp][t] = bv - 0.02f * (float)n2;
+            ncand[grp][t] = 1;
+            ps->cand[t][0] = bi;
         }
-        __syncthreads();
-        if (rowv && !sdark[p4]) {
+        group_sync(bar_id);
+        if (live) {
+            const float th = sthr[grp][p4];
+            const int first = ps->cand[p4][0];
 #pragma unroll
             for (int y = 0; y < NP; ++y) {
-                if (y < N && cv[y] >= sthr[p4]) {
+                if (y < N && cv[y] >= th) {
                     const int idx = y * N + x4;
-                    if (idx != cand[p4][0]) {
-                        const int slot = atomicAdd(&ncand[p4], 1);
-                        if (slot < kMaxCand) cand[p4][slot] = idx;
+                    if (idx != first) {
+                        const int slot = atomicAdd(&ncand[grp][p4], 1);
+                        if (slot < kMaxCand) ps->cand[p4][slot] = idx;
                     }
                 }
             }
         }
-        __syncthreads();
-        // exact integer correlation of every candidate, one warp per (POI, candidate)
-        for (int task = warp; task < PB * kMaxCand; task += kThreads / 32) {
+        group_sync(bar_id);
+        TC_MARK(9);
+        // exact integer correlation of every candidate from the staged windows,
+        // one warp per (POI, candidate); lanes take columns, so the column
+        // wrap of the shift is fixed per lane and the rows wrap once
+        for (int task = warp; task < PB * kMaxCand; task += 4) {
             const int p = task / kMaxCand, slot = task - p * kMaxCand;
-            if (sdark[p] || slot >= min(ncand[p], kMaxCand)) continue;
-            const int idx = cand[p][slot];
+            if (sdark[grp][p] || slot >= min(ncand[grp][p], kMaxCand)) continue;
+            const int idx = ps->cand[p][slot];
             const int kx = idx % N, ky = idx / N;
-            const int2 pyx = poi[b0 + p];
-            const uint8_t* fb = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
-            const uint8_t* gb = tar + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
+            const uint8_t* fw = wwin + (2 * p) * WS + smis[grp][2 * p];
+            const uint8_t* gw = wwin + (2 * p + 1) * WS + smis[grp][2 * p + 1];
             int acc = 0;
-            for (int q = lane; q < n2; q += 32) {
-                const int y = q / N, x = q - (q / N) * N;
-                int yy = y + ky; if (yy >= N) yy -= N;
-                int xx = x + kx; if (xx >= N) xx -= N;
-                acc += (int)fb[(size_t)y * g.pitch + x] * (int)gb[(size_t)yy * g.pitch + xx];
+            for (int x = lane; x < N; x += 32) {
+                int xx = x + kx;
+                if (xx >= N) xx -= N;
+                const uint8_t* fc = fw + x;
+                const uint8_t* gc = gw + xx;
+                const int split = N - ky;  // rows y < split pair with y + ky, the rest with y + ky - N
+#pragma unroll 4
+                for (int y = 0; y < split; ++y) acc += (int)fc[y * BW] * (int)gc[(y + ky) * BW];
+#pragma unroll 4
+                for (int y = split; y < N; ++y) acc += (int)fc[y * BW] * (int)gc[(y - split) * BW];
             }
             acc = warp_sum(acc);
-            if (lane == 0) candS[p][slot] = acc;
+            if (lane == 0) ps->candS[p][slot] = acc;
         }
-        __syncthreads();
+        group_sync(bar_id);
         if (t < PB && b0 + t < s.n) {
             const int gp = b0 + t;
-            if (sdark[t]) {
+            if (sdark[grp][t]) {
                 status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
             } else {
-                const int nc = min(ncand[t], kMaxCand);
-                int best = cand[t][0], bs = candS[t][0];
+                const int nc = min(ncand[grp][t], kMaxCand);
+                int best = ps->cand[t][0], bs = ps->candS[t][0];
                 for (int c = 1; c < nc; ++c) {
-                    const int sc = candS[t][c], id = cand[t][c];
+                    const int sc = ps->candS[t][c], id = ps->cand[t][c];
                     if (sc > bs || (sc == bs && id < best)) { bs = sc; best = id; }
                 }
                 int iu = best % N, iv = best / N;
                 if (iu > g.rx) iu -= N;
                 if (iv > g.ry) iv -= N;
-                const long long sf = wsum[2 * t][0], sg = wsum[2 * t + 1][0];
-                const long long numf = (long long)n2 * wsum[2 * t][1] - sf * sf;
-                const long long numg = (long long)n2 * wsum[2 * t + 1][1] - sg * sg;
+                const long long sf = wsum[grp][2 * t][0], sg = wsum[grp][2 * t + 1][0];
+                const long long numf = (long long)n2 * wsum[grp][2 * t][1] - sf * sf;
+                const long long numg = (long long)n2 * wsum[grp][2 * t + 1][1] - sg * sg;
                 const double cnum = (double)((long long)n2 * bs - sf * sg);
                 u[gp] = (float)iu;
                 v[gp] = (float)iv;
@@ -500,14 +637,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_fftcc_tc(TcShape s, Geom g, con
                 status[gp] = 0;
             }
         }
-        __syncthreads();
+        group_sync(bar_id);
+        TC_MARK(10);
     }
 
     // ---- teardown
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kTmemCols));
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
+                     "r"(kTmemCols * s.groups));
 }
 
 // ----------------------------------------------------------- host side ----
@@ -544,12 +684,22 @@ bool make_shape(const Geom& g, int n, TcShape& s) {
     s.off_s2l = o; o += NP * NP * 2;
     s.off_b4h = o; o += NP * K4 * 2;
     s.off_b4l = o; o += NP * K4 * 2;
-    s.tab_bytes = o;
-    s.off_a13 = o; o += std::max(s.tiles1 * 128 * K1 * 2, 128 * 2 * NP * 2);
-    s.off_a2 = o; o += 16 * 36 * NP;
-    s.off_a4 = o; o += 16 * 18 * K4;
-    s.smem_bytes = o;
-    return s.smem_bytes <= 200 * 1024;
+    s.tab_bytes = round_up(o, 1024);
+    o = s.tab_bytes;
+    // per-group regions
+    s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
+    int q = 0;
+    s.off_a13 = q;
+    q += std::max(std::max(s.tiles1 * 128 * K1 * 2, 128 * 2 * NP * 2), (int)sizeof(PeakScratch));
+    s.off_a2 = q; q += 16 * 36 * NP;
+    s.off_a4 = q; q += 16 * 16 * K4;
+    s.WS = round_up(N * s.BW, 128);  // window stride (TMA destinations are 128-byte aligned)
+    s.off_win = q; q += 2 * pb * s.WS;
+    s.group_bytes = round_up(q, 1024);
+    const int limit = 225 * 1024;
+    s.groups = (o + 2 * s.group_bytes <= limit) ? 2 : 1;
+    s.smem_bytes = o + s.groups * s.group_bytes;
+    return s.smem_bytes <= limit;
 }
 
 // Twiddle matrices B1, C2, S2, B4 (hi and lo FP16) in the no-swizzle K-major
@@ -592,14 +742,51 @@ struct TablesCache {
 
 bool fftcc_tc_supported(const Geom& g) {
     TcShape s;
-    return make_shape(g, 1, s);
+    return (g.pitch % 16) == 0 && make_shape(g, 1, s);
 }
+
+namespace {
+
+// cuTensorMapEncodeTiled, resolved once through the runtime (no link-time
+// dependency on libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// 8-bit image as a 2D tensor (x = column, y = row) read in boxes of
+// BW x N bytes; reads outside the image are zero-filled
+bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape& s) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)g.img_w, (cuuint64_t)g.img_h};
+    const cuuint64_t strides[1] = {(cuuint64_t)g.pitch};
+    const cuuint32_t box[2] = {(cuuint32_t)s.BW, (cuuint32_t)s.N};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(img), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
 
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                             float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     TcShape s;
-    if (!make_shape(g, n, s)) return cudaErrorNotSupported;
+    if (!make_shape(g, n, s) || (g.pitch % 16) != 0 || (reinterpret_cast<uintptr_t>(ref) & 15) ||
+        (reinterpret_cast<uintptr_t>(tar) & 15))
+        return cudaErrorNotSupported;
+    CUtensorMap map_ref, map_tar;
+    if (!image_map(&map_ref, g, ref, s) || !image_map(&map_tar, g, tar, s)) return cudaErrorNotSupported;
     static thread_local TablesCache cache;
     if (cache.N != s.N) {
         if (cache.dev) cudaFree(cache.dev);
@@ -615,24 +802,41 @@ cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* ta
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void (*kern)(TcShape, Geom, const uint8_t*, const uint8_t*, const int2*, const uint4*, float*, float*, float*,
-                 uint8_t*, unsigned*) = nullptr;
-    switch (s.NP) {
-        case 16: kern = k_fftcc_tc<16>; break;
-        case 32: kern = k_fftcc_tc<32>; break;
-        case 48: kern = k_fftcc_tc<48>; break;
-        case 64: kern = k_fftcc_tc<64>; break;
+    void (*kern)(const CUtensorMap, const CUtensorMap, TcShape, Geom, const int2*, const uint4*, float*, float*,
+                 float*, uint8_t*, unsigned*) = nullptr;
+    switch (s.NP * 100 + s.HP) {
+        case 1608: kern = k_fftcc_tc<16, 8>; break;
+        case 1616: kern = k_fftcc_tc<16, 16>; break;
+        case 3216: kern = k_fftcc_tc<32, 16>; break;
+        case 3224: kern = k_fftcc_tc<32, 24>; break;
+        case 4824: kern = k_fftcc_tc<48, 24>; break;
+        case 4832: kern = k_fftcc_tc<48, 32>; break;
+        case 6432: kern = k_fftcc_tc<64, 32>; break;
+        case 6440: kern = k_fftcc_tc<64, 40>; break;
         default: return cudaErrorNotSupported;
     }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, s.smem_bytes);
     if (e != cudaSuccess) return e;
-    int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, s.smem_bytes);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    occ = std::max(1, std::min(occ, 4));  // TMEM: 128 columns per CTA, 512 per SM
-    int grid = std::min(sms * occ, s.n_batches);
-    kern<<<grid, kThreads, s.smem_bytes, st>>>(s, g, ref, tar, poi, cache.dev, u, v, zncc, status, err);
+    // one CTA per SM holds two groups when shared memory allows; with one
+    // group, two CTAs share an SM when they fit
+    const int threads = kThreads * s.groups;
+    int occ = 1;
+    if (s.groups == 1 && 2 * (s.smem_bytes + 2048) <= 228 * 1024) occ = 2;
+    const int grid = std::max(1, std::min(sms * occ, (s.n_batches + s.groups - 1) / s.groups));
+    kern<<<grid, threads, s.smem_bytes, st>>>(map_ref, map_tar, s, g, poi, cache.dev, u, v, zncc, status, err);
     return cudaGetLastError();
 }
 
 }  // namespace twdic
+
+#ifdef TWDIC_TC_TRACE
+// Trace builds only: copy out and clear the per-phase cycle counters.
+extern "C" __attribute__((visibility("default"))) int twdic_tc_trace_read(unsigned long long* out16) {
+    cudaDeviceSynchronize();
+    if (cudaMemcpyFromSymbol(out16, twdic::g_tc_trace, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
+    unsigned long long z[16] = {};
+    return cudaMemcpyToSymbol(twdic::g_tc_trace, z, sizeof(z)) == cudaSuccess ? 0 : -1;
+}
+#endif

@@ -22,6 +22,8 @@
 // with central-difference derivatives (TW_utils.cpp:604-700) is algebraically
 // the separable Catmull-Rom kernel on the 4x4 neighbourhood, so no per-frame
 // LUT is built; the LUT's zero last ROI row and column are reproduced.
+#include <cuda_fp16.h>
+
 #include "dic_common.cuh"
 #include "dic_kernels.h"
 
@@ -29,121 +31,139 @@ namespace twdic {
 
 namespace {
 
-constexpr int kPreThreads = 128;
+constexpr int kPreThreads = 256;
 
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
 // Per-reference precompute (TW_paDIC_ICGN2D_CPU.cpp:516-595, :676-693).
-// Per-thread FP32 partial sums (exact for the intensity sum) and FP32 warp
-// sums; the final cross-warp sums are FP64, one value per lane of warp 0.
-// Thread 0 factors the Hessian (Cholesky, FP64) and forms H^-1 = L^-T L^-1
-// from the factor in FP64, stored packed (21 doubles) for the per-iteration
-// FP64 solve.  On GB300 an FP64 warp instruction holds the FP64 pipe for
-// many cycles whatever its active lanes, so FP64 work is kept to a few
-// lane-parallel instructions.
+// One warp per POI for the subset sums (FP32 lane partials, FP32 warp sums);
+// then the 6x6 factorizations of the CTA's kPrePois POIs run lane-parallel,
+// one POI per lane, in FP64: Cholesky, then H^-1 = L^-T L^-1 stored packed
+// (21 doubles) for the per-iteration solve.  On GB300 an FP64 warp
+// instruction holds the FP64 pipe for many cycles whatever its active lanes,
+// so each FP64 instruction here serves 32 POIs.
+constexpr int kPrePois = 32;
+
 __global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, const uint8_t* __restrict__ ref,
                                                                       const int2* __restrict__ poi, int n,
                                                                       float* stats, double* hinv,
                                                                       uint8_t* rflag) {
-    const int p = blockIdx.x;
-    if (p >= n) return;
-    const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
-    const int2 pyx = poi[p];
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     constexpr int NW = kPreThreads / 32;
-    __shared__ float fred[NW][34];
-    __shared__ double dsum[34];
-    __shared__ int ired[NW];
-    if (pyx.x - g.ry < g.sy || pyx.y - g.rx < g.sx || pyx.x + g.ry >= g.sy + g.rh || pyx.y + g.rx >= g.sx + g.rw) {
-        if (tid == 0) rflag[p] = kOutofROI;
+    __shared__ float fsum[kPrePois][35];  // [0..20] H lower, [21] sum (R-mean)^2, [22..27] sum SD, [28..33] sum SD (R-mean), [34] mean
+    __shared__ int sflag[kPrePois];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
+    const int base = blockIdx.x * kPrePois;
+    for (int slot = wid; slot < kPrePois; slot += NW) {
+        const int p = base + slot;
+        if (p >= n) {
+            if (lane == 0) sflag[slot] = -1;
+            continue;
+        }
+        const int2 pyx = poi[p];
+        if (pyx.x - g.ry < g.sy || pyx.y - g.rx < g.sx || pyx.x + g.ry >= g.sy + g.rh || pyx.y + g.rx >= g.sx + g.rw) {
+            if (lane == 0) sflag[slot] = kOutofROI;
+            continue;
+        }
+        const uint8_t* r0 = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
+        int isum = 0;
+        for (int l = 0; l < SH; ++l)
+            for (int m = lane; m < SW; m += 32) isum += r0[(size_t)l * g.pitch + m];
+        isum = warp_sum(isum);
+        const float mean = (float)isum / (float)S;  // bit-equal to the reference's mean
+        float h[34];
+#pragma unroll
+        for (int k = 0; k < 34; ++k) h[k] = 0.f;
+        for (int l = 0; l < SH; ++l) {
+            for (int m = lane; m < SW; m += 32) {
+                const uint8_t* r = r0 + (size_t)l * g.pitch + m;
+                const float rx = 0.5f * (float)((int)r[1] - (int)r[-1]);
+                const float ry = 0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]);
+                const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
+                const float d[6] = {rx, rx * dx, rx * dy, ry, ry * dx, ry * dy};
+                const float rt = (float)r[0] - mean;
+                int q = 0;
+#pragma unroll
+                for (int a = 0; a < 6; ++a)
+#pragma unroll
+                    for (int b = 0; b <= a; ++b) h[q++] += d[a] * d[b];
+                h[21] += rt * rt;
+#pragma unroll
+                for (int a = 0; a < 6; ++a) {
+                    h[22 + a] += d[a];
+                    h[28 + a] += d[a] * rt;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 34; ++k) {
+            const float w = warp_sum(h[k]);  // every lane holds the total
+            if (lane == (k & 31)) fsum[slot][k] = w;
+        }
+        if (lane == 0) {
+            fsum[slot][34] = mean;
+            sflag[slot] = kSuccess;
+        }
+    }
+    __syncthreads();
+    if (wid != 0) return;
+    // lane-parallel FP64 factorization, one POI per lane
+    const int slot = lane, p = base + lane;
+    const int f0 = sflag[slot];
+    if (f0 < 0) return;
+    float* st = stats + (size_t)p * 16;
+    double* hi = hinv + (size_t)p * 21;
+    if (f0 == kOutofROI) {
+        rflag[p] = kOutofROI;
         return;
     }
-    const uint8_t* r0 = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
-    int isum[1] = {0};
-    for (int l = wid; l < SH; l += NW)
-        for (int m = lane; m < SW; m += 32) isum[0] += r0[(size_t)l * g.pitch + m];
-    block_sum<kPreThreads, 1>(isum, ired);
-    const float mean = (float)isum[0] / (float)S;  // bit-equal to the reference's mean
-    // [0..20] Hessian lower triangle, [21] sum (R-mean)^2, [22..27] sum SD_k,
-    // [28..33] sum SD_k (R - mean)
-    float h[34];
-#pragma unroll
-    for (int k = 0; k < 34; ++k) h[k] = 0.f;
-    for (int l = wid; l < SH; l += NW) {
-        for (int m = lane; m < SW; m += 32) {
-            const uint8_t* r = r0 + (size_t)l * g.pitch + m;
-            const float rx = 0.5f * (float)((int)r[1] - (int)r[-1]);
-            const float ry = 0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]);
-            const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
-            const float d[6] = {rx, rx * dx, rx * dy, ry, ry * dx, ry * dy};
-            const float rt = (float)r[0] - mean;
-            int q = 0;
-#pragma unroll
-            for (int a = 0; a < 6; ++a)
-#pragma unroll
-                for (int b = 0; b <= a; ++b) h[q++] += d[a] * d[b];
-            h[21] += rt * rt;
-#pragma unroll
-            for (int a = 0; a < 6; ++a) {
-                h[22 + a] += d[a];
-                h[28 + a] += d[a] * rt;
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < 34; ++k) {
-        const float w = warp_sum(h[k]);
-        if (lane == 0) fred[wid][k] = w;
-    }
-    __syncthreads();
-    if (wid == 0) {
-        for (int k = lane; k < 34; k += 32) {
-            double a = 0.0;
-            for (int w = 0; w < NW; ++w) a += (double)fred[w][k];
-            dsum[k] = a;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const float rs = (float)sqrt(dsum[21]);
-        uint8_t f = kSuccess;
-        if (fabsf(mean) <= FLT_EPSILON || fabsf(rs) <= FLT_EPSILON) f = kDarkSubset;
-        double a[36];
+    const float mean = fsum[slot][34];
+    const float rs = (float)sqrt((double)fsum[slot][21]);
+    uint8_t f = kSuccess;
+    if (fabsf(mean) <= FLT_EPSILON || fabsf(rs) <= FLT_EPSILON) f = kDarkSubset;
+    double a[36];
+    {
         int q = 0;
+#pragma unroll
         for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) a[i * 6 + j] = (j <= i) ? dsum[q++] : 0.0;
-        if (f == kSuccess && potrf6(a) > 0) f = kSingularHessian;
-        double* hi = hinv + (size_t)p * 21;
-        if (f == kSuccess) {
-            // H^-1 column by column: L y = e_j, then L^T x = y
-            for (int j = 0; j < 6; ++j) {
-                double x[6];
-                for (int k = 0; k < 6; ++k) {
-                    double acc = (k == j) ? 1.0 : 0.0;
-                    for (int i = 0; i < k; ++i) acc -= a[k * 6 + i] * x[i];
-                    x[k] = acc / a[k * 6 + k];
-                }
-                for (int k = 5; k >= 0; --k) {
-                    double acc = x[k];
-                    for (int i = k + 1; i < 6; ++i) acc -= a[i * 6 + k] * x[i];
-                    x[k] = acc / a[k * 6 + k];
-                }
-                for (int k = j; k < 6; ++k) hi[tri(k, j)] = x[k];
-            }
-        } else {
-            for (int k = 0; k < 21; ++k) hi[k] = 0.0;
-        }
-        float* st = stats + (size_t)p * 16;
-        st[0] = mean;
-        st[1] = rs;
-        for (int k = 0; k < 6; ++k) {
-            st[2 + k] = (float)dsum[22 + k];
-            st[8 + k] = (float)dsum[28 + k];
-        }
-        st[14] = 0.f;
-        st[15] = 0.f;
-        rflag[p] = f;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) a[i * 6 + j] = (j <= i) ? (double)fsum[slot][q++] : 0.0;
     }
+    if (f == kSuccess && potrf6(a) > 0) f = kSingularHessian;
+    if (f == kSuccess) {
+        // H^-1 column by column: L y = e_j, then L^T x = y
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            double x[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                double acc = (k == j) ? 1.0 : 0.0;
+#pragma unroll
+                for (int i = 0; i < k; ++i) acc -= a[k * 6 + i] * x[i];
+                x[k] = acc / a[k * 6 + k];
+            }
+#pragma unroll
+            for (int k = 5; k >= 0; --k) {
+                double acc = x[k];
+#pragma unroll
+                for (int i = k + 1; i < 6; ++i) acc -= a[i * 6 + k] * x[i];
+                x[k] = acc / a[k * 6 + k];
+            }
+#pragma unroll
+            for (int k = j; k < 6; ++k) hi[tri(k, j)] = x[k];
+        }
+    } else {
+        for (int k = 0; k < 21; ++k) hi[k] = 0.0;
+    }
+    st[0] = mean;
+    st[1] = rs;
+    for (int k = 0; k < 6; ++k) {
+        st[2 + k] = fsum[slot][22 + k];
+        st[8 + k] = fsum[slot][28 + k];
+    }
+    st[14] = 0.f;
+    st[15] = 0.f;
+    rflag[p] = f;
 }
 
 // Catmull-Rom weights (the Hermite bicubic with central differences).
@@ -155,33 +175,67 @@ __device__ __forceinline__ void cr_weights(float t, float& w0, float& w1, float&
     w3 = t2 * (0.5f * t - 0.5f);
 }
 
+// Affine warp of subset offset (dx, dy) as two FMAs per coordinate.  The
+// reference rounds each operation; the difference is an ulp, which moves a
+// truncated coordinate only at an exact integer, where the bicubic patch is
+// continuous.  Each FMA rounds once, so the result is non-decreasing in dx
+// and in dy separately: its extremes over the subset lie at the corners.
+__device__ __forceinline__ float warp_x(const float* Wm, float bx, float dx, float dy) {
+    return fmaf(Wm[0], dx, fmaf(Wm[1], dy, bx));
+}
+__device__ __forceinline__ float warp_y(const float* Wm, float by, float dx, float dy) {
+    return fmaf(Wm[3], dx, fmaf(Wm[4], dy, by));
+}
+
+// OutofROI test of one pass (TW_paDIC_ICGN2D_CPU.cpp:625-635, :765-770):
+// some sample truncates outside the ROI exactly when one of the four corner
+// samples does, since truncation is monotone and the warp's extremes lie at
+// the corners.
+__device__ __forceinline__ bool pass_out_of_roi(const Geom& g, const float* Wm, float bx, float by) {
+    const float rx = (float)g.rx, ry = (float)g.ry;
+    bool out = false;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float dx = (c & 1) ? rx : -rx, dy = (c & 2) ? ry : -ry;
+        const int ix = (int)warp_x(Wm, bx, dx, dy), iy = (int)warp_y(Wm, by, dx, dy);
+        out |= (unsigned)(ix - g.sx) >= (unsigned)g.rw || (unsigned)(iy - g.sy) >= (unsigned)g.rh;
+    }
+    return out;
+}
+
+// Persistent IC-GN kernel, one POI per CTA at a time.  USE_LUT reads the
+// per-frame LUT (four float4 planes, k_bicubic_lut); otherwise the target window
+// around the guess is staged in shared memory and interpolated with the
+// separable Catmull-Rom weights.
 template <int THREADS, bool USE_LUT>
-__global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __restrict__ ref,
-                                                       const uint8_t* __restrict__ tar,
-                                                       const int2* __restrict__ poi, int n,
-                                                       const float* __restrict__ stats,
-                                                       const double* __restrict__ hinv,
-                                                       const uint8_t* __restrict__ rflag,
-                                                       const float4* __restrict__ lut, int* work, float* u,
-                                                       float* v, float* p6, int* iters, uint8_t* flags, int ws) {
+__global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS / 2))
+    k_icgn_fast(Geom g, const uint8_t* __restrict__ ref, const uint8_t* __restrict__ tar,
+                const int2* __restrict__ poi, int n, const float* __restrict__ stats,
+                const double* __restrict__ hinv, const uint8_t* __restrict__ rflag,
+                const float4* __restrict__ lut, int* work, float* u, float* v, float* p6, int* iters,
+                uint8_t* flags, int ws) {
     constexpr int NW = THREADS / 32;
     constexpr unsigned FULL = 0xffffffffu;
-    // dynamic shared memory: [S] float2 reference gradients (R_x, R_y), then
-    // the [ws][ws] target window
+    // dynamic shared memory: [S] half2 reference gradients (R_x, R_y: half
+    // integers of magnitude <= 127.5, exact in FP16), then (window path) the
+    // [ws][ws] target window
     extern __shared__ __align__(16) float smem_f[];
-    __shared__ float red[NW][9];
+    __shared__ float red[NW][8];
     __shared__ float sW[6];
     __shared__ int sctl[3];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
-    float2* grad = reinterpret_cast<float2*>(smem_f);
-    float* win = smem_f + 2 * ((S + 1) & ~1);
-    const size_t plane = (size_t)g.rw * g.rh;
+    __half2* grad = reinterpret_cast<__half2*>(smem_f);
+    float* win = smem_f + ((S + 3) & ~3);
     const float inv_s = 1.0f / (float)S;
-    // sample k = tid + j*THREADS sits at row l, column m of the subset;
-    // stepping j advances (l, m) by (dl, dm) with carry
-    const int l_first = tid / SW, m_first = tid - (tid / SW) * SW;
-    const int dl = THREADS / SW, dm = THREADS - (THREADS / SW) * SW;
+    // sample k = tid + j*THREADS sits at subset offset (dx, dy); stepping j
+    // advances it by (ddx, ddy) with carry (small integers, exact in FP32)
+    const float dx_first = (float)(tid % SW - g.rx), dy_first = (float)(tid / SW - g.ry);
+    const float ddx = (float)(THREADS % SW), ddy = (float)(THREADS / SW);
+    const float rxf = (float)g.rx, swf = (float)SW;
+    // plane-0 LUT entry of image pixel (ix, iy) is lut0[iy * rw + ix]
+    const size_t plane = (size_t)g.rw * g.rh;
+    const float4* lut0 = lut - ((size_t)g.sy * g.rw + g.sx);
 
     for (;;) {
         if (tid == 0) sctl[2] = atomicAdd(work, 1);
@@ -199,8 +253,7 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
             flags[p] = rf;
             for (int k = 0; k < 6; ++k) p6[(size_t)p * 6 + k] = P[k];
         }
-        // ---- stage the target window and the reference gradients (rows by
-        // warps, columns by lanes)
+        // ---- stage the reference gradients (and the target window)
         const int wx0 = px + (int)floorf(u0) - g.rx - 4;
         const int wy0 = py + (int)floorf(v0) - g.ry - 4;
         if (!done) {
@@ -219,8 +272,8 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
             for (int l = wid; l < SH; l += NW) {
                 for (int m = lane; m < SW; m += 32) {
                     const uint8_t* r = r0 + (size_t)l * g.pitch + m;
-                    grad[l * SW + m] = make_float2(0.5f * (float)((int)r[1] - (int)r[-1]),
-                                                   0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
+                    grad[l * SW + m] = __floats2half2_rn(0.5f * (float)((int)r[1] - (int)r[-1]),
+                                                         0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
                 }
             }
         }
@@ -245,40 +298,52 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
         int it = 0;  // solves completed; abort/counter rule as in the plain kernel
         while (!done) {
             float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            int oor = 0;
-            int l = l_first, m = m_first;
-            // x = px + W00 dx + W01 dy + W02 as two FMAs (the reference rounds
-            // each operation; the difference is an ulp, which moves a
-            // truncated coordinate only at an exact integer, where the
-            // bicubic patch is continuous)
             const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
-#pragma unroll 2
-            for (int k = tid; k < S; k += THREADS) {
-                const float dxf = (float)(m - g.rx), dyf = (float)(l - g.ry);
-                const float wx = fmaf(Wm[0], dxf, fmaf(Wm[1], dyf, bx));
-                const float wy = fmaf(Wm[3], dxf, fmaf(Wm[4], dyf, by));
-                const int ix = (int)wx, iy = (int)wy;
-                float t = 0.f;
-                if ((unsigned)(ix - g.sx) < (unsigned)g.rw && (unsigned)(iy - g.sy) < (unsigned)g.rh) {
-                    const int lx = ix - wx0, ly = iy - wy0;
-                    if (it == 0) {  // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
-                        t = (!USE_LUT && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
-                                ? win[ly * ws + lx]
-                                : (float)tar[(size_t)iy * g.pitch + ix];
-                    } else if (iy - g.sy == g.rh - 1 || ix - g.sx == g.rw - 1) {
-                        t = 0.f;  // the reference LUT's never-written last row / column
-                    } else {
+            // uniform over the CTA: every thread evaluates the same corners
+            const bool oor = pass_out_of_roi(g, Wm, bx, by);
+            if (!oor) {
+                float dxf = dx_first, dyf = dy_first;
+                const __half2* gp = grad + tid;
+                if (it == 0) {
+                    // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
+#pragma unroll 4
+                    for (int k = tid; k < S; k += THREADS) {
+                        const int ix = (int)warp_x(Wm, bx, dxf, dyf), iy = (int)warp_y(Wm, by, dxf, dyf);
+                        const int lx = ix - wx0, ly = iy - wy0;
+                        const float t = (!USE_LUT && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
+                                            ? win[ly * ws + lx]
+                                            : (float)tar[(size_t)iy * g.pitch + ix];
+                        const float2 gr = __half22float2(*gp);
+                        const float tp = t - c;
+                        const float a = gr.x * tp, b = gr.y * tp;
+                        s[0] += tp;
+                        s[1] = fmaf(tp, tp, s[1]);
+                        s[2] += a; s[3] = fmaf(a, dxf, s[3]); s[4] = fmaf(a, dyf, s[4]);
+                        s[5] += b; s[6] = fmaf(b, dxf, s[6]); s[7] = fmaf(b, dyf, s[7]);
+                        gp += THREADS;
+                        dxf += ddx;
+                        dyf += ddy;
+                        if (dxf > rxf) { dxf -= swf; dyf += 1.f; }
+                    }
+                } else {
+#pragma unroll 4
+                    for (int k = tid; k < S; k += THREADS) {
+                        const float wx = warp_x(Wm, bx, dxf, dyf), wy = warp_y(Wm, by, dxf, dyf);
+                        const int ix = (int)wx, iy = (int)wy;
                         const float fx = wx - (float)ix, fy = wy - (float)iy;
+                        float t;
                         if (USE_LUT) {
-                            const size_t o = (size_t)(iy - g.sy) * g.rw + (ix - g.sx);
-                            const float4 a0 = lut[o], a1 = lut[plane + o], a2 = lut[2 * plane + o],
-                                         a3 = lut[3 * plane + o];
+                            const float4* q = lut0 + ((size_t)iy * g.rw + ix);
+                            const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
                             const float r0 = ((a0.w * fx + a0.z) * fx + a0.y) * fx + a0.x;
                             const float r1 = ((a1.w * fx + a1.z) * fx + a1.y) * fx + a1.x;
                             const float r2 = ((a2.w * fx + a2.z) * fx + a2.y) * fx + a2.x;
                             const float r3 = ((a3.w * fx + a3.z) * fx + a3.y) * fx + a3.x;
                             t = ((r3 * fy + r2) * fy + r1) * fy + r0;
+                        } else if (iy - g.sy == g.rh - 1 || ix - g.sx == g.rw - 1) {
+                            t = 0.f;  // the reference LUT's never-written last row / column
                         } else {
+                            const int lx = ix - wx0, ly = iy - wy0;
                             float cx0, cx1, cx2, cx3, cy0, cy1, cy2, cy3;
                             cr_weights(fx, cx0, cx1, cx2, cx3);
                             cr_weights(fy, cy0, cy1, cy2, cy3);
@@ -301,46 +366,42 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
                             }
                             t = cy0 * rr[0] + cy1 * rr[1] + cy2 * rr[2] + cy3 * rr[3];
                         }
+                        const float2 gr = __half22float2(*gp);
+                        const float tp = t - c;
+                        const float a = gr.x * tp, b = gr.y * tp;
+                        s[0] += tp;
+                        s[1] = fmaf(tp, tp, s[1]);
+                        s[2] += a; s[3] = fmaf(a, dxf, s[3]); s[4] = fmaf(a, dyf, s[4]);
+                        s[5] += b; s[6] = fmaf(b, dxf, s[6]); s[7] = fmaf(b, dyf, s[7]);
+                        gp += THREADS;
+                        dxf += ddx;
+                        dyf += ddy;
+                        if (dxf > rxf) { dxf -= swf; dyf += 1.f; }
                     }
-                } else {
-                    oor = 1;
                 }
-                const float2 gr = grad[k];
-                const float tp = t - c;
-                const float dx = dxf, dy = dyf;
-                const float a = gr.x * tp, b = gr.y * tp;
-                s[0] += tp;
-                s[1] += tp * tp;
-                s[2] += a; s[3] += a * dx; s[4] += a * dy;
-                s[5] += b; s[6] += b * dx; s[7] += b * dy;
-                l += dl;
-                m += dm;
-                if (m >= SW) { m -= SW; ++l; }
-            }
-            // ---- one reduction (FP32), then warp 0 finishes the iteration:
-            // FP32 scalars, FP64 H^-1 b on lanes 0-5, warp update on lane 0
+                // ---- one reduction (FP32)
 #pragma unroll
-            for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
-            oor = __any_sync(FULL, oor);
-            if (lane == 0) {
+                for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
+                if (lane == 0) {
 #pragma unroll
-                for (int k = 0; k < 8; ++k) red[wid][k] = s[k];
-                red[wid][8] = (float)oor;
+                    for (int k = 0; k < 8; ++k) red[wid][k] = s[k];
+                }
+                __syncthreads();
             }
-            __syncthreads();
+            // ---- warp 0 finishes the iteration: FP32 scalars, FP64 H^-1 b on
+            // lanes 0-5, warp update on lane 0
             if (wid == 0) {
                 float tot = 0.f;
-                if (lane < 9)
+                if (!oor && lane < 8)
                     for (int w = 0; w < NW; ++w) tot += red[w][lane];
                 const float S0 = __shfl_sync(FULL, tot, 0), S1 = __shfl_sync(FULL, tot, 1);
-                const float any_oor = __shfl_sync(FULL, tot, 8);
                 const float Ak = __shfl_sync(FULL, tot, 2 + (lane < 6 ? lane : 0));
                 const float m0 = S0 * inv_s;
                 const float mean_t = c + m0;
                 const float var = S1 - S0 * m0;
                 const float ts = sqrtf(var > 0.f ? var : 0.f);
                 int flag = kSuccess, cont = 0;
-                if (any_oor > 0.f) {
+                if (oor) {
                     flag = kOutofROI;
                 } else if (fabsf(mean_t) <= FLT_EPSILON || fabsf(ts) <= FLT_EPSILON) {
                     flag = kDarkSubset;
@@ -401,7 +462,7 @@ __global__ void __launch_bounds__(THREADS) k_icgn_fast(Geom g, const uint8_t* __
 cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
                                        double* chol, uint8_t* rflag, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_ref_precompute_fast<<<n, kPreThreads, 0, st>>>(g, ref, poi, n, stats, chol, rflag);
+    k_ref_precompute_fast<<<(n + kPrePois - 1) / kPrePois, kPreThreads, 0, st>>>(g, ref, poi, n, stats, chol, rflag);
     return cudaGetLastError();
 }
 
@@ -414,7 +475,7 @@ static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const u
                                       uint8_t* flags, int ctas_per_sm, cudaStream_t st) {
     const int ws = icgn_fast_window(g);
     const int S = (2 * g.rx + 1) * (2 * g.ry + 1);
-    const size_t smem = sizeof(float) * (2 * (size_t)((S + 1) & ~1) + (LUT ? 0 : (size_t)ws * ws));
+    const size_t smem = sizeof(float) * ((size_t)((S + 3) & ~3) + (LUT ? 0 : (size_t)ws * ws));
     auto kern = k_icgn_fast<THREADS, LUT>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -47,6 +47,7 @@ constexpr unsigned kWaitLimit = 1u << 24;
 
 struct TcShape {
     int N, H, HP, NP, PB, tiles1, K4, BW, WS, n_batches, n, groups;
+    int NW4;  // 32-bit words per window row in the exact re-evaluation
     // shared twiddle tables
     int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
     // per-group operand regions, relative to the group's base
@@ -56,8 +57,6 @@ struct TcShape {
 
 // Epilogue-4 scratch, placed in the A1/A3 region once stage 3 has read A3.
 struct PeakScratch {
-    float bv[kThreads];
-    int bi[kThreads];
     int cand[kMaxPB][kMaxCand];
     int candS[kMaxPB][kMaxCand];
 };
@@ -148,6 +147,22 @@ __device__ __forceinline__ int group_sync_or(int id, int v) {
     return r;
 }
 
+// 4 bytes from any shared-memory byte pointer derived from the dynamic
+// shared buffer (two aligned words, funnel shift)
+__device__ __forceinline__ uint32_t ld_unaligned_p(const uint8_t* a) {
+    const unsigned mis = (unsigned)(reinterpret_cast<uintptr_t>(a) & 3);
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(a - mis);
+    return __funnelshift_r(w[0], w[1], mis * 8u);
+}
+// order-preserving map of FP32 to unsigned, and back
+__device__ __forceinline__ uint32_t f32_ord(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float f32_unord(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
     const __half2 h = __floats2half2_rn(a, b);
     return *reinterpret_cast<const uint32_t*>(&h);
@@ -190,8 +205,9 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
     __shared__ int wsum[2][2 * kMaxPB][2];
     __shared__ float sscale[2][kMaxPB];
     __shared__ int sdark[2][kMaxPB];
-    __shared__ float sthr[2][kMaxPB];
     __shared__ int ncand[2][kMaxPB];
+    __shared__ uint32_t smaxv[2][kMaxPB];  // ordered value of the approximate peak
+    __shared__ int smaxi[2][kMaxPB];       // its first index
     __shared__ int2 spoi[2][kMaxPB];
     __shared__ int smis[2][2 * kMaxPB];
 
@@ -251,7 +267,12 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
     for (int batch = blockIdx.x * s.groups + grp; batch < s.n_batches; batch += gridDim.x * s.groups) {
         const int b0 = batch * PB;
         if (t < 2 * kMaxPB * 2) (&wsum[grp][0][0])[t] = 0;
-        if (t < PB) spoi[grp][t] = (b0 + t < s.n) ? poi[b0 + t] : make_int2(-1, -1);
+        if (t < PB) {
+            spoi[grp][t] = (b0 + t < s.n) ? poi[b0 + t] : make_int2(-1, -1);
+            smaxv[grp][t] = 0u;
+            smaxi[grp][t] = 0x7fffffff;
+            ncand[grp][t] = 1;
+        }
         group_sync(bar_id);
 
         // ---- phase L1: one TMA box per window ([N rows][BW bytes], x aligned
@@ -263,6 +284,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
             mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
             for (int wi = 0; wi < 2 * PB; ++wi) {
                 const int2 pyx = spoi[grp][wi >> 1];
+                smis[grp][wi] = 0;  // read (harmlessly) by the row copies for absent POIs
                 if (pyx.x < 0) continue;
                 const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
                 const int xa = x0 & ~15;
@@ -550,30 +572,31 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
         const bool rowv = t < PB * N;
         const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
         const bool live = rowv && !sdark[grp][p4];
-        {
-            float bv = -3.4e38f;
-            int bi = 0x7fffffff;
-            if (live) {
-#pragma unroll
-                for (int y = 0; y < NP; ++y)
-                    if (y < N && cv[y] > bv) { bv = cv[y]; bi = y * N + x4; }
-            }
-            ps->bv[t] = bv;
-            ps->bi[t] = bi;
-        }
-        group_sync(bar_id);
-        if (t < PB) {
-            float bv = -3.4e38f;
-            int bi = 0x7fffffff;
-            for (int r = t * N; r < t * N + N; ++r) argmax_merge(bv, bi, ps->bv[r], ps->bi[r]);
-            sthr[grp][t] = bv - 0.02f * (float)n2;
-            ncand[grp][t] = 1;
-            ps->cand[t][0] = bi;
-        }
-        group_sync(bar_id);
+        if (t < kMaxPB * kMaxCand) (&ps->candS[0][0])[t] = 0;
+        // approximate peak per POI: row maxima (first on ties), then the
+        // largest value and, among rows holding it, the smallest index, each
+        // by a segmented warp reduction and one shared atomic per warp segment
+        float bv = -3.4e38f;
+        int bi = 0x7fffffff;
         if (live) {
-            const float th = sthr[grp][p4];
-            const int first = ps->cand[p4][0];
+#pragma unroll
+            for (int y = 0; y < NP; ++y)
+                if (y < N && cv[y] > bv) { bv = cv[y]; bi = y * N + x4; }
+        }
+        const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
+        const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
+        if (live && lane == __ffs(seg) - 1) atomicMax(&smaxv[grp][p4], ov);
+        group_sync(bar_id);
+        const uint32_t pv = live ? smaxv[grp][p4] : 0u;
+        const uint32_t mi = __reduce_min_sync(seg, (live && f32_ord(bv) == pv) ? (uint32_t)bi : 0xffffffffu);
+        if (live && lane == __ffs(seg) - 1 && mi != 0xffffffffu) atomicMin(&smaxi[grp][p4], (int)mi);
+        group_sync(bar_id);
+        // candidates: every shift within 2% of N^2 (scaled units) of the
+        // approximate peak; slot 0 holds the approximate argmax
+        if (live) {
+            const float th = f32_unord(pv) - 0.02f * (float)n2;
+            const int first = smaxi[grp][p4];
+            if (x4 == 0) ps->cand[p4][0] = first;
 #pragma unroll
             for (int y = 0; y < NP; ++y) {
                 if (y < N && cv[y] >= th) {
@@ -587,30 +610,51 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
         }
         group_sync(bar_id);
         TC_MARK(9);
-        // exact integer correlation of every candidate from the staged windows,
-        // one warp per (POI, candidate); lanes take columns, so the column
-        // wrap of the shift is fixed per lane and the rows wrap once
-        for (int task = warp; task < PB * kMaxCand; task += 4) {
-            const int p = task / kMaxCand, slot = task - p * kMaxCand;
-            if (sdark[grp][p] || slot >= min(ncand[grp][p], kMaxCand)) continue;
-            const int idx = ps->cand[p][slot];
-            const int kx = idx % N, ky = idx / N;
-            const uint8_t* fw = wwin + (2 * p) * WS + smis[grp][2 * p];
-            const uint8_t* gw = wwin + (2 * p + 1) * WS + smis[grp][2 * p + 1];
-            int acc = 0;
-            for (int x = lane; x < N; x += 32) {
-                int xx = x + kx;
-                if (xx >= N) xx -= N;
-                const uint8_t* fc = fw + x;
-                const uint8_t* gc = gw + xx;
-                const int split = N - ky;  // rows y < split pair with y + ky, the rest with y + ky - N
-#pragma unroll 4
-                for (int y = 0; y < split; ++y) acc += (int)fc[y * BW] * (int)gc[(y + ky) * BW];
-#pragma unroll 4
-                for (int y = split; y < N; ++y) acc += (int)fc[y * BW] * (int)gc[(y - split) * BW];
+        // exact integer correlation of every candidate, read from the staged
+        // windows: tasks (POI, candidate, row) over the group's threads, four
+        // products per DP4A, one shared atomic per task.  Lanes walk the words
+        // of their row in a lane-rotated order, which spreads rows that share
+        // shared-memory banks over different words.
+        {
+            const int NW4 = s.NW4;
+            const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
+            int total = 0;
+            for (int p = 0; p < PB; ++p) total += sdark[grp][p] ? 0 : min(ncand[grp][p], kMaxCand) * N;
+            const int rot = lane % NW4;
+            for (int task = t; task < total; task += 128) {
+                int p = 0, rem = task;
+                for (;;) {
+                    const int cnt = sdark[grp][p] ? 0 : min(ncand[grp][p], kMaxCand) * N;
+                    if (rem < cnt) break;
+                    rem -= cnt;
+                    ++p;
+                }
+                const int c = rem / N, y = rem - c * N;
+                const int idx = ps->cand[p][c];
+                const int ky = idx / N, kx = idx - ky * N;
+                int yy = y + ky;
+                if (yy >= N) yy -= N;
+                const uint8_t* fb = wwin + (2 * p) * WS + smis[grp][2 * p] + y * BW;
+                const uint8_t* gb = wwin + (2 * p + 1) * WS + smis[grp][2 * p + 1] + yy * BW;
+                const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
+                unsigned acc = 0;
+                int j = rot;
+#pragma unroll 2
+                for (int jj = 0; jj < NW4; ++jj) {
+                    uint32_t fw = ld_unaligned_p(fb + 4 * j);
+                    if (j == NW4 - 1) fw &= tail;
+                    int a = kx + 4 * j;  // g bytes (x + kx) mod N for x = 4j .. 4j+3
+                    if (a >= N) a -= N;
+                    uint32_t gw = ld_unaligned_p(gb + a);
+                    if (a + 4 > N) {
+                        const int nlo = N - a;
+                        gw = (gw & (0xffffffffu >> (8 * (4 - nlo)))) | (g0 << (8 * nlo));
+                    }
+                    acc = __dp4a(fw, gw, acc);
+                    if (++j == NW4) j = 0;
+                }
+                atomicAdd(&ps->candS[p][c], (int)acc);
             }
-            acc = warp_sum(acc);
-            if (lane == 0) ps->candS[p][slot] = acc;
         }
         group_sync(bar_id);
         if (t < PB && b0 + t < s.n) {
@@ -619,6 +663,10 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
                 status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
             } else {
                 const int nc = min(ncand[grp][t], kMaxCand);
+#ifdef TWDIC_TC_TRACE
+                atomicAdd(&g_tc_trace[12], (unsigned long long)ncand[grp][t]);
+                if (ncand[grp][t] > kMaxCand) atomicAdd(&g_tc_trace[13], 1ull);
+#endif
                 int best = ps->cand[t][0], bs = ps->candS[t][0];
                 for (int c = 1; c < nc; ++c) {
                     const int sc = ps->candS[t][c], id = ps->cand[t][c];
@@ -689,11 +737,14 @@ bool make_shape(const Geom& g, int n, TcShape& s) {
     // per-group regions
     s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
     int q = 0;
+    s.NW4 = (N + 3) / 4;
     s.off_a13 = q;
     q += std::max(std::max(s.tiles1 * 128 * K1 * 2, 128 * 2 * NP * 2), (int)sizeof(PeakScratch));
     s.off_a2 = q; q += 16 * 36 * NP;
     s.off_a4 = q; q += 16 * 16 * K4;
-    s.WS = round_up(N * s.BW, 128);  // window stride (TMA destinations are 128-byte aligned)
+    // window stride: TMA destinations are 128-byte aligned, and 16 spare bytes
+    // keep the 8-byte reads of ld_unaligned inside the window
+    s.WS = round_up(N * s.BW + 16, 128);
     s.off_win = q; q += 2 * pb * s.WS;
     s.group_bytes = round_up(q, 1024);
     const int limit = 225 * 1024;

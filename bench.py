@@ -336,7 +336,8 @@ def _run_gpu(args, world, rank, local, torch):
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(pair.tar.nbytes),
                     "d2h_bytes_per_step": d2h, "p50_ms": round(pct(e2e_ms, 50), 4),
                     "p99_ms": round(pct(e2e_ms, 99), 4)},
-            "gpu_launches": 2 * args.steps,
+            # per frame: k_fftcc_tc, k_bicubic_lut, k_icgn_fast
+            "gpu_launches": 3 * args.steps,
             "clocks": clk,
             "wall_s_timed_region": round(t_wall, 3)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -347,12 +348,29 @@ def _run_gpu(args, world, rank, local, torch):
     return 0
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+# of each kernel on this workload, from the ncu captures summarised in
+# profiles/k_icgn_fast_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
+NCU_TRAFFIC = {"k_icgn_fast": 305.42e6 + 8.52e6, "k_fftcc_tc": 9.60e6 + 0.0}
+# L2 -> SM bandwidth implied by that IC-GN capture (53.78 GB in 4.119 ms at
+# 53.6 % of the L2 throughput peak); there is no measured L2 peak
+L2_PEAK_GBS_NCU = 53.78e9 / 4.119e-3 / 0.536 / 1e9
+
+
 def roofline(g, P, ph, kbar):
-    """Roofline of the dominant phase.  IC-GN (fast path) moves little DRAM
-    traffic: its algorithmic bytes per POI are the compulsory ones -- the
-    per-reference cache entry (184 B), u/v in and out (16 B), p6 (24 B),
-    iteration count and flag (5 B) -- plus both images once per frame.  Its
-    FP32 work per POI is k*S*64 flops (k = mean iterations)."""
+    """Roofline of the dominant kernel, the fast IC-GN (k_icgn_fast), timed by
+    the per-phase CUDA events of the frame (the IC-GN phase holds that kernel
+    and the memset of its work counter).
+
+    HBM view (the one reported as `frac`): algorithmic bytes per launch are
+    the compulsory ones -- the target LUT read once (64 B per ROI pixel), both
+    images once, and per POI the reference cache entry (statistics 64 B, FP64
+    inverse Hessian 168 B, flag 1 B), the POI (8 B), u/v in (8 B) and out
+    (8 B), p6 (24 B), iteration count (4 B) and flag (1 B).  The kernel is not
+    HBM bound: its gathers of the LUT are served by L2, so the L2 view below
+    (k*S*64 B of LUT gathers per POI, k = mean iterations) and the FP32 view
+    (k*S*64 flops per POI) are reported beside it, with the tensor-core view of
+    the FFT-CC kernel (48 N^3 flops per POI)."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -363,20 +381,29 @@ def roofline(g, P, ph, kbar):
     src = "measured" if peaks else "fallback"
     S = (2 * g.subset_r + 1) ** 2
     N = 2 * g.subset_r
-    if ph["icgn"] >= ph["fftcc"]:
-        bytes_per_launch = P * (184 + 16 + 24 + 5) + 2 * g.img_w * g.img_h
-        achieved = bytes_per_launch / (ph["icgn"] / 1000.0) / 1e9
-        fp32_flops = kbar * S * 64 * P
-        return {"kernel": "k_icgn_fast (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2),
-                "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": None,
-                "peak_source": src, "algorithmic_bytes_per_launch": bytes_per_launch,
-                "fp32_tflops": round(fp32_flops / (ph["icgn"] / 1000.0) / 1e12, 2),
-                "note": "IC-GN is FP32/shared-memory bound; the HBM fraction shows it is not memory bound"}
-    flops = 48 * N ** 3 * P
-    achieved = flops / (ph["fftcc"] / 1000.0) / 1e12
-    return {"kernel": "FFT-CC", "bound": "tensor", "achieved": round(achieved, 2), "peak": tc, "unit": "TFLOP/s",
-            "frac": round(achieved / tc, 4), "traffic": None, "peak_source": src,
-            "algorithmic_flops_per_launch": flops}
+    t_icgn = ph["icgn"] / 1000.0
+    t_fftcc = ph["fftcc"] / 1000.0
+    per_poi = 64 + 168 + 1 + 8 + 8 + 8 + 24 + 4 + 1
+    bytes_icgn = P * per_poi + 64 * g.roi_w * g.roi_h + 2 * g.img_w * g.img_h
+    achieved = bytes_icgn / t_icgn / 1e9
+    gather = kbar * S * 64 * P
+    flops_fftcc = 48 * N ** 3 * P
+    fft_tflops = flops_fftcc / t_fftcc / 1e12
+    return {"kernel": "k_icgn_fast (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
+            "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": NCU_TRAFFIC["k_icgn_fast"],
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)",
+            "algorithmic_bytes_per_launch": int(bytes_icgn), "kernel_ms": round(ph["icgn"], 4),
+            "l2_view": {"gather_bytes_per_launch": int(gather), "achieved_gbs": round(gather / t_icgn / 1e9, 1),
+                        "peak_gbs": round(L2_PEAK_GBS_NCU, 1),
+                        "frac": round(gather / t_icgn / 1e9 / L2_PEAK_GBS_NCU, 4),
+                        "peak_source": "implied by the ncu capture (no measured L2 peak)"},
+            "fp32_view": {"flops_per_launch": int(kbar * S * 64 * P),
+                          "achieved_tflops": round(kbar * S * 64 * P / t_icgn / 1e12, 2)},
+            "fftcc_tensor_view": {"kernel": "k_fftcc_tc", "flops_per_launch": int(flops_fftcc),
+                                  "achieved_tflops": round(fft_tflops, 2), "peak_tflops": tc,
+                                  "frac": round(fft_tflops / tc, 4), "kernel_ms": round(ph["fftcc"], 4),
+                                  "traffic": NCU_TRAFFIC["k_fftcc_tc"]},
+            "note": "frac is against HBM; the IC-GN kernel is bound by L2 gather latency and issue, see l2_view"}
 
 
 def main(argv=None):

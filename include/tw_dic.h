@@ -177,7 +177,7 @@ TWDIC_API int twdic_frame_phase_times(const twdic_frame* h, float* t6);
 TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 
 /* Launch-shape tuning of a frame handle (no counterpart in the reference;
- * set by the autotuner).  icgn_threads: 128 or 256 threads per IC-GN CTA;
+ * set by the autotuner).  icgn_threads: 64, 128 or 256 threads per IC-GN CTA;
  * icgn_ctas_per_sm: persistent CTAs per SM (0 = occupancy limit);
  * icgn_use_lut: 1 = gather a per-frame bicubic LUT from HBM instead of the
  * staged target window; fftcc_use_tc: 1 = tensor-core FFT-CC when available. */

@@ -279,20 +279,30 @@ struct Engine {
 
     // IC-GN of all POIs; u, v in/out device arrays.
     int icgn(float* u, float* v, float* p6, int* iters, uint8_t* flags) {
+        TW_TRY(prepare_target());
+        return icgn_solve(u, v, p6, iters, flags);
+    }
+
+    // Per-target preparation: the bicubic coefficient LUT of the target
+    // (TW_utils.cpp:604-700), when the IC-GN variant reads one.
+    int prepare_target() {
+        if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
+        if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.use_lut) {
+            TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
+        }
+        return TWDIC_OK;
+    }
+
+    int icgn_solve(float* u, float* v, float* p6, int* iters, uint8_t* flags) {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
         TW_TRY(ensure_cache(nullptr));
         const int2* poi = d_poi.as<int2>();
         if (prm.path == TWDIC_PATH_PLAIN) {
-            TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
-            TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
             TW_CUDA(launch_icgn_plain(g, d_tar.as<uint8_t>(), poi, n, c_subR.as<float>(), c_sd.as<float2>(),
                                       c_chol.as<float>(), c_norm.as<float>(), c_flag.as<uint8_t>(),
                                       d_lut.as<float4>(), u, v, p6, iters, flags, stream));
         } else {
-            if (icgn_tune.use_lut) {
-                TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
-                TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
-            }
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.as<float4>(),
                                      d_work.as<int>(), u, v, p6, iters, flags, icgn_tune, stream));
@@ -562,7 +572,9 @@ int twdic_frame_process(twdic_frame* h, const uint8_t* tar, int32_t stride, int 
     TW_CUDA(cudaMemsetAsync(dit, 0, 4 * n, e.stream));
     TW_TRY(e.fftcc(du, dv, dz, e.d_fst.as<uint8_t>()));
     TW_CUDA(cudaEventRecord(e.ev[3], e.stream));
-    TW_TRY(e.icgn(du, dv, dp6, dit, dfl));
+    TW_TRY(e.prepare_target());
+    TW_CUDA(cudaEventRecord(e.ev[6], e.stream));
+    TW_TRY(e.icgn_solve(du, dv, dp6, dit, dfl));
     TW_CUDA(cudaEventRecord(e.ev[4], e.stream));
     if (!dev) {
         TW_TRY(copy_out(u, du, 4 * n, mem_out, e.stream));
@@ -584,16 +596,17 @@ int twdic_frame_phase_times(const twdic_frame* hc, float* t6) {
     Engine& e = h->e;
     if (e.times_pending) {
         TW_CUDA(cudaEventSynchronize(e.ev[5]));
-        float a = 0, b = 0, c = 0, d = 0, f = 0;
+        float a = 0, b = 0, c = 0, d = 0, f = 0, pr = 0;
         TW_CUDA(cudaEventElapsedTime(&a, e.ev[0], e.ev[1]));
         TW_CUDA(cudaEventElapsedTime(&f, e.ev[1], e.ev[2]));
         TW_CUDA(cudaEventElapsedTime(&b, e.ev[2], e.ev[3]));
-        TW_CUDA(cudaEventElapsedTime(&c, e.ev[3], e.ev[4]));
+        TW_CUDA(cudaEventElapsedTime(&pr, e.ev[3], e.ev[6]));
+        TW_CUDA(cudaEventElapsedTime(&c, e.ev[6], e.ev[4]));
         TW_CUDA(cudaEventElapsedTime(&d, e.ev[4], e.ev[5]));
         const bool cached = e.last_times[5] < 0.f;
         e.last_times[0] = a;
         e.last_times[1] = b;
-        e.last_times[2] = 0.f;  // target preparation is inside the IC-GN phase
+        e.last_times[2] = pr;  // target LUT
         e.last_times[3] = c;
         e.last_times[4] = d;
         e.last_times[5] = cached ? 0.f : f;

@@ -363,12 +363,13 @@ def roofline(g, P, ph, kbar):
     and the memset of its work counter).
 
     HBM view (the one reported as `frac`): algorithmic bytes per launch are
-    the compulsory ones -- the target LUT read once (64 B per ROI pixel), both
+    the compulsory ones -- the target's 4x4 neighbourhood table read once
+    (16 B per ROI pixel), both
     images once, and per POI the reference cache entry (statistics 64 B, FP64
     inverse Hessian 168 B, flag 1 B), the POI (8 B), u/v in (8 B) and out
     (8 B), p6 (24 B), iteration count (4 B) and flag (1 B).  The kernel is not
-    HBM bound: its gathers of the LUT are served by L2, so the L2 view below
-    (k*S*64 B of LUT gathers per POI, k = mean iterations) and the FP32 view
+    HBM bound: its gathers of the table are served by L2, so the L2 view below
+    (k*S*16 B of table gathers per POI, k = mean iterations) and the FP32 view
     (k*S*64 flops per POI) are reported beside it, with the tensor-core view of
     the FFT-CC kernel (48 N^3 flops per POI)."""
     peaks = {}
@@ -384,9 +385,9 @@ def roofline(g, P, ph, kbar):
     t_icgn = ph["icgn"] / 1000.0
     t_fftcc = ph["fftcc"] / 1000.0
     per_poi = 64 + 168 + 1 + 8 + 8 + 8 + 24 + 4 + 1
-    bytes_icgn = P * per_poi + 64 * g.roi_w * g.roi_h + 2 * g.img_w * g.img_h
+    bytes_icgn = P * per_poi + 16 * g.roi_w * g.roi_h + 2 * g.img_w * g.img_h
     achieved = bytes_icgn / t_icgn / 1e9
-    gather = kbar * S * 64 * P
+    gather = kbar * S * 16 * P
     flops_fftcc = 48 * N ** 3 * P
     fft_tflops = flops_fftcc / t_fftcc / 1e12
     return {"kernel": "k_icgn_fast (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,

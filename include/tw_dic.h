@@ -179,9 +179,10 @@ TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 /* Launch-shape tuning of a frame handle (no counterpart in the reference;
  * set by the autotuner).  icgn_threads: 64, 128 or 256 threads per IC-GN CTA;
  * icgn_ctas_per_sm: persistent CTAs per SM (0 = occupancy limit);
- * icgn_use_lut: 1 = gather a per-frame bicubic LUT from HBM instead of the
- * staged target window; fftcc_use_tc: 1 = tensor-core FFT-CC when available. */
-TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
+ * icgn_sampler: target interpolation of the fast IC-GN, 0 = staged window,
+ * 1 = per-frame bicubic coefficient LUT, 2 = per-frame 4x4 neighbourhood
+ * table; fftcc_use_tc: 1 = tensor-core FFT-CC when available. */
+TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                                      int fftcc_use_tc);
 
 /* ------------------------------------------- IC-GN without allocation --- */

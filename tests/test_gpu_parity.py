@@ -6,7 +6,7 @@ import pytest
 
 from oracle import compare as C
 from oracle import oracle as O
-from tw_gb300 import PATH_FAST, PATH_PLAIN, synth
+from tw_gb300 import PATH_FAST, PATH_PLAIN, SAMPLER_LUT, SAMPLER_NBHD, SAMPLER_WINDOW, synth
 from tw_gb300 import dic
 
 pytestmark = pytest.mark.gpu
@@ -86,6 +86,29 @@ def test_frame_parity(request, case, path):
     fr.process(pair.tar, **out2)
     for k in out:
         np.testing.assert_array_equal(out[k], out2[k])
+
+
+@pytest.mark.parametrize("threads", [64, 128, 256])
+@pytest.mark.parametrize("sampler", [SAMPLER_WINDOW, SAMPLER_LUT, SAMPLER_NBHD])
+def test_fast_icgn_samplers(plain512, sampler, threads):
+    """Every launch shape and target sampler of the fast IC-GN meets the
+    parity bar against the oracle (staged window and neighbourhood table
+    evaluate the Catmull-Rom form, the LUT sampler the reference's Hermite
+    coefficients)."""
+    pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = plain512
+    fr = dic.DICFrame(params_of(g, PATH_FAST))
+    fr.set_tuning(threads, 0, sampler, 1)
+    fr.set_reference(pair.ref)
+    out = fr.alloc_outputs()
+    fr.process(pair.tar, **out)
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                      g.grid, g.margin, g.margin, path=PATH_FAST)
+    U, V, Z = f.InitializeFFTCC(pair.ref)
+    f.ComputeFFTCC(U, V, Z, pair.tar)
+    same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
+    rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start,
+                        r=g.subset_r)
+    assert rep.ok(), (sampler, threads, rep)
 
 
 @pytest.mark.parametrize("path", PATHS)

@@ -26,6 +26,8 @@ MEM_HOST = 0
 MEM_DEVICE = 1
 PATH_PLAIN = 0
 PATH_FAST = 1
+# fast IC-GN target samplers (twdic_frame_set_tuning)
+SAMPLER_WINDOW, SAMPLER_LUT, SAMPLER_NBHD = 0, 1, 2
 
 # every symbol include/tw_dic.h declares
 EXPORTED = (

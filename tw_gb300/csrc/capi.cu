@@ -166,9 +166,10 @@ struct Engine {
     int init(const twdic_params& p, int num_pois) {
         prm = p;
         // fastest measured IC-GN shape on GB300 at 41x41 subsets: 64 threads
-        // per POI gathering a per-frame LUT (the autotuner may change it)
+        // per POI gathering the per-frame 4x4 neighbourhood table (16 B per
+        // ROI pixel; the autotuner may change it)
         icgn_tune.threads = 64;
-        icgn_tune.use_lut = 1;
+        icgn_tune.sampler = kSampNbhd;
         g = make_geom(p);
         n = num_pois;
         TW_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
@@ -287,9 +288,12 @@ struct Engine {
     // (TW_utils.cpp:604-700), when the IC-GN variant reads one.
     int prepare_target() {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
-        if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.use_lut) {
+        if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.sampler == kSampLut) {
             TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
             TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
+        } else if (icgn_tune.sampler == kSampNbhd) {
+            TW_TRY(d_lut.ensure(sizeof(uint4) * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_nbhd_table(g, d_tar.as<uint8_t>(), d_lut.as<uint4>(), stream));
         }
         return TWDIC_OK;
     }
@@ -304,7 +308,7 @@ struct Engine {
                                       d_lut.as<float4>(), u, v, p6, iters, flags, stream));
         } else {
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
-                                     c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.as<float4>(),
+                                     c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.p,
                                      d_work.as<int>(), u, v, p6, iters, flags, icgn_tune, stream));
         }
         return TWDIC_OK;
@@ -621,14 +625,16 @@ int twdic_frame_destroy(twdic_frame* h) {
 }
 
 // Tuning (internal to the Python autotuner; not part of the reference interface).
-int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_use_lut,
+int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                            int fftcc_use_tc) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
     if (icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
         return fail(TWDIC_ERR_INVALID_ARG, "threads must be 64, 128 or 256");
     h->e.icgn_tune.threads = icgn_threads;
     h->e.icgn_tune.ctas_per_sm = icgn_ctas_per_sm;
-    h->e.icgn_tune.use_lut = icgn_use_lut;
+    if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
+        return fail(TWDIC_ERR_INVALID_ARG, "sampler must be 0 (window), 1 (LUT) or 2 (neighbourhood table)");
+    h->e.icgn_tune.sampler = icgn_sampler;
     h->e.fftcc_tune.use_tc = fftcc_use_tc;
     return TWDIC_OK;
 }

@@ -8,11 +8,18 @@
 
 namespace twdic {
 
+// Target samplers of the fast IC-GN kernel.
+enum IcgnSampler {
+    kSampWindow = 0,  // staged target window in shared memory, Catmull-Rom
+    kSampLut = 1,     // per-frame float bicubic LUT (64 B per ROI pixel), Horner
+    kSampNbhd = 2,    // per-frame 4x4 byte neighbourhood table (16 B per ROI pixel), Catmull-Rom
+};
+
 // Launch shape of the fast IC-GN kernel, chosen by the autotuner.
 struct IcgnTune {
     int threads = 128;    // 64, 128 or 256 threads per CTA (one POI per CTA at a time)
     int ctas_per_sm = 0;  // persistent CTAs per SM (0 = occupancy limit)
-    int use_lut = 0;      // 1: gather the per-frame LUT from HBM instead of the staged window
+    int sampler = kSampWindow;  // needs no per-frame table
 };
 
 // Launch shape of the tensor-core FFT-CC kernel.
@@ -27,6 +34,8 @@ cudaError_t launch_fftcc_plain(const Geom& g, const uint8_t* ref, const uint8_t*
 cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* subR,
                                         float2* sd, float* chol, float* refnorm, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
+// 4x4 byte neighbourhoods of every ROI pixel of the target (kernels_icgn_fast.cu)
+cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st);
 cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi, int n, const float* subR,
                               const float2* sd, const float* chol, const float* refnorm, const uint8_t* rflag,
                               const float4* lut, float* u, float* v, float* p6, int* iters, uint8_t* flags,
@@ -39,7 +48,7 @@ cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi
 cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
                                        double* chol, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                             const float* stats, const double* chol, const uint8_t* rflag, const float4* lut,
+                             const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st);
 int icgn_fast_window(const Geom& g);

@@ -166,6 +166,30 @@ __global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, con
     rflag[p] = f;
 }
 
+// 4x4 byte neighbourhood of every ROI pixel (i, j) of the target: rows
+// i-1 .. i+2, columns j-1 .. j+2 of the ROI-relative pixel, one 32-bit word
+// per row, lowest byte leftmost.  Zero on the ROI's last row and column, the
+// entries the reference's LUT never writes (TW_MemManager.cpp calloc).  The
+// ROI has one pixel of border on every side (validated on the host), and the
+// neighbourhood of the other last-but-one pixels stays inside the image.
+__global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __restrict__ table) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.rh || j >= g.rw) return;
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    if (i != g.rh - 1 && j != g.rw - 1) {
+        const uint8_t* t = tar + (size_t)(i + g.sy - 1) * g.pitch + (j + g.sx - 1);
+        uint32_t w[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const uint8_t* r = t + (size_t)a * g.pitch;
+            w[a] = (uint32_t)r[0] | ((uint32_t)r[1] << 8) | ((uint32_t)r[2] << 16) | ((uint32_t)r[3] << 24);
+        }
+        q = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    table[(size_t)i * g.rw + j] = q;
+}
+
 // Catmull-Rom weights (the Hermite bicubic with central differences).
 __device__ __forceinline__ void cr_weights(float t, float& w0, float& w1, float& w2, float& w3) {
     const float t2 = t * t;
@@ -203,16 +227,21 @@ __device__ __forceinline__ bool pass_out_of_roi(const Geom& g, const float* Wm, 
     return out;
 }
 
-// Persistent IC-GN kernel, one POI per CTA at a time.  USE_LUT reads the
-// per-frame LUT (four float4 planes, k_bicubic_lut); otherwise the target window
-// around the guess is staged in shared memory and interpolated with the
-// separable Catmull-Rom weights.
-template <int THREADS, bool USE_LUT>
+// Persistent IC-GN kernel, one POI per CTA at a time.  The target sampler:
+//   kSampWindow: the target window around the guess is staged in shared
+//     memory and interpolated with the separable Catmull-Rom weights;
+//   kSampLut: the per-frame bicubic coefficient LUT (four float4 planes,
+//     k_bicubic_lut), evaluated by Horner's rule;
+//   kSampNbhd: the per-frame 4x4 neighbourhood table (16 bytes per ROI
+//     pixel, k_nbhd_table), one 16-byte gather per sample, Catmull-Rom.
+// The Catmull-Rom form with central-difference derivatives is algebraically
+// the reference's Hermite bicubic LUT (TW_utils.cpp:604-700).
+template <int THREADS, int SAMPLER>
 __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS / 2))
     k_icgn_fast(Geom g, const uint8_t* __restrict__ ref, const uint8_t* __restrict__ tar,
                 const int2* __restrict__ poi, int n, const float* __restrict__ stats,
                 const double* __restrict__ hinv, const uint8_t* __restrict__ rflag,
-                const float4* __restrict__ lut, int* work, float* u, float* v, float* p6, int* iters,
+                const void* __restrict__ table, int* work, float* u, float* v, float* p6, int* iters,
                 uint8_t* flags, int ws) {
     constexpr int NW = THREADS / 32;
     constexpr unsigned FULL = 0xffffffffu;
@@ -235,7 +264,8 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
     const float rxf = (float)g.rx, swf = (float)SW;
     // plane-0 LUT entry of image pixel (ix, iy) is lut0[iy * rw + ix]
     const size_t plane = (size_t)g.rw * g.rh;
-    const float4* lut0 = lut - ((size_t)g.sy * g.rw + g.sx);
+    const float4* lut0 = static_cast<const float4*>(table) - ((size_t)g.sy * g.rw + g.sx);
+    const uint4* nb0 = static_cast<const uint4*>(table) - ((size_t)g.sy * g.rw + g.sx);
 
     for (;;) {
         if (tid == 0) sctl[2] = atomicAdd(work, 1);
@@ -257,7 +287,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
         const int wx0 = px + (int)floorf(u0) - g.rx - 4;
         const int wy0 = py + (int)floorf(v0) - g.ry - 4;
         if (!done) {
-            if (!USE_LUT) {
+            if (SAMPLER == kSampWindow) {
                 for (int yy = wid; yy < ws; yy += NW) {
                     const int gy = wy0 + yy;
                     const bool rowok = gy >= 0 && gy < g.img_h;
@@ -310,7 +340,7 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                     for (int k = tid; k < S; k += THREADS) {
                         const int ix = (int)warp_x(Wm, bx, dxf, dyf), iy = (int)warp_y(Wm, by, dxf, dyf);
                         const int lx = ix - wx0, ly = iy - wy0;
-                        const float t = (!USE_LUT && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
+                        const float t = (SAMPLER == kSampWindow && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
                                             ? win[ly * ws + lx]
                                             : (float)tar[(size_t)iy * g.pitch + ix];
                         const float2 gr = __half22float2(*gp);
@@ -332,7 +362,21 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                         const int ix = (int)wx, iy = (int)wy;
                         const float fx = wx - (float)ix, fy = wy - (float)iy;
                         float t;
-                        if (USE_LUT) {
+                        if (SAMPLER == kSampNbhd) {
+                            // 4x4 pixels around (ix, iy), row-major bytes; zero on the
+                            // ROI's last row and column, as the reference LUT is there
+                            const uint4 q = nb0[(size_t)iy * g.rw + ix];
+                            float cx0, cx1, cx2, cx3, cy0, cy1, cy2, cy3;
+                            cr_weights(fx, cx0, cx1, cx2, cx3);
+                            cr_weights(fy, cy0, cy1, cy2, cy3);
+                            const uint32_t wr[4] = {q.x, q.y, q.z, q.w};
+                            float rr[4];
+#pragma unroll
+                            for (int a = 0; a < 4; ++a)
+                                rr[a] = cx0 * (float)(wr[a] & 0xffu) + cx1 * (float)((wr[a] >> 8) & 0xffu) +
+                                        cx2 * (float)((wr[a] >> 16) & 0xffu) + cx3 * (float)(wr[a] >> 24);
+                            t = cy0 * rr[0] + cy1 * rr[1] + cy2 * rr[2] + cy3 * rr[3];
+                        } else if (SAMPLER == kSampLut) {
                             const float4* q = lut0 + ((size_t)iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
                             const float r0 = ((a0.w * fx + a0.z) * fx + a0.y) * fx + a0.x;
@@ -466,17 +510,24 @@ cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const 
     return cudaGetLastError();
 }
 
+cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st) {
+    dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
+    k_nbhd_table<<<grd, blk, 0, st>>>(g, tar, table);
+    return cudaGetLastError();
+}
+
 int icgn_fast_window(const Geom& g) { return 2 * (g.rx > g.ry ? g.rx : g.ry) + 1 + 10; }
 
-template <int THREADS, bool LUT>
+template <int THREADS, int SAMPLER>
 static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi,
                                       int n, const float* stats, const double* chol, const uint8_t* rflag,
-                                      const float4* lut, int* work, float* u, float* v, float* p6, int* iters,
+                                      const void* table, int* work, float* u, float* v, float* p6, int* iters,
                                       uint8_t* flags, int ctas_per_sm, cudaStream_t st) {
     const int ws = icgn_fast_window(g);
     const int S = (2 * g.rx + 1) * (2 * g.ry + 1);
-    const size_t smem = sizeof(float) * ((size_t)((S + 3) & ~3) + (LUT ? 0 : (size_t)ws * ws));
-    auto kern = k_icgn_fast<THREADS, LUT>;
+    const size_t smem =
+        sizeof(float) * ((size_t)((S + 3) & ~3) + (SAMPLER == kSampWindow ? (size_t)ws * ws : 0));
+    auto kern = k_icgn_fast<THREADS, SAMPLER>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -492,24 +543,28 @@ static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const u
     if (grid > n) grid = n;
     e = cudaMemsetAsync(work, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    kern<<<grid, THREADS, smem, st>>>(g, ref, tar, poi, n, stats, chol, rflag, lut, work, u, v, p6, iters, flags, ws);
+    kern<<<grid, THREADS, smem, st>>>(g, ref, tar, poi, n, stats, chol, rflag, table, work, u, v, p6, iters, flags,
+                                      ws);
     return cudaGetLastError();
 }
 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                             const float* stats, const double* chol, const uint8_t* rflag, const float4* lut,
+                             const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    const bool use_lut = tune.use_lut != 0;
-#define TWDIC_ICGN_FAST(TH)                                                                                      \
-    return use_lut ? launch_icgn_fast_t<TH, true>(g, ref, tar, poi, n, stats, chol, rflag, lut, work, u, v, p6,   \
-                                                  iters, flags, tune.ctas_per_sm, st)                              \
-                   : launch_icgn_fast_t<TH, false>(g, ref, tar, poi, n, stats, chol, rflag, lut, work, u, v, p6,  \
-                                                   iters, flags, tune.ctas_per_sm, st)
-    if (tune.threads == 64) { TWDIC_ICGN_FAST(64); }
-    if (tune.threads == 256) { TWDIC_ICGN_FAST(256); }
-    TWDIC_ICGN_FAST(128);
+    if (tune.sampler != kSampWindow && !table) return cudaErrorInvalidValue;
+#define TWDIC_ICGN_FAST(TH, SA)                                                                                 \
+    return launch_icgn_fast_t<TH, SA>(g, ref, tar, poi, n, stats, chol, rflag, table, work, u, v, p6, iters,    \
+                                      flags, tune.ctas_per_sm, st)
+#define TWDIC_ICGN_FAST_T(TH)                                                                                   \
+    if (tune.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                                             \
+    if (tune.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                                           \
+    TWDIC_ICGN_FAST(TH, kSampWindow)
+    if (tune.threads == 64) { TWDIC_ICGN_FAST_T(64); }
+    if (tune.threads == 256) { TWDIC_ICGN_FAST_T(256); }
+    TWDIC_ICGN_FAST_T(128);
+#undef TWDIC_ICGN_FAST_T
 #undef TWDIC_ICGN_FAST
 }
 

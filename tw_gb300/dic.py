@@ -266,8 +266,9 @@ class DICFrame:
         ptr = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
         check(self._lib.twdic_frame_set_stream(self._h, ptr))
 
-    def set_tuning(self, icgn_threads=128, icgn_ctas_per_sm=0, icgn_use_lut=0, fftcc_use_tc=1):
-        check(self._lib.twdic_frame_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_use_lut,
+    def set_tuning(self, icgn_threads=128, icgn_ctas_per_sm=0, icgn_sampler=0, fftcc_use_tc=1):
+        """icgn_sampler: SAMPLER_WINDOW, SAMPLER_LUT or SAMPLER_NBHD."""
+        check(self._lib.twdic_frame_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler,
                                                fftcc_use_tc))
 
     def process(self, tar, u, v, zncc=None, p6=None, iters=None, flags=None):

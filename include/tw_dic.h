@@ -218,6 +218,34 @@ TWDIC_API int twdic_icgn_compute_noalloc(const twdic_params* p, const uint8_t* d
                                          const int32_t* d_poi_yx, int32_t num_pois, float* d_u, float* d_v,
                                          float* d_p6, int32_t* d_iters, uint8_t* d_flags, void* stream);
 
+/* ---- batches (no reference counterpart) ----
+ * Several frame handles' targets in one set of launches: fast-path frames
+ * with the same subset radius share one tensor-core FFT-CC launch, all
+ * fast-path frames share one persistent IC-GN launch (up to 32 frames per
+ * launch; larger batches take several).  Image pairs and POI sets may differ
+ * in size.  Results equal those of twdic_frame_process on each frame.  Each
+ * frame appears at most once per call; frames must live on the current
+ * device.  The batch's IC-GN launch shape (set_tuning) applies to all its
+ * fast-path frames.
+ *
+ * Graph mode (set_graph(1)): a call with device inputs and outputs whose
+ * frames and arrays equal the previous call's replays a CUDA graph captured
+ * from that call (one cudaGraphLaunch; `*replayed` = 1).  Inputs are read
+ * from the same device arrays, so the caller refreshes their contents
+ * between calls. */
+typedef struct twdic_batch twdic_batch;
+TWDIC_API int twdic_batch_create(twdic_batch** out);
+TWDIC_API int twdic_batch_set_stream(twdic_batch* b, void* stream);
+TWDIC_API int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler);
+TWDIC_API int twdic_batch_set_graph(twdic_batch* b, int enable);
+/* Arrays of `count` entries; zncc, p6, iters, flags (the arrays) may be NULL,
+ * strides may be NULL (contiguous images); replayed may be NULL. */
+TWDIC_API int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frames,
+                                  const uint8_t* const* tars, const int32_t* strides, int mem_in, float* const* u,
+                                  float* const* v, float* const* zncc, float* const* p6, int32_t* const* iters,
+                                  uint8_t* const* flags, int mem_out, int32_t* replayed);
+TWDIC_API int twdic_batch_destroy(twdic_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

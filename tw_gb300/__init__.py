@@ -6,7 +6,7 @@ Python mirror of the reference's cuFFTCC2D / cuICGN2D class interfaces.
 """
 from ._lib import (MEM_DEVICE, MEM_HOST, PATH_FAST, PATH_PLAIN, SAMPLER_LUT, SAMPLER_NBHD,  # noqa: F401
                    SAMPLER_WINDOW, TWDICError, load)
-from .dic import DICFrame, ICGN_FLAGS, cuFFTCC2D, cuICGN2D, make_params, num_pois, poi_positions  # noqa: F401
+from .dic import DICBatch, DICFrame, ICGN_FLAGS, cuFFTCC2D, cuICGN2D, make_params, num_pois, poi_positions  # noqa: F401
 
 __all__ = ["cuFFTCC2D", "cuICGN2D", "DICFrame", "make_params", "num_pois", "poi_positions", "TWDICError",
            "PATH_FAST", "PATH_PLAIN", "MEM_HOST", "MEM_DEVICE", "ICGN_FLAGS", "load"]

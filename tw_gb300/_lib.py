@@ -38,6 +38,8 @@ EXPORTED = (
     "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
     "twdic_frame_set_tuning", "twdic_icgn_compute_noalloc",
+    "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_graph",
+    "twdic_batch_process", "twdic_batch_destroy",
 )
 
 
@@ -104,6 +106,13 @@ def load():
         "twdic_frame_destroy": ([_VP], _I),
         "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
         "twdic_icgn_compute_noalloc": ([P, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP], _I),
+        "twdic_batch_create": ([ctypes.POINTER(_VP)], _I),
+        "twdic_batch_set_stream": ([_VP, _VP], _I),
+        "twdic_batch_set_tuning": ([_VP, _I, _I, _I], _I),
+        "twdic_batch_set_graph": ([_VP, _I], _I),
+        "twdic_batch_process": ([_VP, ctypes.c_int32, _VP, _VP, _VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I,
+                                 _I32P], _I),
+        "twdic_batch_destroy": ([_VP], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

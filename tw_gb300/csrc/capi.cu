@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -154,12 +155,14 @@ struct Engine {
     DevBuf c_stat, c_chol64, c_flag64;            // fast
     DevBuf d_lut;
     cudaEvent_t ev[7] = {};
+    cudaEvent_t ev_sync = nullptr;  // orders this handle's stream with a batch stream
     float last_times[6] = {0, 0, 0, 0, 0, 0};
     bool times_pending = false;
 
     ~Engine() {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        if (ev_sync) cudaEventDestroy(ev_sync);
         if (own_stream) cudaStreamDestroy(own_stream);
     }
 
@@ -175,6 +178,7 @@ struct Engine {
         TW_CUDA(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
         stream = own_stream;
         for (auto& e : ev) TW_CUDA(cudaEventCreate(&e));
+        TW_CUDA(cudaEventCreateWithFlags(&ev_sync, cudaEventDisableTiming));
         const size_t img = (size_t)g.pitch * p.img_height;
         TW_TRY(d_ref.ensure(img));
         TW_TRY(d_tar.ensure(img));
@@ -636,6 +640,325 @@ int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_s
         return fail(TWDIC_ERR_INVALID_ARG, "sampler must be 0 (window), 1 (LUT) or 2 (neighbourhood table)");
     h->e.icgn_tune.sampler = icgn_sampler;
     h->e.fftcc_tune.use_tc = fftcc_use_tc;
+    return TWDIC_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- batches ----
+// Several frame handles' targets in one set of launches: fast-path frames of
+// one window size share one tensor-core FFT-CC launch and all fast-path
+// frames share one persistent IC-GN launch (kMaxJobs per launch).  No
+// reference counterpart (the reference runs one frame per call).
+struct twdic_batch {
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    DevBuf d_work, d_err;
+    IcgnTune tune;
+    bool use_graph = false;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uintptr_t> key;  // the call the instantiated graph replays
+    cudaEvent_t done = nullptr;
+    ~twdic_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (done) cudaEventDestroy(done);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+};
+
+namespace {
+
+struct BatchArgs {
+    int count;
+    twdic_frame* const* frames;
+    const uint8_t* const* tars;
+    const int32_t* strides;
+    int mem_in;
+    float* const* u;
+    float* const* v;
+    float* const* zncc;
+    float* const* p6;
+    int32_t* const* iters;
+    uint8_t* const* flags;
+    int mem_out;
+};
+
+// Per-frame device outputs of a batch call: the caller's arrays (device
+// outputs) or the handle's own buffers (host outputs, copied out after).
+struct FrameOut {
+    float *u, *v, *z, *p6;
+    int* it;
+    uint8_t* fl;
+};
+
+FrameOut frame_out(Engine& e, const BatchArgs& a, int i) {
+    const bool dev = a.mem_out == TWDIC_MEM_DEVICE;
+    FrameOut o;
+    o.u = dev ? a.u[i] : e.d_u.as<float>();
+    o.v = dev ? a.v[i] : e.d_v.as<float>();
+    o.z = (dev && a.zncc && a.zncc[i]) ? a.zncc[i] : e.d_zncc.as<float>();
+    o.p6 = (dev && a.p6 && a.p6[i]) ? a.p6[i] : e.d_p6.as<float>();
+    o.it = (dev && a.iters && a.iters[i]) ? a.iters[i] : e.d_iters.as<int>();
+    o.fl = (dev && a.flags && a.flags[i]) ? a.flags[i] : e.d_flags.as<uint8_t>();
+    return o;
+}
+
+// The frame's per-frame target table for the batch's sampler.
+int prepare_target_for(Engine& e, int sampler) {
+    const Geom& g = e.g;
+    if (sampler == kSampLut) {
+        TW_TRY(e.d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
+        TW_CUDA(launch_bicubic_lut(g, e.d_tar.as<uint8_t>(), e.d_lut.as<float4>(), e.stream));
+    } else if (sampler == kSampNbhd) {
+        TW_TRY(e.d_lut.ensure(sizeof(uint4) * (size_t)g.rw * g.rh));
+        TW_CUDA(launch_nbhd_table(g, e.d_tar.as<uint8_t>(), e.d_lut.as<uint4>(), e.stream));
+    }
+    return TWDIC_OK;
+}
+
+// All work of one batch call on b->stream (the frames' streams are switched
+// to it for the duration).  Nothing here allocates once the frames' buffers
+// exist, so a second identical call can be captured into a graph.
+int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
+    const int count = a.count;
+    std::vector<int> fast_tc, fast_ic;
+    for (int i = 0; i < count; ++i) {
+        Engine& e = a.frames[i]->e;
+        e.stream = b->stream;
+        TW_TRY(e.ensure_cache(nullptr));
+        TW_TRY(e.set_tar(a.tars[i], a.strides ? a.strides[i] : 0, a.mem_in));
+        const FrameOut o = frame_out(e, a, i);
+        const size_t n = (size_t)e.n;
+        TW_CUDA(cudaMemsetAsync(o.u, 0, 4 * n, b->stream));
+        TW_CUDA(cudaMemsetAsync(o.v, 0, 4 * n, b->stream));
+        TW_CUDA(cudaMemsetAsync(o.z, 0, 4 * n, b->stream));
+        TW_CUDA(cudaMemsetAsync(o.it, 0, 4 * n, b->stream));
+        const bool fast = e.prm.path == TWDIC_PATH_FAST;
+        if (fast && e.fftcc_tune.use_tc && fftcc_tc_supported(e.g))
+            fast_tc.push_back(i);
+        else
+            TW_TRY(e.fftcc(o.u, o.v, o.z, e.d_fst.as<uint8_t>()));
+        if (fast) fast_ic.push_back(i);
+    }
+    // tensor-core FFT-CC: one launch per window size (and per kMaxJobs frames)
+    std::vector<bool> used(fast_tc.size(), false);
+    for (size_t k = 0; k < fast_tc.size(); ++k) {
+        if (used[k]) continue;
+        const int rx = a.frames[fast_tc[k]]->e.g.rx;
+        std::vector<FftccJob> jobs;
+        for (size_t m = k; m < fast_tc.size(); ++m) {
+            if (used[m] || a.frames[fast_tc[m]]->e.g.rx != rx) continue;
+            const int i = fast_tc[m];
+            Engine& e = a.frames[i]->e;
+            const FrameOut o = frame_out(e, a, i);
+            jobs.push_back(FftccJob{e.g, e.d_ref.as<uint8_t>(), e.d_tar.as<uint8_t>(), e.d_poi.as<int2>(), e.n, o.u,
+                                    o.v, o.z, e.d_fst.as<uint8_t>()});
+            used[m] = true;
+            if ((int)jobs.size() == kMaxJobs) {
+                TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->d_err.as<unsigned>(), b->stream));
+                jobs.clear();
+            }
+        }
+        if (!jobs.empty())
+            TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->d_err.as<unsigned>(), b->stream));
+    }
+    // target tables, then one persistent IC-GN launch over the fast frames
+    for (int i = 0; i < count; ++i) {
+        Engine& e = a.frames[i]->e;
+        if (e.prm.path == TWDIC_PATH_FAST)
+            TW_TRY(prepare_target_for(e, b->tune.sampler));
+        else
+            TW_TRY(e.prepare_target());
+    }
+    for (size_t k0 = 0; k0 < fast_ic.size(); k0 += kMaxJobs) {
+        IcgnJobs J;
+        J.njobs = 0;
+        J.total = 0;
+        for (size_t k = k0; k < fast_ic.size() && k < k0 + kMaxJobs; ++k) {
+            const int i = fast_ic[k];
+            Engine& e = a.frames[i]->e;
+            const FrameOut o = frame_out(e, a, i);
+            IcgnJob& jb = J.job[J.njobs++];
+            jb.g = e.g;
+            jb.ref = e.d_ref.as<uint8_t>();
+            jb.tar = e.d_tar.as<uint8_t>();
+            jb.poi = e.d_poi.as<int2>();
+            jb.stats = e.c_stat.as<float>();
+            jb.hinv = e.c_chol64.as<double>();
+            jb.rflag = e.c_flag64.as<uint8_t>();
+            jb.table = b->tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
+            jb.u = o.u;
+            jb.v = o.v;
+            jb.p6 = o.p6;
+            jb.iters = o.it;
+            jb.flags = o.fl;
+            jb.n = e.n;
+            jb.begin = J.total;
+            J.total += e.n;
+        }
+        TW_CUDA(launch_icgn_fast_jobs(J, b->d_work.as<int>(), b->tune, b->stream));
+    }
+    for (int i = 0; i < count; ++i) {
+        Engine& e = a.frames[i]->e;
+        if (e.prm.path == TWDIC_PATH_FAST) continue;
+        const FrameOut o = frame_out(e, a, i);
+        TW_TRY(e.icgn_solve(o.u, o.v, o.p6, o.it, o.fl));
+    }
+    return TWDIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int twdic_batch_create(twdic_batch** out) {
+    if (!out) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    std::unique_ptr<twdic_batch> b(new twdic_batch());
+    TW_CUDA(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
+    b->stream = b->own_stream;
+    TW_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    TW_TRY(b->d_work.ensure(sizeof(int) * 4));
+    TW_TRY(b->d_err.ensure(sizeof(unsigned)));
+    TW_CUDA(cudaMemset(b->d_err.p, 0, sizeof(unsigned)));
+    b->tune.threads = 64;
+    b->tune.sampler = kSampNbhd;
+    *out = b.release();
+    return TWDIC_OK;
+}
+
+int twdic_batch_set_stream(twdic_batch* b, void* stream) {
+    if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->key.clear();
+    return TWDIC_OK;
+}
+
+int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler) {
+    if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 64, 128 or 256");
+    if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
+        return fail(TWDIC_ERR_INVALID_ARG, "sampler must be 0, 1 or 2");
+    b->tune.threads = icgn_threads;
+    b->tune.ctas_per_sm = icgn_ctas_per_sm;
+    b->tune.sampler = icgn_sampler;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->key.clear();
+    return TWDIC_OK;
+}
+
+int twdic_batch_set_graph(twdic_batch* b, int enable) {
+    if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    b->use_graph = enable != 0;
+    return TWDIC_OK;
+}
+
+int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frames, const uint8_t* const* tars,
+                        const int32_t* strides, int mem_in, float* const* u, float* const* v, float* const* zncc,
+                        float* const* p6, int32_t* const* iters, uint8_t* const* flags, int mem_out,
+                        int32_t* replayed) {
+    if (!b || !frames || !tars || !u || !v) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    if (count < 1) return fail(TWDIC_ERR_INVALID_ARG, "count must be >= 1");
+    TW_TRY(check_mem(mem_in));
+    TW_TRY(check_mem(mem_out));
+    if (replayed) *replayed = 0;
+    for (int i = 0; i < count; ++i) {
+        if (!frames[i] || !tars[i] || !u[i] || !v[i]) return fail(TWDIC_ERR_INVALID_ARG, "NULL frame %d argument", i);
+        if (!frames[i]->e.have_ref) return fail(TWDIC_ERR_STATE, "frame %d has no reference image", i);
+        for (int k = 0; k < i; ++k)
+            if (frames[k] == frames[i]) return fail(TWDIC_ERR_INVALID_ARG, "frame %d appears twice in the batch", i);
+    }
+    const BatchArgs a{count, frames, tars, strides, mem_in, u, v, zncc, p6, iters, flags, mem_out};
+    // order after earlier work on each frame's own stream (reference uploads)
+    std::vector<cudaStream_t> saved(count);
+    for (int i = 0; i < count; ++i) {
+        Engine& e = frames[i]->e;
+        saved[i] = e.stream;
+        if (e.stream != b->stream) {
+            TW_CUDA(cudaEventRecord(e.ev_sync, e.stream));
+            TW_CUDA(cudaStreamWaitEvent(b->stream, e.ev_sync, 0));
+        }
+    }
+    auto restore = [&]() {
+        for (int i = 0; i < count; ++i) frames[i]->e.stream = saved[i];
+    };
+    // graph replay: same frames and arrays, device-resident, caches built
+    const bool graphable = b->use_graph && mem_in == TWDIC_MEM_DEVICE && mem_out == TWDIC_MEM_DEVICE;
+    std::vector<uintptr_t> key;
+    bool caches_ok = true;
+    if (graphable) {
+        key.push_back((uintptr_t)count);
+        for (int i = 0; i < count; ++i) {
+            const Engine& e = frames[i]->e;
+            caches_ok = caches_ok && e.cache_valid;
+            for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)tars[i], (uintptr_t)(strides ? strides[i] : 0),
+                                (uintptr_t)u[i], (uintptr_t)v[i], (uintptr_t)(zncc ? zncc[i] : nullptr),
+                                (uintptr_t)(p6 ? p6[i] : nullptr), (uintptr_t)(iters ? iters[i] : nullptr),
+                                (uintptr_t)(flags ? flags[i] : nullptr)})
+                key.push_back(x);
+        }
+    }
+    int rc = TWDIC_OK;
+    if (graphable && caches_ok && b->exec && key == b->key) {
+        for (int i = 0; i < count; ++i) frames[i]->e.have_tar = true;
+        cudaError_t e = cudaGraphLaunch(b->exec, b->stream);
+        if (e != cudaSuccess) rc = fail(TWDIC_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+        if (replayed && rc == TWDIC_OK) *replayed = 1;
+    } else {
+        rc = batch_enqueue(b, a);
+        if (rc == TWDIC_OK && graphable) {
+            // record the same call into a graph for the next identical call
+            if (b->exec) cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+            b->key.clear();
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                const int rc2 = batch_enqueue(b, a);
+                e = cudaStreamEndCapture(b->stream, &graph);
+                if (rc2 == TWDIC_OK && e == cudaSuccess && graph) {
+                    if (cudaGraphInstantiate(&b->exec, graph, 0) == cudaSuccess) b->key = key;
+                    else b->exec = nullptr;
+                }
+                if (graph) cudaGraphDestroy(graph);
+            }
+            cudaGetLastError();  // a failed capture leaves the batch ungraphed, not broken
+        }
+    }
+    restore();
+    if (rc != TWDIC_OK) return rc;
+    // later work on each frame's own stream waits for the batch
+    TW_CUDA(cudaEventRecord(b->done, b->stream));
+    for (int i = 0; i < count; ++i)
+        if (frames[i]->e.stream != b->stream) TW_CUDA(cudaStreamWaitEvent(frames[i]->e.stream, b->done, 0));
+    if (mem_out == TWDIC_MEM_HOST) {
+        for (int i = 0; i < count; ++i) {
+            Engine& e = frames[i]->e;
+            const FrameOut o = frame_out(e, a, i);
+            const size_t n = (size_t)e.n;
+            TW_TRY(copy_out(u[i], o.u, 4 * n, mem_out, b->stream));
+            TW_TRY(copy_out(v[i], o.v, 4 * n, mem_out, b->stream));
+            if (zncc) TW_TRY(copy_out(zncc[i], o.z, 4 * n, mem_out, b->stream));
+            if (p6) TW_TRY(copy_out(p6[i], o.p6, 24 * n, mem_out, b->stream));
+            if (iters) TW_TRY(copy_out(iters[i], o.it, 4 * n, mem_out, b->stream));
+            if (flags) TW_TRY(copy_out(flags[i], o.fl, n, mem_out, b->stream));
+        }
+        unsigned h = 0;
+        TW_CUDA(cudaMemcpyAsync(&h, b->d_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
+        TW_CUDA(cudaStreamSynchronize(b->stream));
+        if (h & kErrTimeout) {
+            cudaMemsetAsync(b->d_err.p, 0, sizeof(unsigned), b->stream);
+            return fail(TWDIC_ERR_TIMEOUT, "a bounded device-side wait gave up");
+        }
+    }
+    return TWDIC_OK;
+}
+
+int twdic_batch_destroy(twdic_batch* b) {
+    delete b;
     return TWDIC_OK;
 }
 

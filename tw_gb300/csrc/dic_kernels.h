@@ -22,6 +22,34 @@ struct IcgnTune {
     int sampler = kSampWindow;  // needs no per-frame table
 };
 
+// Image pairs (jobs) of one batched launch: each job has its own geometry,
+// images, POI set, reference cache and outputs.  The table is a kernel
+// parameter (__grid_constant__).
+constexpr int kMaxJobs = 32;
+
+struct IcgnJob {
+    Geom g;
+    const uint8_t* ref;
+    const uint8_t* tar;
+    const int2* poi;
+    const float* stats;   // 16 floats per POI (launch_ref_precompute_fast)
+    const double* hinv;   // 21 doubles per POI
+    const uint8_t* rflag;
+    const void* table;    // per-frame target table of the sampler (or null: window)
+    float* u;
+    float* v;
+    float* p6;
+    int* iters;
+    uint8_t* flags;
+    int n;      // POIs of the job
+    int begin;  // first global POI index of the job
+};
+struct IcgnJobs {
+    int njobs = 0;
+    int total = 0;  // POIs of all jobs
+    IcgnJob job[kMaxJobs];
+};
+
 // Launch shape of the tensor-core FFT-CC kernel.
 struct FftccTune {
     int use_tc = 1;       // 0: FP32 SIMT DFT kernel
@@ -52,10 +80,25 @@ cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* t
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st);
 int icgn_fast_window(const Geom& g);
+// all jobs of the table in one persistent launch
+cudaError_t launch_icgn_fast_jobs(const IcgnJobs& jobs, int* work, const IcgnTune& tune, cudaStream_t st);
 
 // ---- tensor-core FFT-CC (kernels_fftcc_tc.cu)
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                             float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st);
+// One image pair of a batched tensor-core FFT-CC launch (all jobs share rx = ry).
+struct FftccJob {
+    Geom g;
+    const uint8_t* ref;
+    const uint8_t* tar;
+    const int2* poi;
+    int n;
+    float* u;
+    float* v;
+    float* zncc;
+    uint8_t* status;
+};
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, unsigned* err, cudaStream_t st);
 bool fftcc_tc_supported(const Geom& g);
 
 }  // namespace twdic

@@ -28,6 +28,9 @@
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <memory>
+#include <mutex>
+#include <map>
 #include <cstring>
 #include <vector>
 
@@ -46,7 +49,7 @@ constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
 
 struct TcShape {
-    int N, H, HP, NP, PB, tiles1, K4, BW, WS, n_batches, n, groups;
+    int N, H, HP, NP, PB, tiles1, K4, BW, WS, groups;
     int NW4;  // 32-bit words per window row in the exact re-evaluation
     // shared twiddle tables
     int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
@@ -56,6 +59,26 @@ struct TcShape {
 };
 
 // Epilogue-4 scratch, placed in the A1/A3 region once stage 3 has read A3.
+// One image pair (job) of a launch.  All jobs of a launch share the window
+// size N; each has its own images (tensor maps), POIs and outputs.
+struct TcJob {
+    CUtensorMap map_ref;  // 64-byte aligned
+    CUtensorMap map_tar;
+    Geom g;
+    const int2* poi;
+    float* u;
+    float* v;
+    float* zncc;
+    uint8_t* status;
+    int n;            // POIs of the job
+    int batch_begin;  // first global batch index of the job
+};
+struct TcJobs {
+    int njobs;
+    int nbatch;  // batches of all jobs
+    TcJob job[kMaxJobs];
+};
+
 struct PeakScratch {
     int cand[kMaxPB][kMaxCand];
     int candS[kMaxPB][kMaxCand];
@@ -192,12 +215,9 @@ __device__ unsigned long long g_tc_trace[16];
 // (own operand buffers, TMEM columns, mbarriers and named barrier) and the
 // groups share the twiddle tables, so one group's load and MMA latency
 // overlaps another's epilogues.
-template <int NP, int HP>
-__global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUtensorMap map_ref,
-                                                     const __grid_constant__ CUtensorMap map_tar, TcShape s, Geom g,
-                                                     const int2* __restrict__ poi,
-                                                     const uint4* __restrict__ tables, float* u, float* v,
-                                                     float* zncc, uint8_t* status, unsigned* err) {
+template <int NP, int HP, bool MULTI>
+__global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
+                                                     const uint4* __restrict__ tables, unsigned* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ __align__(8) uint64_t mbar_mma[2];
     __shared__ __align__(8) uint64_t mbar_tma[2];
@@ -234,8 +254,10 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
             mbar_init(&mbar_mma[k]);
             mbar_init(&mbar_tma[k]);
         }
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_ref)) : "memory");
-        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_tar)) : "memory");
+        for (int j = 0; j < J.njobs; ++j) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&J.job[j].map_ref)) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&J.job[j].map_tar)) : "memory");
+        }
     }
     {
         uint4* dst = reinterpret_cast<uint4*>(sm);
@@ -264,11 +286,21 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
     long long tmark_ = clock64();
 #endif
 
-    for (int batch = blockIdx.x * s.groups + grp; batch < s.n_batches; batch += gridDim.x * s.groups) {
-        const int b0 = batch * PB;
+    for (int batch = blockIdx.x * s.groups + grp; batch < J.nbatch; batch += gridDim.x * s.groups) {
+        // the job (image pair, POI set) of this batch: batches of job j are
+        // [batch_begin_j, batch_begin_j + ceil(n_j / PB))
+        int jj = 0;
+        if (MULTI) {
+            while (jj + 1 < J.njobs && batch >= J.job[jj + 1].batch_begin) ++jj;
+        }
+        const TcJob& jb = J.job[jj];
+        const Geom& g = jb.g;
+        const int2* __restrict__ poi = jb.poi;
+        const int n_job = jb.n;
+        const int b0 = (batch - jb.batch_begin) * PB;
         if (t < 2 * kMaxPB * 2) (&wsum[grp][0][0])[t] = 0;
         if (t < PB) {
-            spoi[grp][t] = (b0 + t < s.n) ? poi[b0 + t] : make_int2(-1, -1);
+            spoi[grp][t] = (b0 + t < n_job) ? poi[b0 + t] : make_int2(-1, -1);
             smaxv[grp][t] = 0u;
             smaxi[grp][t] = 0x7fffffff;
             ncand[grp][t] = 1;
@@ -289,7 +321,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
                 const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
                 const int xa = x0 & ~15;
                 smis[grp][wi] = x0 - xa;
-                tma_load_2d(wwin + wi * WS, (wi & 1) ? &map_tar : &map_ref, xa, y0, tbar);
+                tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.map_tar : &jb.map_ref, xa, y0, tbar);
             }
         }
         bool ok = mbar_wait(tbar, tphase);
@@ -354,7 +386,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
             const int wf = 2 * t, wg = 2 * t + 1;
             const long long numf = (long long)n2 * wsum[grp][wf][1] - (long long)wsum[grp][wf][0] * wsum[grp][wf][0];
             const long long numg = (long long)n2 * wsum[grp][wg][1] - (long long)wsum[grp][wg][0] * wsum[grp][wg][0];
-            const bool dark = b0 + t >= s.n || numf == 0 || numg == 0;
+            const bool dark = b0 + t >= n_job || numf == 0 || numg == 0;
             sdark[grp][t] = dark ? 1 : 0;
             sscale[grp][t] = dark ? 0.f : (float)((double)n2 / sqrt((double)numf * (double)numg));
         }
@@ -657,8 +689,12 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
             }
         }
         group_sync(bar_id);
-        if (t < PB && b0 + t < s.n) {
+        if (t < PB && b0 + t < n_job) {
             const int gp = b0 + t;
+            float* u = jb.u;
+            float* v = jb.v;
+            float* zncc = jb.zncc;
+            uint8_t* status = jb.status;
             if (sdark[grp][t]) {
                 status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
             } else {
@@ -701,7 +737,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ CUt
 // ----------------------------------------------------------- host side ----
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
-bool make_shape(const Geom& g, int n, TcShape& s) {
+bool make_shape(const Geom& g, int /*n*/, TcShape& s) {
     if (g.rx != g.ry) return false;
     const int N = 2 * g.rx;
     if (N < 8 || N > 64) return false;
@@ -720,8 +756,6 @@ bool make_shape(const Geom& g, int n, TcShape& s) {
     // tensor-memory columns used by the stages must fit the allocation
     if (s.tiles1 * 2 * s.HP > kTmemCols || 2 * s.NP > kTmemCols || s.tiles1 > 2) return false;
     if (2 * pb * s.H > 128 || pb * N > 128) return false;
-    s.n = n;
-    s.n_batches = (n + pb - 1) / pb;
     const int K1 = s.NP, N1 = 2 * s.HP, NP = s.NP, K4 = s.K4;
     int o = 0;
     s.off_b1h = o; o += N1 * K1 * 2;
@@ -781,13 +815,42 @@ std::vector<uint8_t> make_tables(const TcShape& s) {
     return blob;
 }
 
+// Twiddle tables per (device, N), built once per process and kept for its
+// lifetime (a few tens of KB each), so that launches after the first never
+// allocate: a launch captured into a CUDA graph must not.
 struct TablesCache {
-    int N = -1;
-    uint4* dev = nullptr;
-    ~TablesCache() {
-        if (dev) cudaFree(dev);
-    }
+    std::mutex mu;
+    std::map<std::pair<int, int>, uint4*> dev;
 };
+TablesCache& tables_cache() {
+    static TablesCache* c = new TablesCache();  // never destroyed: may outlive the CUDA context
+    return *c;
+}
+
+cudaError_t tables_for(const TcShape& s, const uint4** out) {
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return e;
+    TablesCache& c = tables_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto it = c.dev.find({device, s.N});
+    if (it != c.dev.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    std::vector<uint8_t> blob = make_tables(s);
+    uint4* d = nullptr;
+    e = cudaMalloc(&d, blob.size());
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(d, blob.data(), blob.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return e;
+    }
+    c.dev[{device, s.N}] = d;
+    *out = d;
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -829,43 +892,62 @@ bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape&
 
 }  // namespace
 
-cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st) {
-    if (n <= 0) return cudaSuccess;
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, unsigned* err, cudaStream_t st) {
+    if (njobs < 1 || njobs > kMaxJobs) return cudaErrorInvalidValue;
     TcShape s;
-    if (!make_shape(g, n, s) || (g.pitch % 16) != 0 || (reinterpret_cast<uintptr_t>(ref) & 15) ||
-        (reinterpret_cast<uintptr_t>(tar) & 15))
-        return cudaErrorNotSupported;
-    CUtensorMap map_ref, map_tar;
-    if (!image_map(&map_ref, g, ref, s) || !image_map(&map_tar, g, tar, s)) return cudaErrorNotSupported;
-    static thread_local TablesCache cache;
-    if (cache.N != s.N) {
-        if (cache.dev) cudaFree(cache.dev);
-        cache.dev = nullptr;
-        cache.N = -1;
-        std::vector<uint8_t> blob = make_tables(s);
-        cudaError_t e = cudaMalloc(&cache.dev, blob.size());
+    if (!make_shape(jobs[0].g, 1, s)) return cudaErrorNotSupported;
+    // the table is large (tensor maps); build it in heap memory
+    std::unique_ptr<TcJobs> J(new TcJobs());
+    J->njobs = njobs;
+    int nb = 0;
+    for (int j = 0; j < njobs; ++j) {
+        const FftccJob& in = jobs[j];
+        const Geom& g = in.g;
+        if (g.rx != jobs[0].g.rx || g.ry != jobs[0].g.ry) return cudaErrorInvalidValue;  // one window size
+        if ((g.pitch % 16) != 0 || (reinterpret_cast<uintptr_t>(in.ref) & 15) ||
+            (reinterpret_cast<uintptr_t>(in.tar) & 15))
+            return cudaErrorNotSupported;
+        TcJob& o = J->job[j];
+        if (!image_map(&o.map_ref, g, in.ref, s) || !image_map(&o.map_tar, g, in.tar, s))
+            return cudaErrorNotSupported;
+        o.g = g;
+        o.poi = in.poi;
+        o.u = in.u;
+        o.v = in.v;
+        o.zncc = in.zncc;
+        o.status = in.status;
+        o.n = in.n;
+        o.batch_begin = nb;
+        nb += (in.n + s.PB - 1) / s.PB;
+    }
+    J->nbatch = nb;
+    if (nb == 0) return cudaSuccess;
+    const uint4* tables = nullptr;
+    {
+        cudaError_t e = tables_for(s, &tables);
         if (e != cudaSuccess) return e;
-        e = cudaMemcpy(cache.dev, blob.data(), blob.size(), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return e;
-        cache.N = s.N;
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void (*kern)(const CUtensorMap, const CUtensorMap, TcShape, Geom, const int2*, const uint4*, float*, float*,
-                 float*, uint8_t*, unsigned*) = nullptr;
+    void (*kern)(const TcJobs, TcShape, const uint4*, unsigned*) = nullptr;
+    const bool multi = njobs > 1;
+#define TWDIC_TC_CASE(NPV, HPV)                                                   \
+    case NPV * 100 + HPV:                                                         \
+        kern = multi ? k_fftcc_tc<NPV, HPV, true> : k_fftcc_tc<NPV, HPV, false>; \
+        break;
     switch (s.NP * 100 + s.HP) {
-        case 1608: kern = k_fftcc_tc<16, 8>; break;
-        case 1616: kern = k_fftcc_tc<16, 16>; break;
-        case 3216: kern = k_fftcc_tc<32, 16>; break;
-        case 3224: kern = k_fftcc_tc<32, 24>; break;
-        case 4824: kern = k_fftcc_tc<48, 24>; break;
-        case 4832: kern = k_fftcc_tc<48, 32>; break;
-        case 6432: kern = k_fftcc_tc<64, 32>; break;
-        case 6440: kern = k_fftcc_tc<64, 40>; break;
+        TWDIC_TC_CASE(16, 8)
+        TWDIC_TC_CASE(16, 16)
+        TWDIC_TC_CASE(32, 16)
+        TWDIC_TC_CASE(32, 24)
+        TWDIC_TC_CASE(48, 24)
+        TWDIC_TC_CASE(48, 32)
+        TWDIC_TC_CASE(64, 32)
+        TWDIC_TC_CASE(64, 40)
         default: return cudaErrorNotSupported;
     }
+#undef TWDIC_TC_CASE
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, s.smem_bytes);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -875,9 +957,16 @@ cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* ta
     const int threads = kThreads * s.groups;
     int occ = 1;
     if (s.groups == 1 && 2 * (s.smem_bytes + 2048) <= 228 * 1024) occ = 2;
-    const int grid = std::max(1, std::min(sms * occ, (s.n_batches + s.groups - 1) / s.groups));
-    kern<<<grid, threads, s.smem_bytes, st>>>(map_ref, map_tar, s, g, poi, cache.dev, u, v, zncc, status, err);
+    const int grid = std::max(1, std::min(sms * occ, (nb + s.groups - 1) / s.groups));
+    kern<<<grid, threads, s.smem_bytes, st>>>(*J, s, tables, err);
     return cudaGetLastError();
+}
+
+cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    FftccJob job{g, ref, tar, poi, n, u, v, zncc, status};
+    return launch_fftcc_tc_jobs(&job, 1, err, st);
 }
 
 }  // namespace twdic

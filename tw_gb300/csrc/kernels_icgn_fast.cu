@@ -24,6 +24,8 @@
 // LUT is built; the LUT's zero last ROI row and column are reproduced.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "dic_common.cuh"
 #include "dic_kernels.h"
 
@@ -236,42 +238,59 @@ __device__ __forceinline__ bool pass_out_of_roi(const Geom& g, const float* Wm, 
 //     pixel, k_nbhd_table), one 16-byte gather per sample, Catmull-Rom.
 // The Catmull-Rom form with central-difference derivatives is algebraically
 // the reference's Hermite bicubic LUT (TW_utils.cpp:604-700).
-template <int THREADS, int SAMPLER>
+template <int THREADS, int SAMPLER, bool MULTI>
 __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS / 2))
-    k_icgn_fast(Geom g, const uint8_t* __restrict__ ref, const uint8_t* __restrict__ tar,
-                const int2* __restrict__ poi, int n, const float* __restrict__ stats,
-                const double* __restrict__ hinv, const uint8_t* __restrict__ rflag,
-                const void* __restrict__ table, int* work, float* u, float* v, float* p6, int* iters,
-                uint8_t* flags, int ws) {
+    k_icgn_fast(const __grid_constant__ IcgnJobs J, int* work) {
     constexpr int NW = THREADS / 32;
     constexpr unsigned FULL = 0xffffffffu;
     // dynamic shared memory: [S] half2 reference gradients (R_x, R_y: half
     // integers of magnitude <= 127.5, exact in FP16), then (window path) the
-    // [ws][ws] target window
+    // [ws][ws] target window; sized for the largest subset of the launch
     extern __shared__ __align__(16) float smem_f[];
     __shared__ float red[NW][8];
     __shared__ float sW[6];
     __shared__ int sctl[3];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
-    __half2* grad = reinterpret_cast<__half2*>(smem_f);
-    float* win = smem_f + ((S + 3) & ~3);
-    const float inv_s = 1.0f / (float)S;
-    // sample k = tid + j*THREADS sits at subset offset (dx, dy); stepping j
-    // advances it by (ddx, ddy) with carry (small integers, exact in FP32)
-    const float dx_first = (float)(tid % SW - g.rx), dy_first = (float)(tid / SW - g.ry);
-    const float ddx = (float)(THREADS % SW), ddy = (float)(THREADS / SW);
-    const float rxf = (float)g.rx, swf = (float)SW;
-    // plane-0 LUT entry of image pixel (ix, iy) is lut0[iy * rw + ix]
-    const size_t plane = (size_t)g.rw * g.rh;
-    const float4* lut0 = static_cast<const float4*>(table) - ((size_t)g.sy * g.rw + g.sx);
-    const uint4* nb0 = static_cast<const uint4*>(table) - ((size_t)g.sy * g.rw + g.sx);
 
     for (;;) {
         if (tid == 0) sctl[2] = atomicAdd(work, 1);
         __syncthreads();
-        const int p = sctl[2];
-        if (p >= n) break;
+        const int pg = sctl[2];
+        if (pg >= J.total) break;
+        // the job (image pair, POI set) this POI belongs to; POIs of job j
+        // are the global indices [begin_j, begin_j + n_j)
+        int jj = 0;
+        if (MULTI) {
+            while (jj + 1 < J.njobs && pg >= J.job[jj + 1].begin) ++jj;
+        }
+        const IcgnJob& jb = J.job[jj];
+        const Geom& g = jb.g;
+        const uint8_t* __restrict__ ref = jb.ref;
+        const uint8_t* __restrict__ tar = jb.tar;
+        const int2* __restrict__ poi = jb.poi;
+        const float* __restrict__ stats = jb.stats;
+        const double* __restrict__ hinv = jb.hinv;
+        const uint8_t* __restrict__ rflag = jb.rflag;
+        float* u = jb.u;
+        float* v = jb.v;
+        float* p6 = jb.p6;
+        int* iters = jb.iters;
+        uint8_t* flags = jb.flags;
+        const int p = pg - jb.begin;
+        const int ws = 2 * (g.rx > g.ry ? g.rx : g.ry) + 11;
+        const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
+        __half2* grad = reinterpret_cast<__half2*>(smem_f);
+        float* win = smem_f + ((S + 3) & ~3);
+        const float inv_s = 1.0f / (float)S;
+        // sample k = tid + j*THREADS sits at subset offset (dx, dy); stepping j
+        // advances it by (ddx, ddy) with carry (small integers, exact in FP32)
+        const float dx_first = (float)(tid % SW - g.rx), dy_first = (float)(tid / SW - g.ry);
+        const float ddx = (float)(THREADS % SW), ddy = (float)(THREADS / SW);
+        const float rxf = (float)g.rx, swf = (float)SW;
+        // plane-0 LUT entry of image pixel (ix, iy) is lut0[iy * rw + ix]
+        const size_t plane = (size_t)g.rw * g.rh;
+        const float4* lut0 = static_cast<const float4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
+        const uint4* nb0 = static_cast<const uint4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
         const int2 pyx = poi[p];
         const int py = pyx.x, px = pyx.y;
         const float u0 = u[p], v0 = v[p];
@@ -518,16 +537,17 @@ cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, c
 
 int icgn_fast_window(const Geom& g) { return 2 * (g.rx > g.ry ? g.rx : g.ry) + 1 + 10; }
 
-template <int THREADS, int SAMPLER>
-static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi,
-                                      int n, const float* stats, const double* chol, const uint8_t* rflag,
-                                      const void* table, int* work, float* u, float* v, float* p6, int* iters,
-                                      uint8_t* flags, int ctas_per_sm, cudaStream_t st) {
-    const int ws = icgn_fast_window(g);
-    const int S = (2 * g.rx + 1) * (2 * g.ry + 1);
+template <int THREADS, int SAMPLER, bool MULTI>
+static cudaError_t launch_icgn_fast_t(const IcgnJobs& J, int* work, int ctas_per_sm, cudaStream_t st) {
+    int S_max = 0, ws_max = 0;
+    for (int j = 0; j < J.njobs; ++j) {
+        const Geom& g = J.job[j].g;
+        S_max = std::max(S_max, (2 * g.rx + 1) * (2 * g.ry + 1));
+        ws_max = std::max(ws_max, icgn_fast_window(g));
+    }
     const size_t smem =
-        sizeof(float) * ((size_t)((S + 3) & ~3) + (SAMPLER == kSampWindow ? (size_t)ws * ws : 0));
-    auto kern = k_icgn_fast<THREADS, SAMPLER>;
+        sizeof(float) * ((size_t)((S_max + 3) & ~3) + (SAMPLER == kSampWindow ? (size_t)ws_max * ws_max : 0));
+    auto kern = k_icgn_fast<THREADS, SAMPLER, MULTI>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -540,12 +560,31 @@ static cudaError_t launch_icgn_fast_t(const Geom& g, const uint8_t* ref, const u
     if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
     if (occ < 1) occ = 1;
     int grid = sms * occ;
-    if (grid > n) grid = n;
+    if (grid > J.total) grid = J.total;
     e = cudaMemsetAsync(work, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    kern<<<grid, THREADS, smem, st>>>(g, ref, tar, poi, n, stats, chol, rflag, table, work, u, v, p6, iters, flags,
-                                      ws);
+    kern<<<grid, THREADS, smem, st>>>(J, work);
     return cudaGetLastError();
+}
+
+cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& tune, cudaStream_t st) {
+    if (J.njobs < 1 || J.njobs > kMaxJobs) return cudaErrorInvalidValue;
+    if (J.total <= 0) return cudaSuccess;
+    for (int j = 0; j < J.njobs; ++j)
+        if (tune.sampler != kSampWindow && !J.job[j].table) return cudaErrorInvalidValue;
+    const bool multi = J.njobs > 1;
+#define TWDIC_ICGN_FAST(TH, SA)                                                                  \
+    return multi ? launch_icgn_fast_t<TH, SA, true>(J, work, tune.ctas_per_sm, st)               \
+                 : launch_icgn_fast_t<TH, SA, false>(J, work, tune.ctas_per_sm, st)
+#define TWDIC_ICGN_FAST_T(TH)                                                                    \
+    if (tune.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                              \
+    if (tune.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                            \
+    TWDIC_ICGN_FAST(TH, kSampWindow)
+    if (tune.threads == 64) { TWDIC_ICGN_FAST_T(64); }
+    if (tune.threads == 256) { TWDIC_ICGN_FAST_T(256); }
+    TWDIC_ICGN_FAST_T(128);
+#undef TWDIC_ICGN_FAST_T
+#undef TWDIC_ICGN_FAST
 }
 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
@@ -553,19 +592,26 @@ cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* t
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    if (tune.sampler != kSampWindow && !table) return cudaErrorInvalidValue;
-#define TWDIC_ICGN_FAST(TH, SA)                                                                                 \
-    return launch_icgn_fast_t<TH, SA>(g, ref, tar, poi, n, stats, chol, rflag, table, work, u, v, p6, iters,    \
-                                      flags, tune.ctas_per_sm, st)
-#define TWDIC_ICGN_FAST_T(TH)                                                                                   \
-    if (tune.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                                             \
-    if (tune.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                                           \
-    TWDIC_ICGN_FAST(TH, kSampWindow)
-    if (tune.threads == 64) { TWDIC_ICGN_FAST_T(64); }
-    if (tune.threads == 256) { TWDIC_ICGN_FAST_T(256); }
-    TWDIC_ICGN_FAST_T(128);
-#undef TWDIC_ICGN_FAST_T
-#undef TWDIC_ICGN_FAST
+    IcgnJobs J;
+    J.njobs = 1;
+    J.total = n;
+    IcgnJob& jb = J.job[0];
+    jb.g = g;
+    jb.ref = ref;
+    jb.tar = tar;
+    jb.poi = poi;
+    jb.stats = stats;
+    jb.hinv = chol;
+    jb.rflag = rflag;
+    jb.table = table;
+    jb.u = u;
+    jb.v = v;
+    jb.p6 = p6;
+    jb.iters = iters;
+    jb.flags = flags;
+    jb.n = n;
+    jb.begin = 0;
+    return launch_icgn_fast_jobs(J, work, tune, st);
 }
 
 }  // namespace twdic

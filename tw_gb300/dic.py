@@ -307,3 +307,68 @@ class DICFrame:
             self.close()
         except Exception:
             pass
+
+
+class DICBatch:
+    """Several DICFrame targets in one set of launches (twdic_batch_*): fast-path
+    frames of one subset radius share one tensor-core FFT-CC launch and all
+    fast-path frames one persistent IC-GN launch.  `graph=True` replays a CUDA
+    graph when a device-resident call repeats with the same frames and arrays."""
+
+    def __init__(self, graph: bool = False):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.twdic_batch_create(ctypes.byref(h)))
+        self._h = h
+        check(self._lib.twdic_batch_set_graph(self._h, 1 if graph else 0))
+        self.replayed = False
+
+    def set_stream(self, stream):
+        ptr = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
+        check(self._lib.twdic_batch_set_stream(self._h, ptr))
+
+    def set_tuning(self, icgn_threads=64, icgn_ctas_per_sm=0, icgn_sampler=2):
+        check(self._lib.twdic_batch_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler))
+
+    def process(self, frames, tars, outs):
+        """frames: list of DICFrame; tars: their target images; outs: list of
+        output dicts (DICFrame.alloc_outputs), all host or all device."""
+        k = len(frames)
+        if not (len(tars) == k == len(outs)) or k == 0:
+            raise ValueError("frames, tars and outs must have the same non-zero length")
+        keep = []
+        fr = (ctypes.c_void_p * k)(*[f._h.value for f in frames])
+        tp = (ctypes.c_void_p * k)()
+        st = (ctypes.c_int32 * k)()
+        mem_in = None
+        for i, (f, t) in enumerate(zip(frames, tars)):
+            p, stride, m, owner = _image(t, f.params.img_width, f.params.img_height)
+            keep.append(owner)
+            tp[i] = p.value
+            st[i] = stride
+            if mem_in is not None and m != mem_in:
+                raise ValueError("targets must be all host or all device")
+            mem_in = m
+
+        def arr(key):
+            a = (ctypes.c_void_p * k)()
+            for i, o in enumerate(outs):
+                a[i] = _ptr(o[key]).value
+            return a
+
+        mem_out = _mem(outs[0]["u"])
+        rep = ctypes.c_int32(0)
+        check(self._lib.twdic_batch_process(self._h, k, fr, tp, st, mem_in, arr("u"), arr("v"), arr("zncc"),
+                                            arr("p6"), arr("iters"), arr("flags"), mem_out, ctypes.byref(rep)))
+        self.replayed = bool(rep.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.twdic_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

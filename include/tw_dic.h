@@ -52,6 +52,8 @@ extern "C" {
 #define TWDIC_ERR_NO_MEMORY (-6)    /* device allocation failed or the HBM budget would be exceeded */
 #define TWDIC_ERR_UNSUPPORTED (-7)  /* parameter outside this build's limits (e.g. subset radius > 31) */
 #define TWDIC_ERR_TIMEOUT (-8)      /* a bounded device-side wait gave up */
+#define TWDIC_ERR_BUSY (-9)         /* a serving stream's queue is full: the frame was dropped */
+#define TWDIC_PENDING 1             /* twdic_poll: the frame is not done yet (not an error) */
 
 #define TWDIC_MEM_HOST 0
 #define TWDIC_MEM_DEVICE 1
@@ -245,6 +247,54 @@ TWDIC_API int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* co
                                   float* const* v, float* const* zncc, float* const* p6, int32_t* const* iters,
                                   uint8_t* const* flags, int mem_out, int32_t* replayed);
 TWDIC_API int twdic_batch_destroy(twdic_batch* b);
+
+/* Device memory a frame handle with these parameters holds after its first
+ * frame (fast path: images, POIs, outputs, per-reference cache, target
+ * table; plain path likewise), rounded to allocation granules.  Host-only. */
+TWDIC_API int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes);
+
+/* ---- serving (no reference counterpart) ----
+ * Several camera streams of possibly different sizes.  Each stream keeps its
+ * reference precompute and per-frame tables on the device; a stream is
+ * admitted only while the device memory of all admitted streams stays within
+ * hbm_budget_bytes (0 = 90 % of the free memory at creation).  twdic_submit
+ * copies a target into one of the stream's queue_depth pinned slots, or drops
+ * it with TWDIC_ERR_BUSY when all are taken (the reference's bounded frame
+ * queue).  A scheduler thread batches the oldest pending frame of every idle
+ * stream (up to max_batch) into one twdic_batch launch on a free lane (CUDA
+ * stream, up to `lanes` batches in flight), so frames that arrive while
+ * others are on the GPU join the next batch.  Results equal
+ * twdic_frame_process on the same frame.  twdic_poll returns TWDIC_PENDING
+ * until the frame is done (wait = 1 blocks), then copies the results out and
+ * frees the slot; latency_ms is submit-to-done. */
+typedef struct twdic_server twdic_server;
+typedef struct {
+    uint64_t hbm_budget_bytes;
+    int32_t max_batch;    /* 1..32 frames per batched launch */
+    int32_t queue_depth;  /* 1..64 pending frames per stream */
+    int32_t lanes;        /* 1..4 batches in flight */
+    int32_t use_graph;    /* replay CUDA graphs when a stream mix repeats */
+    int32_t start_paused; /* 1: hold frames until twdic_server_resume */
+    int32_t icgn_threads; /* fast IC-GN launch shape (0 = default) */
+    int32_t icgn_sampler; /* fast IC-GN target sampler when icgn_threads > 0 */
+} twdic_server_config;
+typedef struct {
+    uint64_t submitted, completed, dropped, batches, batched_frames, graph_replays;
+    uint64_t committed_bytes, budget_bytes;
+    int32_t streams;
+    double p50_ms, p99_ms, max_ms; /* submit-to-done latency over completed frames */
+} twdic_server_counters;
+TWDIC_API int twdic_server_create(const twdic_server_config* cfg, twdic_server** out);
+TWDIC_API int twdic_server_add_stream(twdic_server* s, const twdic_params* p, int32_t* stream_id);
+TWDIC_API int twdic_server_remove_stream(twdic_server* s, int32_t stream_id);
+TWDIC_API int twdic_server_set_reference(twdic_server* s, int32_t stream_id, const uint8_t* img, int32_t stride);
+TWDIC_API int twdic_submit(twdic_server* s, int32_t stream_id, const uint8_t* tar, int32_t stride,
+                           uint64_t* ticket);
+TWDIC_API int twdic_poll(twdic_server* s, uint64_t ticket, int32_t wait, float* u, float* v, float* zncc,
+                         float* p6, int32_t* iters, uint8_t* flags, double* latency_ms);
+TWDIC_API int twdic_server_resume(twdic_server* s);
+TWDIC_API int twdic_server_stats(twdic_server* s, twdic_server_counters* out);
+TWDIC_API int twdic_server_destroy(twdic_server* s);
 
 #ifdef __cplusplus
 }

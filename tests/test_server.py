@@ -1,0 +1,107 @@
+"""Serving (twdic_server_*): admission by HBM budget, drop-if-full queues,
+continuous batching across streams of different sizes; each frame's result is
+the same alone and in the mix."""
+import numpy as np
+import pytest
+
+from tw_gb300 import PATH_FAST, dic, synth
+from tw_gb300.serve import DICServer, frame_device_bytes
+
+
+def _params(g, path=PATH_FAST):
+    return dic.make_params(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r,
+                           g.grid, g.grid, g.margin, g.margin, g.max_iter, g.delta_p, path)
+
+
+def test_frame_device_bytes_formula():
+    """Host-only estimate used for admission: images padded to 16-byte rows,
+    per-POI buffers and the fast path's cache and neighbourhood table, each
+    rounded up to 2 MiB."""
+    _, g = synth.small_case(h=160, w=197, r=10, grid=7)
+    p = _params(g)
+    n = dic.num_pois(p)[0] * dic.num_pois(p)[1]
+    r = lambda b: -(-b // (2 << 20)) * (2 << 20)  # noqa: E731
+    pitch = (197 + 15) // 16 * 16
+    want = (2 * r(pitch * 160) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 3 * r(1024)
+            + r(64 * n) + r(168 * n) + r(n) + r(16 * g.roi_w * g.roi_h))
+    assert frame_device_bytes(p) == want
+    big = _params(synth.Geometry(2048, 2048, 1, 1, 2046, 2046, 20, 5, 20))
+    assert frame_device_bytes(big) > 128 << 20  # 155k POIs: 67 MB neighbourhood table, 36 MB cache
+
+
+def test_frame_device_bytes_rejects_bad_params():
+    p = dic.make_params(100, 100, 0, 0, 100, 100, 10, 10, 5, 5, 0, 0)  # no image border
+    with pytest.raises(dic.TWDICError):
+        frame_device_bytes(p)
+
+
+CASES = [(160, 192, 10, 7, 21), (130, 257, 10, 5, 22), (200, 150, 16, 9, 23)]
+
+
+@pytest.mark.gpu
+def test_results_same_alone_and_in_the_mix():
+    pairs = [synth.small_case(h=h, w=w, r=r, grid=gr, seed=s) for h, w, r, gr, s in CASES]
+    pairs2 = [synth.small_case(h=h, w=w, r=r, grid=gr, seed=s, u0=-0.7, v0=1.3) for h, w, r, gr, s in CASES]
+    srv = DICServer(max_batch=8, queue_depth=4, lanes=2)
+    sids = []
+    for pair, g in pairs:
+        sid = srv.add_stream(_params(g))
+        srv.set_reference(sid, pair.ref)
+        sids.append(sid)
+    # frames of all streams interleaved, several in flight at once
+    tickets = []
+    for rnd in range(3):
+        for sid, (pair, _), (pair2, _) in zip(sids, pairs, pairs2):
+            tar = pair.tar if rnd % 2 == 0 else pair2.tar
+            t = srv.submit(sid, tar)
+            assert t is not None
+            tickets.append((sid, t, rnd))
+    got = {(sid, rnd): srv.poll(sid, t) for sid, t, rnd in tickets}
+    st = srv.stats()
+    assert st["completed"] == len(tickets) and st["dropped"] == 0
+    assert st["batches"] >= 1 and st["batched_frames"] == len(tickets)
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    for sid, (pair, g), (pair2, _) in zip(sids, pairs, pairs2):
+        f = dic.DICFrame(_params(g))
+        f.set_reference(pair.ref)
+        for rnd in range(3):
+            w = f.alloc_outputs()
+            f.process(pair.tar if rnd % 2 == 0 else pair2.tar, **w)
+            o = got[(sid, rnd)]
+            assert (w["flags"] == 0).mean() > 0.9
+            for k in w:
+                np.testing.assert_array_equal(o[k], w[k], err_msg=f"stream {sid} frame {rnd} {k}")
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_admission_by_hbm_budget():
+    (_, g1), (_, g2) = synth.small_case(h=160, w=192, r=10), synth.small_case(h=200, w=150, r=16)
+    b1 = frame_device_bytes(_params(g1))
+    srv = DICServer(hbm_budget_bytes=b1 + (8 << 20), queue_depth=1)
+    srv.add_stream(_params(g1))
+    with pytest.raises(dic.TWDICError) as e:
+        srv.add_stream(_params(g2))
+    assert "NO_MEMORY" in str(e.value)
+    st = srv.stats()
+    assert st["streams"] == 1 and st["committed_bytes"] <= st["budget_bytes"]
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_full_queue_drops_frames():
+    pair, g = synth.small_case()
+    srv = DICServer(queue_depth=2, start_paused=True)
+    sid = srv.add_stream(_params(g))
+    srv.set_reference(sid, pair.ref)
+    t1, t2 = srv.submit(sid, pair.tar), srv.submit(sid, pair.tar)
+    assert t1 is not None and t2 is not None
+    assert srv.submit(sid, pair.tar) is None  # both slots taken: dropped
+    assert srv.poll(sid, t1, wait=False) is None  # held while paused
+    srv.resume()
+    a, b = srv.poll(sid, t1), srv.poll(sid, t2)
+    for k in ("u", "v", "p6", "iters", "flags"):
+        np.testing.assert_array_equal(a[k], b[k])
+    st = srv.stats()
+    assert st["dropped"] == 1 and st["completed"] == 2
+    srv.close()

@@ -21,7 +21,9 @@ ERR = {
     -6: "TWDIC_ERR_NO_MEMORY",
     -7: "TWDIC_ERR_UNSUPPORTED",
     -8: "TWDIC_ERR_TIMEOUT",
+    -9: "TWDIC_ERR_BUSY",
 }
+PENDING = 1  # twdic_poll: not done yet
 MEM_HOST = 0
 MEM_DEVICE = 1
 PATH_PLAIN = 0
@@ -39,7 +41,9 @@ EXPORTED = (
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
     "twdic_frame_set_tuning", "twdic_icgn_compute_noalloc",
     "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_graph",
-    "twdic_batch_process", "twdic_batch_destroy",
+    "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
+    "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
+    "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
 )
 
 
@@ -62,6 +66,25 @@ class Params(ctypes.Structure):
         ("max_iterations", ctypes.c_int32),
         ("delta_p", ctypes.c_float),
         ("path", ctypes.c_int32),
+    ]
+
+
+class ServerConfig(ctypes.Structure):
+    """twdic_server_config"""
+    _fields_ = [
+        ("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("queue_depth", ctypes.c_int32),
+        ("lanes", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("start_paused", ctypes.c_int32),
+        ("icgn_threads", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32),
+    ]
+
+
+class ServerCounters(ctypes.Structure):
+    """twdic_server_counters"""
+    _fields_ = [
+        ("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("dropped", ctypes.c_uint64),
+        ("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
+        ("committed_bytes", ctypes.c_uint64), ("budget_bytes", ctypes.c_uint64), ("streams", ctypes.c_int32),
+        ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
     ]
 
 
@@ -113,6 +136,17 @@ def load():
         "twdic_batch_process": ([_VP, ctypes.c_int32, _VP, _VP, _VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I,
                                  _I32P], _I),
         "twdic_batch_destroy": ([_VP], _I),
+        "twdic_frame_device_bytes": ([P, ctypes.POINTER(ctypes.c_uint64)], _I),
+        "twdic_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)], _I),
+        "twdic_server_add_stream": ([_VP, P, _I32P], _I),
+        "twdic_server_remove_stream": ([_VP, ctypes.c_int32], _I),
+        "twdic_server_set_reference": ([_VP, ctypes.c_int32, _VP, ctypes.c_int32], _I),
+        "twdic_submit": ([_VP, ctypes.c_int32, _VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)], _I),
+        "twdic_poll": ([_VP, ctypes.c_uint64, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP,
+                        ctypes.POINTER(ctypes.c_double)], _I),
+        "twdic_server_resume": ([_VP], _I),
+        "twdic_server_stats": ([_VP, ctypes.POINTER(ServerCounters)], _I),
+        "twdic_server_destroy": ([_VP], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -628,6 +628,36 @@ int twdic_frame_destroy(twdic_frame* h) {
     return TWDIC_OK;
 }
 
+// Device memory of a frame handle after its first fast-path frame (the
+// allocations of Engine::init, the per-reference cache and the default
+// neighbourhood table), each rounded up to the 2 MiB the allocator may
+// reserve for it.  Host-only: no CUDA call.
+int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
+    if (!bytes) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(validate(p, true, true));
+    int nx = 0, ny = 0;
+    TW_TRY(num_pois_of(*p, &nx, &ny));
+    const uint64_t n = (uint64_t)nx * ny;
+    const uint64_t pitch = (uint64_t)((p->img_width + 15) & ~15);
+    const uint64_t img = pitch * (uint64_t)p->img_height;
+    auto r = [](uint64_t b) { return (b + (2ull << 20) - 1) / (2ull << 20) * (2ull << 20); };
+    uint64_t t = 0;
+    t += 2 * r(img);                                        // reference, target
+    t += r(8 * n);                                          // POIs
+    t += 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n);  // u, v, zncc, status, p6, iters, flags
+    t += 3 * r(1024);                                       // error flag, work counter, twiddles
+    if (p->path == TWDIC_PATH_PLAIN) {
+        const uint64_t S = (uint64_t)(2 * p->subset_x + 1) * (2 * p->subset_y + 1);
+        t += r(4 * n * S) + r(24 * n * S) + r(144 * n) + r(4 * n) + r(n);
+        t += r(64 * (uint64_t)p->roi_width * p->roi_height);  // float LUT
+    } else {
+        t += r(64 * n) + r(168 * n) + r(n);                 // statistics, inverse Hessian, flags
+        t += r(16 * (uint64_t)p->roi_width * p->roi_height);  // neighbourhood table
+    }
+    *bytes = t;
+    return TWDIC_OK;
+}
+
 // Tuning (internal to the Python autotuner; not part of the reference interface).
 int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                            int fftcc_use_tc) {
@@ -828,10 +858,8 @@ int twdic_batch_create(twdic_batch** out) {
 
 int twdic_batch_set_stream(twdic_batch* b, void* stream) {
     if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    // a captured graph may be launched into any stream: it stays valid
     b->stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    b->exec = nullptr;
-    b->key.clear();
     return TWDIC_OK;
 }
 

@@ -340,6 +340,13 @@ def _run_gpu(args, world, rank, local, torch):
             "gpu_launches": 3 * args.steps,
             "clocks": clk,
             "wall_s_timed_region": round(t_wall, 3)}
+    if rank == 0 and not args.no_serving:
+        # serving (12 camera streams, Poisson arrivals) and batched uneven
+        # pairs, each on its own synthetic data generated before its run
+        from tw_gb300.batch_bench import run_batched
+        from tw_gb300.serve_bench import run_serving
+        line["serving"] = run_serving(seconds=4.0)
+        line["batched"] = run_batched(pairs=48, steps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O  # noqa: F401  (CPU baseline leg)
         line["cpu_baseline"] = cpu_baseline(pair, g, poi)
@@ -414,6 +421,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving and batched legs")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -176,3 +176,28 @@ def small_case(h: int = 160, w: int = 192, r: int = 10, grid: int = 7, seed: int
     field, grad = affine_field(u0, v0, 0.004, -0.002, 0.003, -0.0035, w / 2, h / 2)
     pair = make_pair(h, w, n, field, grad, seed, description=f"{w}x{h} affine speckle pair")
     return pair, Geometry(w, h, 1, 1, w - 2, h - 2, r, grid, 12)
+
+
+def camera_sequence(w: int, h: int, frames: int = 3, seed: int = 31, r: int = 15, grid: int = 8,
+                    margin: int = 20):
+    """A simulated camera: one reference and `frames` targets under a linear
+    ramp of strain (up to 1 % at the last frame) plus a drift of 0.5 px per
+    frame, speckle density as in the 512x512 case.  Returns (ref, targets,
+    Geometry) with 31x31 subsets at step 8 by default."""
+    rng_seed = seed
+    n = int(6000 * h * w / (512 * 512))
+    rng = np.random.default_rng(rng_seed)
+    intensity = speckle_intensity(h, w, n, rng)
+    ref = np.clip(np.rint(intensity), 0, 255).astype(np.uint8)
+    tars = []
+    yp, xp = np.meshgrid(np.arange(h, dtype=np.float64), np.arange(w, dtype=np.float64), indexing="ij")
+    cx, cy = w / 2, h / 2
+    for k in range(1, frames + 1):
+        s = 0.01 * k / frames
+        u0, v0, ux, vy = 0.5 * k, -0.35 * k, s, -0.6 * s
+        # inverse of the affine map X + u(X) = x' in closed form
+        X = cx + (xp - cx - u0) / (1.0 + ux)
+        Y = cy + (yp - cy - v0) / (1.0 + vy)
+        tar_f = bicubic_sample(intensity, X, Y) + rng.normal(0.0, 2.0, (h, w))
+        tars.append(np.clip(np.rint(tar_f), 0, 255).astype(np.uint8))
+    return ref, tars, Geometry(w, h, 1, 1, w - 2, h - 2, r, grid, margin)

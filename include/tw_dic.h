@@ -187,6 +187,27 @@ TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                                      int fftcc_use_tc);
 
+/* FFT-CC tile of a frame handle: use_tc (tensor-core kernel), groups (0 = as
+ * many 128-thread groups per CTA as fit, 1 = one), pois_per_group (POIs per
+ * group batch, 0 = the most the tiles hold).  No reference counterpart. */
+TWDIC_API int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group);
+
+typedef struct {
+    int32_t icgn_threads, icgn_ctas_per_sm, icgn_sampler;
+    int32_t fftcc_use_tc, fftcc_groups, fftcc_pois_per_group;
+    float fftcc_ms, icgn_ms; /* phase times of the chosen shapes (target preparation included in icgn_ms) */
+    int32_t from_cache;      /* 1: read from the cache file, not measured */
+} twdic_tuning;
+TWDIC_API int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out);
+/* Autotuner (no reference counterpart): times the FFT-CC tile shapes and the
+ * IC-GN launch shapes and samplers on this handle's reference and the given
+ * target (one warm-up and three timed frames each, median), keeps the fastest
+ * and returns it.  cache_path (may be NULL): a text file of earlier choices
+ * keyed by GPU name, SM count and every geometry parameter; a hit is applied
+ * without timing, a new choice is appended. */
+TWDIC_API int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int mem,
+                                   const char* cache_path, twdic_tuning* out);
+
 /* ------------------------------------------- IC-GN without allocation --- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they run IC-GN: a real-time camera loop whose frame deadline

@@ -44,6 +44,7 @@ EXPORTED = (
     "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
     "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
+    "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
 )
 
 
@@ -75,6 +76,15 @@ class ServerConfig(ctypes.Structure):
         ("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("queue_depth", ctypes.c_int32),
         ("lanes", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("start_paused", ctypes.c_int32),
         ("icgn_threads", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32),
+    ]
+
+
+class Tuning(ctypes.Structure):
+    """twdic_tuning"""
+    _fields_ = [
+        ("icgn_threads", ctypes.c_int32), ("icgn_ctas_per_sm", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32),
+        ("fftcc_use_tc", ctypes.c_int32), ("fftcc_groups", ctypes.c_int32), ("fftcc_pois_per_group", ctypes.c_int32),
+        ("fftcc_ms", ctypes.c_float), ("icgn_ms", ctypes.c_float), ("from_cache", ctypes.c_int32),
     ]
 
 
@@ -147,6 +157,9 @@ def load():
         "twdic_server_resume": ([_VP], _I),
         "twdic_server_stats": ([_VP, ctypes.POINTER(ServerCounters)], _I),
         "twdic_server_destroy": ([_VP], _I),
+        "twdic_frame_set_fftcc_tuning": ([_VP, _I, _I, _I], _I),
+        "twdic_frame_get_tuning": ([_VP, ctypes.POINTER(Tuning)], _I),
+        "twdic_frame_autotune": ([_VP, _VP, ctypes.c_int32, _I, ctypes.c_char_p, ctypes.POINTER(Tuning)], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

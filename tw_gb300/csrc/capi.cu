@@ -5,6 +5,7 @@
 // host<->device staging on the handle's stream, and the per-reference cache.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -250,7 +251,7 @@ struct Engine {
         const int2* poi = d_poi.as<int2>();
         if (prm.path == TWDIC_PATH_FAST && fftcc_tune.use_tc && fftcc_tc_supported(g)) {
             TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st,
-                                    d_err.as<unsigned>(), stream));
+                                    d_err.as<unsigned>(), fftcc_tune, stream));
         } else {
             TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, d_tw.as<float2>(), u, v, z,
                                        st, stream));
@@ -673,6 +674,199 @@ int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_s
     return TWDIC_OK;
 }
 
+
+int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (groups < 0 || groups > 2 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
+    h->e.fftcc_tune.use_tc = use_tc;
+    h->e.fftcc_tune.groups = groups;
+    h->e.fftcc_tune.pois_per_group = pois_per_group;
+    return TWDIC_OK;
+}
+
+int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out) {
+    if (!h || !out) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->icgn_threads = h->e.icgn_tune.threads;
+    out->icgn_ctas_per_sm = h->e.icgn_tune.ctas_per_sm;
+    out->icgn_sampler = h->e.icgn_tune.sampler;
+    out->fftcc_use_tc = h->e.fftcc_tune.use_tc;
+    out->fftcc_groups = h->e.fftcc_tune.groups;
+    out->fftcc_pois_per_group = h->e.fftcc_tune.pois_per_group;
+    return TWDIC_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Key of a tuning cache entry: the GPU and every parameter that changes the
+// launch shapes' costs.
+std::string tuning_key(const Engine& e) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    std::memset(&prop, 0, sizeof(prop));
+    cudaGetDeviceProperties(&prop, dev);
+    std::string name(prop.name);
+    for (char& c : name)
+        if (c == ' ' || c == '|') c = '_';
+    const twdic_params& p = e.prm;
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s|sm%d|%dx%d|roi%dx%d|r%dx%d|g%dx%d|m%dx%d|path%d", name.c_str(),
+             prop.multiProcessorCount, p.img_width, p.img_height, p.roi_width, p.roi_height, p.subset_x, p.subset_y,
+             p.grid_space_x, p.grid_space_y, p.margin_x, p.margin_y, p.path);
+    return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& key, twdic_tuning* t) {
+    FILE* f = path ? std::fopen(path, "r") : nullptr;
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (std::fgets(line, sizeof(line), f)) {
+        const size_t k = key.size();
+        if (std::strncmp(line, key.c_str(), k) != 0 || line[k] != ' ') continue;
+        twdic_tuning c;
+        std::memset(&c, 0, sizeof(c));
+        if (std::sscanf(line + k, " %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm, &c.icgn_sampler,
+                        &c.fftcc_use_tc, &c.fftcc_groups, &c.fftcc_pois_per_group, &c.fftcc_ms, &c.icgn_ms) == 8) {
+            *t = c;  // the last entry for a key wins
+            found = true;
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Measures the launch shapes on this frame's target and keeps the fastest:
+// the FFT-CC tile (groups per CTA, POIs per group batch) by the FFT-CC phase
+// time, the IC-GN shape (threads per CTA, target sampler) by the time of
+// target preparation plus IC-GN; each candidate takes one warm-up and three
+// timed frames (median).  With cache_path, an entry for this GPU and these
+// parameters is reused without timing, and a new choice is appended.
+int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int mem, const char* cache_path,
+                         twdic_tuning* out) {
+    if (!h || !tar || !out) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    Engine& e = h->e;
+    if (!e.have_ref) return fail(TWDIC_ERR_STATE, "autotune needs a reference image");
+    const std::string key = tuning_key(e);
+    twdic_tuning t;
+    std::memset(&t, 0, sizeof(t));
+    if (cache_lookup(cache_path, key, &t)) {
+        e.icgn_tune.threads = t.icgn_threads;
+        e.icgn_tune.ctas_per_sm = t.icgn_ctas_per_sm;
+        e.icgn_tune.sampler = t.icgn_sampler;
+        e.fftcc_tune.use_tc = t.fftcc_use_tc;
+        e.fftcc_tune.groups = t.fftcc_groups;
+        e.fftcc_tune.pois_per_group = t.fftcc_pois_per_group;
+        t.from_cache = 1;
+        *out = t;
+        return TWDIC_OK;
+    }
+    const IcgnTune icgn0 = e.icgn_tune;
+    const FftccTune fft0 = e.fftcc_tune;
+    auto measure = [&](float* fftcc_ms, float* icgn_ms) -> int {
+        std::vector<float> fa, ia;
+        for (int r = 0; r < 4; ++r) {
+            TW_TRY(twdic_frame_process(h, tar, stride, mem, e.d_u.as<float>(), e.d_v.as<float>(),
+                                       e.d_zncc.as<float>(), e.d_p6.as<float>(), e.d_iters.as<int>(),
+                                       e.d_flags.as<uint8_t>(), TWDIC_MEM_DEVICE));
+            float t6[6];
+            TW_TRY(twdic_frame_phase_times(h, t6));
+            if (r == 0) continue;
+            fa.push_back(t6[1]);
+            ia.push_back(t6[2] + t6[3]);
+        }
+        std::sort(fa.begin(), fa.end());
+        std::sort(ia.begin(), ia.end());
+        *fftcc_ms = fa[fa.size() / 2];
+        *icgn_ms = ia[ia.size() / 2];
+        return TWDIC_OK;
+    };
+    // FFT-CC tile shapes (the IC-GN shape stays as it was)
+    FftccTune best_f = fft0;
+    float best_fms = 1e30f;
+    if (e.prm.path == TWDIC_PATH_FAST && fftcc_tc_supported(e.g)) {
+        for (int groups : {0, 1}) {
+            for (int ppg : {0, 2, 1}) {
+                FftccTune c;
+                c.use_tc = 1;
+                c.groups = groups;
+                c.pois_per_group = ppg;
+                e.fftcc_tune = c;
+                float f = 0, ic = 0;
+                const int rc = measure(&f, &ic);
+                if (rc != TWDIC_OK) {
+                    e.fftcc_tune = fft0;
+                    e.icgn_tune = icgn0;
+                    return rc;
+                }
+                if (f < best_fms) {
+                    best_fms = f;
+                    best_f = c;
+                }
+            }
+        }
+    }
+    e.fftcc_tune = best_f;
+    // IC-GN shapes
+    IcgnTune best_i = icgn0;
+    float best_ims = 1e30f, fms = best_fms;
+    if (e.prm.path == TWDIC_PATH_FAST) {
+        for (int threads : {64, 128, 256}) {
+            for (int sampler : {kSampNbhd, kSampLut, kSampWindow}) {
+                IcgnTune c;
+                c.threads = threads;
+                c.ctas_per_sm = 0;
+                c.sampler = sampler;
+                e.icgn_tune = c;
+                float f = 0, ic = 0;
+                const int rc = measure(&f, &ic);
+                if (rc != TWDIC_OK) {
+                    e.fftcc_tune = fft0;
+                    e.icgn_tune = icgn0;
+                    return rc;
+                }
+                if (ic < best_ims) {
+                    best_ims = ic;
+                    best_i = c;
+                    if (best_fms >= 1e30f) fms = f;
+                }
+            }
+        }
+    } else {
+        float f = 0, ic = 0;
+        TW_TRY(measure(&f, &ic));
+        best_ims = ic;
+        fms = f;
+    }
+    e.icgn_tune = best_i;
+    t.icgn_threads = best_i.threads;
+    t.icgn_ctas_per_sm = best_i.ctas_per_sm;
+    t.icgn_sampler = best_i.sampler;
+    t.fftcc_use_tc = e.fftcc_tune.use_tc;
+    t.fftcc_groups = e.fftcc_tune.groups;
+    t.fftcc_pois_per_group = e.fftcc_tune.pois_per_group;
+    t.fftcc_ms = fms < 1e30f ? fms : 0.f;
+    t.icgn_ms = best_ims;
+    t.from_cache = 0;
+    if (cache_path) {
+        FILE* f = std::fopen(cache_path, "a");
+        if (f) {
+            std::fprintf(f, "%s %d %d %d %d %d %d %.4f %.4f\n", key.c_str(), t.icgn_threads, t.icgn_ctas_per_sm,
+                         t.icgn_sampler, t.fftcc_use_tc, t.fftcc_groups, t.fftcc_pois_per_group, t.fftcc_ms,
+                         t.icgn_ms);
+            std::fclose(f);
+        }
+    }
+    *out = t;
+    return TWDIC_OK;
+}
 }  // extern "C"
 
 // ------------------------------------------------------------- batches ----
@@ -685,6 +879,7 @@ struct twdic_batch {
     cudaStream_t own_stream = nullptr;
     DevBuf d_work, d_err;
     IcgnTune tune;
+    FftccTune fftcc_tune;
     bool use_graph = false;
     cudaGraphExec_t exec = nullptr;
     std::vector<uintptr_t> key;  // the call the instantiated graph replays
@@ -785,12 +980,14 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
                                     o.v, o.z, e.d_fst.as<uint8_t>()});
             used[m] = true;
             if ((int)jobs.size() == kMaxJobs) {
-                TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->d_err.as<unsigned>(), b->stream));
+                TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
+                                             b->stream));
                 jobs.clear();
             }
         }
         if (!jobs.empty())
-            TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->d_err.as<unsigned>(), b->stream));
+            TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
+                                         b->stream));
     }
     // target tables, then one persistent IC-GN launch over the fast frames
     for (int i = 0; i < count; ++i) {

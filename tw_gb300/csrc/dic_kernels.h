@@ -52,7 +52,9 @@ struct IcgnJobs {
 
 // Launch shape of the tensor-core FFT-CC kernel.
 struct FftccTune {
-    int use_tc = 1;       // 0: FP32 SIMT DFT kernel
+    int use_tc = 1;          // 0: FP32 SIMT DFT kernel
+    int groups = 0;          // tensor-core kernel: 0 = as many 128-thread groups per CTA as fit, 1 = one
+    int pois_per_group = 0;  // POIs per group batch (0 = the most the tiles hold)
 };
 
 // ---- plain FP32 path (kernels_plain.cu)
@@ -85,7 +87,8 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& jobs, int* work, const IcgnTun
 
 // ---- tensor-core FFT-CC (kernels_fftcc_tc.cu)
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st);
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, const FftccTune& tune,
+                            cudaStream_t st);
 // One image pair of a batched tensor-core FFT-CC launch (all jobs share rx = ry).
 struct FftccJob {
     Geom g;
@@ -98,7 +101,8 @@ struct FftccJob {
     float* zncc;
     uint8_t* status;
 };
-cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, unsigned* err, cudaStream_t st);
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err,
+                                 cudaStream_t st);
 bool fftcc_tc_supported(const Geom& g);
 
 }  // namespace twdic

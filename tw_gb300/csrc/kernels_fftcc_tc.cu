@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
 // ----------------------------------------------------------- host side ----
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
-bool make_shape(const Geom& g, int /*n*/, TcShape& s) {
+bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     if (g.rx != g.ry) return false;
     const int N = 2 * g.rx;
     if (N < 8 || N > 64) return false;
@@ -749,6 +749,7 @@ bool make_shape(const Geom& g, int /*n*/, TcShape& s) {
     pb = std::min(pb, 64 / s.H);
     pb = std::min(pb, 128 / N);
     pb = std::min(pb, kMaxPB);
+    if (tune.pois_per_group > 0) pb = std::min(pb, tune.pois_per_group);  // tuned batch size
     if (pb < 1 || 2 * s.HP > 80) return false;
     s.PB = pb;
     s.tiles1 = (pb * 2 * N + 127) / 128;
@@ -783,6 +784,7 @@ bool make_shape(const Geom& g, int /*n*/, TcShape& s) {
     s.group_bytes = round_up(q, 1024);
     const int limit = 225 * 1024;
     s.groups = (o + 2 * s.group_bytes <= limit) ? 2 : 1;
+    if (tune.groups == 1) s.groups = 1;  // tuned: one group per CTA (two CTAs per SM when they fit)
     s.smem_bytes = o + s.groups * s.group_bytes;
     return s.smem_bytes <= limit;
 }
@@ -856,7 +858,7 @@ cudaError_t tables_for(const TcShape& s, const uint4** out) {
 
 bool fftcc_tc_supported(const Geom& g) {
     TcShape s;
-    return (g.pitch % 16) == 0 && make_shape(g, 1, s);
+    return (g.pitch % 16) == 0 && make_shape(g, FftccTune{}, s);
 }
 
 namespace {
@@ -892,10 +894,11 @@ bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape&
 
 }  // namespace
 
-cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, unsigned* err, cudaStream_t st) {
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err,
+                                 cudaStream_t st) {
     if (njobs < 1 || njobs > kMaxJobs) return cudaErrorInvalidValue;
     TcShape s;
-    if (!make_shape(jobs[0].g, 1, s)) return cudaErrorNotSupported;
+    if (!make_shape(jobs[0].g, tune, s)) return cudaErrorNotSupported;
     // the table is large (tensor maps); build it in heap memory
     std::unique_ptr<TcJobs> J(new TcJobs());
     J->njobs = njobs;
@@ -963,10 +966,11 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, unsigned* err,
 }
 
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, cudaStream_t st) {
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, const FftccTune& tune,
+                            cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     FftccJob job{g, ref, tar, poi, n, u, v, zncc, status};
-    return launch_fftcc_tc_jobs(&job, 1, err, st);
+    return launch_fftcc_tc_jobs(&job, 1, tune, err, st);
 }
 
 }  // namespace twdic

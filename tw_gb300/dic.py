@@ -271,6 +271,24 @@ class DICFrame:
         check(self._lib.twdic_frame_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler,
                                                fftcc_use_tc))
 
+    def set_fftcc_tuning(self, use_tc=1, groups=0, pois_per_group=0):
+        check(self._lib.twdic_frame_set_fftcc_tuning(self._h, use_tc, groups, pois_per_group))
+
+    def tuning(self) -> dict:
+        t = _lib.Tuning()
+        check(self._lib.twdic_frame_get_tuning(self._h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in _lib.Tuning._fields_}
+
+    def autotune(self, tar, cache_path=None) -> dict:
+        """Time the launch shapes on this target, keep the fastest (see
+        twdic_frame_autotune); `cache_path` reuses and records choices."""
+        p, stride, mem_in, _keep = _image(tar, self.params.img_width, self.params.img_height)
+        t = _lib.Tuning()
+        check(self._lib.twdic_frame_autotune(self._h, p, stride, mem_in,
+                                             None if cache_path is None else str(cache_path).encode(),
+                                             ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in _lib.Tuning._fields_}
+
     def process(self, tar, u, v, zncc=None, p6=None, iters=None, flags=None):
         """Outputs are all numpy (host) or all torch CUDA tensors (device)."""
         p, stride, mem_in, _keep = _image(tar, self.params.img_width, self.params.img_height)

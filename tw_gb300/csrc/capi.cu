@@ -792,7 +792,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     FftccTune best_f = fft0;
     float best_fms = 1e30f;
     if (e.prm.path == TWDIC_PATH_FAST && fftcc_tc_supported(e.g)) {
-        for (int groups : {0, 1}) {
+        for (int groups : {0, 2, 1}) {
             for (int ppg : {0, 2, 1}) {
                 FftccTune c;
                 c.use_tc = 1;

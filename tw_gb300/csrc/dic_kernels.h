@@ -53,7 +53,7 @@ struct IcgnJobs {
 // Launch shape of the tensor-core FFT-CC kernel.
 struct FftccTune {
     int use_tc = 1;          // 0: FP32 SIMT DFT kernel
-    int groups = 0;          // tensor-core kernel: 0 = as many 128-thread groups per CTA as fit, 1 = one
+    int groups = 0;          // tensor-core kernel: 128-thread groups per CTA (0 = as many as fit, up to 4)
     int pois_per_group = 0;  // POIs per group batch (0 = the most the tiles hold)
 };
 

@@ -43,7 +43,8 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kMaxCand = 16;      // exact re-evaluations per POI
-constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
+constexpr int kMaxPB = 8;
+constexpr int kMaxGroups = 4;         // POIs per batch (upper bound)
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
@@ -139,15 +140,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     return false;
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
 #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
@@ -211,25 +210,27 @@ __device__ unsigned long long g_tc_trace[16];
 #endif
 
 // ----------------------------------------------------------------- kernel --
-// blockDim = 128 * s.groups.  Each 128-thread group runs its own batches
-// (own operand buffers, TMEM columns, mbarriers and named barrier) and the
-// groups share the twiddle tables, so one group's load and MMA latency
-// overlaps another's epilogues.
+// blockDim = 128 * s.groups (up to four).  Each 128-thread group runs its
+// own batches (own operand region, TMEM columns, mbarriers and named barrier)
+// and the groups share the twiddle tables, so one group's load and MMA
+// latency overlaps other groups' epilogues.  A group's GEMM operands A1, A2,
+// A3, A4 and its peak scratch share one region: each is written only after
+// the MMA that reads the previous one has completed.
 template <int NP, int HP, bool MULTI>
-__global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
-                                                     const uint4* __restrict__ tables, unsigned* err) {
+__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
+                                                                 const uint4* __restrict__ tables, unsigned* err) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ __align__(8) uint64_t mbar_mma[2];
-    __shared__ __align__(8) uint64_t mbar_tma[2];
+    __shared__ __align__(8) uint64_t mbar_mma[kMaxGroups];
+    __shared__ __align__(8) uint64_t mbar_tma[kMaxGroups];
     __shared__ uint32_t tmem_slot;
-    __shared__ int wsum[2][2 * kMaxPB][2];
-    __shared__ float sscale[2][kMaxPB];
-    __shared__ int sdark[2][kMaxPB];
-    __shared__ int ncand[2][kMaxPB];
-    __shared__ uint32_t smaxv[2][kMaxPB];  // ordered value of the approximate peak
-    __shared__ int smaxi[2][kMaxPB];       // its first index
-    __shared__ int2 spoi[2][kMaxPB];
-    __shared__ int smis[2][2 * kMaxPB];
+    __shared__ int wsum[kMaxGroups][2 * kMaxPB][2];
+    __shared__ float sscale[kMaxGroups][kMaxPB];
+    __shared__ int sdark[kMaxGroups][kMaxPB];
+    __shared__ int ncand[kMaxGroups][kMaxPB];
+    __shared__ uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
+    __shared__ int smaxi[kMaxGroups][kMaxPB];       // its first index
+    __shared__ int2 spoi[kMaxGroups][kMaxPB];
+    __shared__ int smis[kMaxGroups][2 * kMaxPB];
 
     const int grp = threadIdx.x >> 7;
     const int t = threadIdx.x & 127, warp = t >> 5, lane = t & 31;
@@ -243,10 +244,11 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
     uint64_t* mbar = &mbar_mma[grp];
     uint64_t* tbar = &mbar_tma[grp];
 
-    // ---- set-up: TMEM (128 columns per group), mbarriers, tables, zeroed A2/A4
+    // ---- set-up: TMEM (128 columns per group), mbarriers, tables
+    const uint32_t tmem_cols = s.groups == 1 ? 128u : (s.groups == 2 ? 256u : 512u);
     if (threadIdx.x < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(kTmemCols * s.groups));
+                     "r"(tmem_cols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (threadIdx.x == 0) {
@@ -262,8 +264,6 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
     {
         uint4* dst = reinterpret_cast<uint4*>(sm);
         for (int i = threadIdx.x; i < s.tab_bytes / 16; i += blockDim.x) dst[i] = tables[i];
-        uint4* a2 = reinterpret_cast<uint4*>(gbase + s.off_a2);
-        for (int i = t; i < (s.off_win - s.off_a2) / 16; i += 128) a2[i] = make_uint4(0, 0, 0, 0);
     }
     fence_async_smem();
     tc_fence_before();
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
         if (threadIdx.x < 32)
             asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
-                         "r"(kTmemCols * s.groups));
+                         "r"(tmem_cols));
         return;
     }
     const uint32_t tm = tmem_slot + grp * kTmemCols;
@@ -396,30 +396,47 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         tc_fence_after();
         TC_MARK(2);
 
-        // ---- epilogue 1: Y -> A2 (rows (p, ky, w), K = (part, x)), FP16
+        // ---- epilogue 1: Y -> A2 (rows (p, ky, w), K = (part, x)), FP16.  A2
+        // overwrites A1 (the region is shared), so the K padding x in [N, NP)
+        // of the data rows is zeroed first, then the data is written
+        {
+            const int c0 = N >> 3, nc = NP / 8 - c0;  // 8-column chunks holding padding
+            const int rows = 2 * PB * H;
+            for (int i = t; i < rows * 2 * nc; i += 128) {
+                const int r2 = i / (2 * nc), rem = i - r2 * (2 * nc);
+                const int part = rem / nc, c = c0 + rem - part * nc;
+                *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, part * NP + 8 * c, 2 * NP)) =
+                    make_uint4(0, 0, 0, 0);
+            }
+            group_sync(bar_id);
+        }
         for (int tile = 0; tile < s.tiles1; ++tile) {
-            float d[2 * HP];
-#pragma unroll
-            for (int c = 0; c < 2 * HP; c += 16) tmem_ld16(tm_warp + tile * 2 * HP + c, d + c);
-            tmem_ld_wait();
             const int rr = tile * 128 + t;
             const int wi = rr / N, x = rr - wi * N;
-            if (wi < 2 * PB) {
-                const int p = wi >> 1, wsel = wi & 1;
-                // rows r2 = (p H + ky) 2 + wsel step by 2: +32 B inside an 8-row
-                // group, +SBO - 96 B when the step crosses into the next group
-                int r2 = (p * H) * 2 + wsel;
-                uint8_t* rowp = gbase + s.off_a2 + kmaj144(r2, 0, 2 * NP);
-                const int kre = (x >> 3) * 144 + (x & 7) * 2;
-                const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
-                const int sbo = 36 * NP;
+            const bool data = wi < 2 * PB;
+            const int p = wi >> 1, wsel = wi & 1;
+            // rows r2 = (p H + ky) 2 + wsel step by 2: +32 B inside an 8-row
+            // group, +SBO - 96 B when the step crosses into the next group
+            int r2 = (p * H) * 2 + wsel;
+            uint8_t* rowp = gbase + s.off_a2 + kmaj144(data ? r2 : 0, 0, 2 * NP);
+            const int kre = (x >> 3) * 144 + (x & 7) * 2;
+            const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
+            const int sbo = 36 * NP;
 #pragma unroll
-                for (int ky = 0; ky < HP; ++ky) {
-                    if (ky < H) {
-                        st_half(rowp + kre, d[ky]);
-                        st_half(rowp + kim, d[HP + ky]);
-                        r2 += 2;
-                        rowp += ((r2 & 7) < 2) ? (sbo - 96) : 32;
+            for (int ky0 = 0; ky0 < HP; ky0 += 8) {
+                float dre[8], dim[8];
+                tmem_ld8(tm_warp + tile * 2 * HP + ky0, dre);
+                tmem_ld8(tm_warp + tile * 2 * HP + HP + ky0, dim);
+                tmem_ld_wait();
+                if (data) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (ky0 + j < H) {
+                            st_half(rowp + kre, dre[j]);
+                            st_half(rowp + kim, dim[j]);
+                            r2 += 2;
+                            rowp += ((r2 & 7) < 2) ? (sbo - 96) : 32;
+                        }
                     }
                 }
             }
@@ -459,13 +476,6 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
 
         // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
         {
-            float re[NP], im[NP];
-#pragma unroll
-            for (int c = 0; c < NP; c += 16) {
-                tmem_ld16(tm_warp + c, re + c);
-                tmem_ld16(tm_warp + NP + c, im + c);
-            }
-            tmem_ld_wait();
             const bool rowv = t < 2 * PB * H;
             const int p = rowv ? t / (2 * H) : 0;
             const int ky = rowv ? (t >> 1) % H : 0;
@@ -474,25 +484,35 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
             const int r3 = p * H + ky;
             uint8_t* a3 = gbase + s.off_a13;
             constexpr int HALF = NP / 2;
-            float br[8], bi[8];
 #pragma unroll
-            for (int i = 0; i < HALF; ++i) {
-                const float own_r = wsel ? re[HALF + i] : re[i];
-                const float own_i = wsel ? im[HALF + i] : im[i];
-                const float snd_r = wsel ? re[i] : re[HALF + i];
-                const float snd_i = wsel ? im[i] : im[HALF + i];
-                const float oth_r = __shfl_xor_sync(kFull, snd_r, 1);
-                const float oth_i = __shfl_xor_sync(kFull, snd_i, 1);
-                const float fr = wsel ? oth_r : own_r, fi = wsel ? oth_i : own_i;
-                const float gr = wsel ? own_r : oth_r, gi = wsel ? own_i : oth_i;
-                const int kx = wsel ? HALF + i : i;
-                float cr = (fr * gr + fi * gi) * sc;
-                float ci = (fr * gi - fi * gr) * sc;
-                if (kx >= N || (ky == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
-                br[i & 7] = cr;
-                bi[i & 7] = -ci;  // conj(C) feeds the forward matrices of stage 3
-                if ((i & 7) == 7 && rowv) {
-                    const int k0 = kx - 7;
+            for (int c = 0; c < HALF; c += 8) {
+                // columns [c, c+8) and [HALF+c, HALF+c+8) of Re and Im
+                float re_lo[8], re_hi[8], im_lo[8], im_hi[8];
+                tmem_ld8(tm_warp + c, re_lo);
+                tmem_ld8(tm_warp + HALF + c, re_hi);
+                tmem_ld8(tm_warp + NP + c, im_lo);
+                tmem_ld8(tm_warp + NP + HALF + c, im_hi);
+                tmem_ld_wait();
+                float br[8], bi[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const float own_r = wsel ? re_hi[i] : re_lo[i];
+                    const float own_i = wsel ? im_hi[i] : im_lo[i];
+                    const float snd_r = wsel ? re_lo[i] : re_hi[i];
+                    const float snd_i = wsel ? im_lo[i] : im_hi[i];
+                    const float oth_r = __shfl_xor_sync(kFull, snd_r, 1);
+                    const float oth_i = __shfl_xor_sync(kFull, snd_i, 1);
+                    const float fr = wsel ? oth_r : own_r, fi = wsel ? oth_i : own_i;
+                    const float gr = wsel ? own_r : oth_r, gi = wsel ? own_i : oth_i;
+                    const int kx = (wsel ? HALF : 0) + c + i;
+                    float cr = (fr * gr + fi * gi) * sc;
+                    float ci = (fr * gi - fi * gr) * sc;
+                    if (kx >= N || (ky == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
+                    br[i] = cr;
+                    bi[i] = -ci;  // conj(C) feeds the forward matrices of stage 3
+                }
+                if (rowv) {
+                    const int k0 = (wsel ? HALF : 0) + c;
                     uint4 q;
                     q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
                     q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
@@ -502,7 +522,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
                     *reinterpret_cast<uint4*>(a3 + kmaj(r3, NP + k0, 2 * NP)) = q;
                 }
             }
-            // rows of A3 past the data are zero (A3 shares memory with A1)
+            // rows of A3 past the data are zero (A3 shares memory with A1, A2)
             if (t >= PB * H) {
                 for (int k0 = 0; k0 < 2 * NP; k0 += 8)
                     *reinterpret_cast<uint4*>(a3 + kmaj(t, k0, 2 * NP)) = make_uint4(0, 0, 0, 0);
@@ -541,32 +561,44 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         tc_fence_after();
         TC_MARK(6);
 
-        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (part, ky)), c2r weights folded in
+        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (part, ky)), c2r weights
+        // folded in.  A4 overwrites A3 (stage 3 has completed), so the K
+        // padding ky in [H, HP) of the data rows is zeroed first
         {
-            float re[NP], im[NP];
-#pragma unroll
-            for (int c = 0; c < NP; c += 16) {
-                tmem_ld16(tm_warp + c, re + c);
-                tmem_ld16(tm_warp + NP + c, im + c);
+            const int c0 = H >> 3, nc = HP / 8 - c0;
+            const int rows = PB * N;
+            for (int i = t; i < rows * 2 * nc; i += 128) {
+                const int r4 = i / (2 * nc), rem = i - r4 * (2 * nc);
+                const int part = rem / nc, c = c0 + rem - part * nc;
+                *reinterpret_cast<uint4*>(gbase + s.off_a4 + kmaj(r4, part * HP + 8 * c, K4)) =
+                    make_uint4(0, 0, 0, 0);
             }
-            tmem_ld_wait();
-            if (t < PB * H) {
-                const int p = t / H, ky = t - (t / H) * H;
-                const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
-                // rows r4 = p N + x step by 1: +16 B inside an 8-row group,
-                // +SBO - 112 B when the step crosses into the next group
-                int r4 = p * N;
-                uint8_t* rowp = gbase + s.off_a4 + kmaj(r4, 0, K4);
-                const int kre = (ky >> 3) * 128 + (ky & 7) * 2;
-                const int kim = ((HP + ky) >> 3) * 128 + ((HP + ky) & 7) * 2;
-                const int sbo = 16 * K4;
+            group_sync(bar_id);
+            const bool rowv = t < PB * H;
+            const int p = rowv ? t / H : 0, ky = rowv ? t - (t / H) * H : 0;
+            const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
+            // rows r4 = p N + x step by 1: +16 B inside an 8-row group,
+            // +SBO - 112 B when the step crosses into the next group
+            int r4 = p * N;
+            uint8_t* rowp = gbase + s.off_a4 + kmaj(r4, 0, K4);
+            const int kre = (ky >> 3) * 128 + (ky & 7) * 2;
+            const int kim = ((HP + ky) >> 3) * 128 + ((HP + ky) & 7) * 2;
+            const int sbo = 16 * K4;
 #pragma unroll
-                for (int x = 0; x < NP; ++x) {
-                    if (x < N) {
-                        st_half(rowp + kre, wgt * re[x]);
-                        st_half(rowp + kim, -wgt * im[x]);  // Zi = -D_i
-                        ++r4;
-                        rowp += ((r4 & 7) == 0) ? (sbo - 112) : 16;
+            for (int x0 = 0; x0 < NP; x0 += 8) {
+                float re[8], im[8];
+                tmem_ld8(tm_warp + x0, re);
+                tmem_ld8(tm_warp + NP + x0, im);
+                tmem_ld_wait();
+                if (rowv) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (x0 + j < N) {
+                            st_half(rowp + kre, wgt * re[j]);
+                            st_half(rowp + kim, -wgt * im[j]);  // Zi = -D_i
+                            ++r4;
+                            rowp += ((r4 & 7) == 0) ? (sbo - 112) : 16;
+                        }
                     }
                 }
             }
@@ -595,12 +627,8 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         TC_MARK(8);
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
-        // (scratch in the A1/A3 region, which stage 3 has finished reading)
-        float cv[NP];
-#pragma unroll
-        for (int c = 0; c < NP; c += 16) tmem_ld16(tm_warp + c, cv + c);
-        tmem_ld_wait();
-        tc_fence_before();
+        // (scratch in the shared operand region, which stage 4 has finished
+        // reading; the surface stays in TMEM and is read twice in chunks)
         const bool rowv = t < PB * N;
         const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
         const bool live = rowv && !sdark[grp][p4];
@@ -610,10 +638,14 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         // by a segmented warp reduction and one shared atomic per warp segment
         float bv = -3.4e38f;
         int bi = 0x7fffffff;
-        if (live) {
 #pragma unroll
-            for (int y = 0; y < NP; ++y)
-                if (y < N && cv[y] > bv) { bv = cv[y]; bi = y * N + x4; }
+        for (int y0 = 0; y0 < NP; y0 += 8) {
+            float cv[8];
+            tmem_ld8(tm_warp + y0, cv);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (live && y0 + j < N && cv[j] > bv) { bv = cv[j]; bi = (y0 + j) * N + x4; }
         }
         const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
         const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
@@ -625,21 +657,28 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
         group_sync(bar_id);
         // candidates: every shift within 2% of N^2 (scaled units) of the
         // approximate peak; slot 0 holds the approximate argmax
-        if (live) {
+        {
             const float th = f32_unord(pv) - 0.02f * (float)n2;
-            const int first = smaxi[grp][p4];
-            if (x4 == 0) ps->cand[p4][0] = first;
+            const int first = live ? smaxi[grp][p4] : -1;
+            if (live && x4 == 0) ps->cand[p4][0] = first;
 #pragma unroll
-            for (int y = 0; y < NP; ++y) {
-                if (y < N && cv[y] >= th) {
-                    const int idx = y * N + x4;
-                    if (idx != first) {
-                        const int slot = atomicAdd(&ncand[grp][p4], 1);
-                        if (slot < kMaxCand) ps->cand[p4][slot] = idx;
+            for (int y0 = 0; y0 < NP; y0 += 8) {
+                float cv[8];
+                tmem_ld8(tm_warp + y0, cv);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    if (live && y0 + j < N && cv[j] >= th) {
+                        const int idx = (y0 + j) * N + x4;
+                        if (idx != first) {
+                            const int slot = atomicAdd(&ncand[grp][p4], 1);
+                            if (slot < kMaxCand) ps->cand[p4][slot] = idx;
+                        }
                     }
                 }
             }
         }
+        tc_fence_before();
         group_sync(bar_id);
         TC_MARK(9);
         // exact integer correlation of every candidate, read from the staged
@@ -731,7 +770,7 @@ __global__ void __launch_bounds__(256, 1) k_fftcc_tc(const __grid_constant__ TcJ
     tc_fence_after();
     if (threadIdx.x < 32)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
-                     "r"(kTmemCols * s.groups));
+                     "r"(tmem_cols));
 }
 
 // ----------------------------------------------------------- host side ----
@@ -769,22 +808,25 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     s.off_b4l = o; o += NP * K4 * 2;
     s.tab_bytes = round_up(o, 1024);
     o = s.tab_bytes;
-    // per-group regions
+    // per-group regions: one operand region shared by A1, A2, A3, A4 and the
+    // peak scratch, then the windows
     s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
-    int q = 0;
     s.NW4 = (N + 3) / 4;
-    s.off_a13 = q;
-    q += std::max(std::max(s.tiles1 * 128 * K1 * 2, 128 * 2 * NP * 2), (int)sizeof(PeakScratch));
-    s.off_a2 = q; q += 16 * 36 * NP;
-    s.off_a4 = q; q += 16 * 16 * K4;
+    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 16 * K4;
+    const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
+                                128);
+    s.off_a13 = 0;
+    s.off_a2 = 0;
+    s.off_a4 = 0;
     // window stride: TMA destinations are 128-byte aligned, and 16 spare bytes
-    // keep the 8-byte reads of ld_unaligned inside the window
+    // keep the 8-byte reads of ld_unaligned_p inside the window
     s.WS = round_up(N * s.BW + 16, 128);
-    s.off_win = q; q += 2 * pb * s.WS;
-    s.group_bytes = round_up(q, 1024);
+    s.off_win = region;
+    s.group_bytes = round_up(region + 2 * pb * s.WS, 1024);
     const int limit = 225 * 1024;
-    s.groups = (o + 2 * s.group_bytes <= limit) ? 2 : 1;
-    if (tune.groups == 1) s.groups = 1;  // tuned: one group per CTA (two CTAs per SM when they fit)
+    s.groups = std::min(kMaxGroups, (limit - o) / s.group_bytes);
+    if (tune.groups > 0) s.groups = std::min(s.groups, tune.groups);  // tuned group count
+    if (s.groups < 1) return false;
     s.smem_bytes = o + s.groups * s.group_bytes;
     return s.smem_bytes <= limit;
 }

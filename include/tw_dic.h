@@ -179,7 +179,7 @@ TWDIC_API int twdic_frame_phase_times(const twdic_frame* h, float* t6);
 TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 
 /* Launch-shape tuning of a frame handle (no counterpart in the reference;
- * set by the autotuner).  icgn_threads: 64, 128 or 256 threads per IC-GN CTA;
+ * set by the autotuner).  icgn_threads: 32, 64, 128 or 256 threads per IC-GN CTA;
  * icgn_ctas_per_sm: persistent CTAs per SM (0 = occupancy limit);
  * icgn_sampler: target interpolation of the fast IC-GN, 0 = staged window,
  * 1 = per-frame bicubic coefficient LUT, 2 = per-frame 4x4 neighbourhood

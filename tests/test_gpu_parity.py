@@ -88,7 +88,7 @@ def test_frame_parity(request, case, path):
         np.testing.assert_array_equal(out[k], out2[k])
 
 
-@pytest.mark.parametrize("threads", [64, 128, 256])
+@pytest.mark.parametrize("threads", [32, 64, 128, 256])
 @pytest.mark.parametrize("sampler", [SAMPLER_WINDOW, SAMPLER_LUT, SAMPLER_NBHD])
 def test_fast_icgn_samplers(plain512, sampler, threads):
     """Every launch shape and target sampler of the fast IC-GN meets the

@@ -169,10 +169,10 @@ struct Engine {
 
     int init(const twdic_params& p, int num_pois) {
         prm = p;
-        // fastest measured IC-GN shape on GB300 at 41x41 subsets: 64 threads
+        // fastest measured IC-GN shape on GB300 at 41x41 subsets: one warp
         // per POI gathering the per-frame 4x4 neighbourhood table (16 B per
         // ROI pixel; the autotuner may change it)
-        icgn_tune.threads = 64;
+        icgn_tune.threads = 32;
         icgn_tune.sampler = kSampNbhd;
         g = make_geom(p);
         n = num_pois;
@@ -663,8 +663,8 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
 int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                            int fftcc_use_tc) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
-        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 64, 128 or 256");
+    if (icgn_threads != 32 && icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
     h->e.icgn_tune.threads = icgn_threads;
     h->e.icgn_tune.ctas_per_sm = icgn_ctas_per_sm;
     if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
@@ -818,7 +818,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     IcgnTune best_i = icgn0;
     float best_ims = 1e30f, fms = best_fms;
     if (e.prm.path == TWDIC_PATH_FAST) {
-        for (int threads : {64, 128, 256}) {
+        for (int threads : {32, 64, 128, 256}) {
             for (int sampler : {kSampNbhd, kSampLut, kSampWindow}) {
                 IcgnTune c;
                 c.threads = threads;
@@ -1047,7 +1047,7 @@ int twdic_batch_create(twdic_batch** out) {
     TW_TRY(b->d_work.ensure(sizeof(int) * 4));
     TW_TRY(b->d_err.ensure(sizeof(unsigned)));
     TW_CUDA(cudaMemset(b->d_err.p, 0, sizeof(unsigned)));
-    b->tune.threads = 64;
+    b->tune.threads = 32;
     b->tune.sampler = kSampNbhd;
     *out = b.release();
     return TWDIC_OK;
@@ -1062,8 +1062,8 @@ int twdic_batch_set_stream(twdic_batch* b, void* stream) {
 
 int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler) {
     if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
-        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 64, 128 or 256");
+    if (icgn_threads != 32 && icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
     if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
         return fail(TWDIC_ERR_INVALID_ARG, "sampler must be 0, 1 or 2");
     b->tune.threads = icgn_threads;

@@ -17,7 +17,7 @@ enum IcgnSampler {
 
 // Launch shape of the fast IC-GN kernel, chosen by the autotuner.
 struct IcgnTune {
-    int threads = 128;    // 64, 128 or 256 threads per CTA (one POI per CTA at a time)
+    int threads = 128;    // 32, 64, 128 or 256 threads per CTA (one POI per CTA at a time)
     int ctas_per_sm = 0;  // persistent CTAs per SM (0 = occupancy limit)
     int sampler = kSampWindow;  // needs no per-frame table
 };

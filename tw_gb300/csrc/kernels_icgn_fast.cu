@@ -580,6 +580,7 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
     if (tune.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                              \
     if (tune.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                            \
     TWDIC_ICGN_FAST(TH, kSampWindow)
+    if (tune.threads == 32) { TWDIC_ICGN_FAST_T(32); }
     if (tune.threads == 64) { TWDIC_ICGN_FAST_T(64); }
     if (tune.threads == 256) { TWDIC_ICGN_FAST_T(256); }
     TWDIC_ICGN_FAST_T(128);

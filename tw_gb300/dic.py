@@ -345,7 +345,7 @@ class DICBatch:
         ptr = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
         check(self._lib.twdic_batch_set_stream(self._h, ptr))
 
-    def set_tuning(self, icgn_threads=64, icgn_ctas_per_sm=0, icgn_sampler=2):
+    def set_tuning(self, icgn_threads=32, icgn_ctas_per_sm=0, icgn_sampler=2):
         check(self._lib.twdic_batch_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler))
 
     def process(self, frames, tars, outs):

@@ -192,6 +192,34 @@ __global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __r
     table[(size_t)i * g.rw + j] = q;
 }
 
+// Catmull-Rom interpolation along one row of four pixels v0..v3 (bytes of
+// w, v0 lowest) at fraction t, times two:
+//   2 h(t) = e0 + t (e1 + t (e2 + t e3)),
+//   e0 = 2 v1, e1 = v2 - v0, e2 = 2 v0 - 5 v1 + 4 v2 - v3, e3 = -v0 + 3 v1 - 3 v2 + v3,
+// the integer coefficients by one DP4A each (unsigned pixel bytes times signed
+// weight bytes), exact; then Horner in FP32.
+__device__ __forceinline__ int dp4a_us(uint32_t a, uint32_t b) {
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(0));
+    return d;
+}
+__device__ __forceinline__ float cr_row2(uint32_t w, float t) {
+    const float e0 = (float)(int)(((w >> 8) & 0xffu) << 1);
+    const float e1 = (float)dp4a_us(w, 0x000100FFu);  // (-1, 0, 1, 0)
+    const float e2 = (float)dp4a_us(w, 0xFF04FB02u);  // (2, -5, 4, -1)
+    const float e3 = (float)dp4a_us(w, 0x01FD03FFu);  // (-1, 3, -3, 1)
+    return fmaf(fmaf(fmaf(e3, t, e2), t, e1), t, e0);
+}
+// Catmull-Rom combination in fraction t of four row values given times two
+// (H_a = 2 h_a): the interpolated value.
+__device__ __forceinline__ float cr_combine4(const float* H, float t) {
+    const float f1 = H[2] - H[0];
+    const float f2 = fmaf(2.f, H[0], fmaf(-5.f, H[1], fmaf(4.f, H[2], -H[3])));
+    const float f3 = fmaf(3.f, H[1] - H[2], H[3] - H[0]);
+    const float f0 = 2.f * H[1];
+    return 0.25f * fmaf(fmaf(fmaf(f3, t, f2), t, f1), t, f0);
+}
+
 // Catmull-Rom weights (the Hermite bicubic with central differences).
 __device__ __forceinline__ void cr_weights(float t, float& w0, float& w1, float& w2, float& w3) {
     const float t2 = t * t;
@@ -385,16 +413,11 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                             // 4x4 pixels around (ix, iy), row-major bytes; zero on the
                             // ROI's last row and column, as the reference LUT is there
                             const uint4 q = nb0[(size_t)iy * g.rw + ix];
-                            float cx0, cx1, cx2, cx3, cy0, cy1, cy2, cy3;
-                            cr_weights(fx, cx0, cx1, cx2, cx3);
-                            cr_weights(fy, cy0, cy1, cy2, cy3);
                             const uint32_t wr[4] = {q.x, q.y, q.z, q.w};
-                            float rr[4];
+                            float hr[4];
 #pragma unroll
-                            for (int a = 0; a < 4; ++a)
-                                rr[a] = cx0 * (float)(wr[a] & 0xffu) + cx1 * (float)((wr[a] >> 8) & 0xffu) +
-                                        cx2 * (float)((wr[a] >> 16) & 0xffu) + cx3 * (float)(wr[a] >> 24);
-                            t = cy0 * rr[0] + cy1 * rr[1] + cy2 * rr[2] + cy3 * rr[3];
+                            for (int a = 0; a < 4; ++a) hr[a] = cr_row2(wr[a], fx);
+                            t = cr_combine4(hr, fy);
                         } else if (SAMPLER == kSampLut) {
                             const float4* q = lut0 + ((size_t)iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];

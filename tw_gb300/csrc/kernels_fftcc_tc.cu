@@ -43,8 +43,14 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kMaxCand = 16;      // exact re-evaluations per POI
-constexpr int kMaxPB = 8;
-constexpr int kMaxGroups = 4;         // POIs per batch (upper bound)
+constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
+constexpr int kMaxGroups = 4;     // 128-thread groups per CTA (upper bound)
+// Candidate window of the approximate correlation surface, in ZNCC units.
+// The exact peak lies within twice the surface's error of the approximate
+// maximum; the largest error measured at any evaluated candidate on the
+// 2048x2048 / r = 20 workload (155,236 POIs) is 4.7e-4 (FP16 operands,
+// FP32 accumulation), so 0.01 keeps a tenfold margin.
+constexpr float kCandZncc = 0.01f;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
@@ -82,6 +88,7 @@ struct TcJobs {
 
 struct PeakScratch {
     int cand[kMaxPB][kMaxCand];
+    float candV[kMaxPB][kMaxCand];  // approximate surface value of each candidate
     int candS[kMaxPB][kMaxCand];
 };
 
@@ -655,12 +662,15 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         const uint32_t mi = __reduce_min_sync(seg, (live && f32_ord(bv) == pv) ? (uint32_t)bi : 0xffffffffu);
         if (live && lane == __ffs(seg) - 1 && mi != 0xffffffffu) atomicMin(&smaxi[grp][p4], (int)mi);
         group_sync(bar_id);
-        // candidates: every shift within 2% of N^2 (scaled units) of the
-        // approximate peak; slot 0 holds the approximate argmax
+        // candidates: every shift within kCandZncc (ZNCC units; the surface is
+        // N^2 ZNCC) of the approximate peak; slot 0 holds the approximate argmax
         {
-            const float th = f32_unord(pv) - 0.02f * (float)n2;
+            const float th = f32_unord(pv) - kCandZncc * (float)n2;
             const int first = live ? smaxi[grp][p4] : -1;
-            if (live && x4 == 0) ps->cand[p4][0] = first;
+            if (live && x4 == 0) {
+                ps->cand[p4][0] = first;
+                ps->candV[p4][0] = f32_unord(pv);
+            }
 #pragma unroll
             for (int y0 = 0; y0 < NP; y0 += 8) {
                 float cv[8];
@@ -672,7 +682,10 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                         const int idx = (y0 + j) * N + x4;
                         if (idx != first) {
                             const int slot = atomicAdd(&ncand[grp][p4], 1);
-                            if (slot < kMaxCand) ps->cand[p4][slot] = idx;
+                            if (slot < kMaxCand) {
+                                ps->cand[p4][slot] = idx;
+                                ps->candV[p4][slot] = cv[j];
+                            }
                         }
                     }
                 }
@@ -757,6 +770,15 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 u[gp] = (float)iu;
                 v[gp] = (float)iv;
                 zncc[gp] = (float)(cnum / sqrt((double)numf * (double)numg));
+#ifdef TWDIC_TC_TRACE
+                // largest error of the approximate surface at the candidates, ZNCC units x 1e6
+                for (int c = 0; c < nc; ++c) {
+                    const double zk = (double)((long long)n2 * ps->candS[t][c] - sf * sg) /
+                                      sqrt((double)numf * (double)numg);
+                    const double e = fabs((double)ps->candV[t][c] / n2 - zk);
+                    atomicMax(&g_tc_trace[14], (unsigned long long)(e * 1e6));
+                }
+#endif
                 status[gp] = 0;
             }
         }

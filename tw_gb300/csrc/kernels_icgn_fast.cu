@@ -204,7 +204,7 @@ __device__ __forceinline__ int dp4a_us(uint32_t a, uint32_t b) {
     return d;
 }
 __device__ __forceinline__ float cr_row2(uint32_t w, float t) {
-    const float e0 = (float)(int)(((w >> 8) & 0xffu) << 1);
+    const float e0 = (float)dp4a_us(w, 0x00000200u);  // (0, 2, 0, 0)
     const float e1 = (float)dp4a_us(w, 0x000100FFu);  // (-1, 0, 1, 0)
     const float e2 = (float)dp4a_us(w, 0xFF04FB02u);  // (2, -5, 4, -1)
     const float e3 = (float)dp4a_us(w, 0x01FD03FFu);  // (-1, 3, -3, 1)

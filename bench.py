@@ -358,9 +358,9 @@ def _run_gpu(args, world, rank, local, torch):
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
 # profiles/k_icgn_fast_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
-NCU_TRAFFIC = {"k_icgn_fast": 305.42e6 + 8.52e6, "k_fftcc_tc": 9.60e6 + 0.0}
-# L2 -> SM bandwidth implied by that IC-GN capture (53.78 GB in 4.119 ms at
-# 53.6 % of the L2 throughput peak); there is no measured L2 peak
+NCU_TRAFFIC = {"k_icgn_fast": 111.91e6 + 5.94e6, "k_fftcc_tc": 9.65e6 + 0.0}
+# L2 -> SM bandwidth implied by an ncu capture of the float-LUT IC-GN sampler (53.78 GB in
+# 4.119 ms at 53.6 % of the L2 throughput peak); there is no measured L2 peak
 L2_PEAK_GBS_NCU = 53.78e9 / 4.119e-3 / 0.536 / 1e9
 
 

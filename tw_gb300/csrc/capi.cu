@@ -997,12 +997,20 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         else
             TW_TRY(e.prepare_target());
     }
-    for (size_t k0 = 0; k0 < fast_ic.size(); k0 += kMaxJobs) {
+    // one launch per residency level (and per kMaxJobs frames): a launch sizes
+    // shared memory for its largest subset, so frames whose subsets allow
+    // more resident CTAs are not launched with larger ones
+    std::vector<std::pair<int, int>> order;  // (residency, frame index)
+    for (int i : fast_ic) order.emplace_back(icgn_fast_residency(a.frames[i]->e.g, b->tune), i);
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first > y.first; });
+    for (size_t k0 = 0; k0 < order.size();) {
         IcgnJobs J;
         J.njobs = 0;
         J.total = 0;
-        for (size_t k = k0; k < fast_ic.size() && k < k0 + kMaxJobs; ++k) {
-            const int i = fast_ic[k];
+        size_t k = k0;
+        for (; k < order.size() && J.njobs < kMaxJobs && order[k].first == order[k0].first; ++k) {
+            const int i = order[k].second;
             Engine& e = a.frames[i]->e;
             const FrameOut o = frame_out(e, a, i);
             IcgnJob& jb = J.job[J.njobs++];
@@ -1023,6 +1031,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             jb.begin = J.total;
             J.total += e.n;
         }
+        k0 = k;
         TW_CUDA(launch_icgn_fast_jobs(J, b->d_work.as<int>(), b->tune, b->stream));
     }
     for (int i = 0; i < count; ++i) {

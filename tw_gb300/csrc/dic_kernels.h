@@ -82,6 +82,11 @@ cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* t
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
                              const IcgnTune& tune, cudaStream_t st);
 int icgn_fast_window(const Geom& g);
+// CTAs per SM the fast IC-GN kernel can keep resident for this geometry and
+// launch shape (shared memory, registers, the 32-CTA limit): jobs batched
+// into one launch should share it, since the launch sizes shared memory for
+// its largest subset
+int icgn_fast_residency(const Geom& g, const IcgnTune& tune);
 // all jobs of the table in one persistent launch
 cudaError_t launch_icgn_fast_jobs(const IcgnJobs& jobs, int* work, const IcgnTune& tune, cudaStream_t st);
 

@@ -590,6 +590,15 @@ static cudaError_t launch_icgn_fast_t(const IcgnJobs& J, int* work, int ctas_per
     return cudaGetLastError();
 }
 
+int icgn_fast_residency(const Geom& g, const IcgnTune& tune) {
+    const int S = (2 * g.rx + 1) * (2 * g.ry + 1), ws = icgn_fast_window(g);
+    const size_t smem = sizeof(float) * ((size_t)((S + 3) & ~3) + (tune.sampler == kSampWindow ? (size_t)ws * ws : 0));
+    const int threads = tune.threads == 32 || tune.threads == 64 || tune.threads == 256 ? tune.threads : 128;
+    const int by_regs = 65536 / (64 * threads);            // the kernels' 64-register budget
+    const int by_smem = (int)((228u * 1024u) / (smem + 1024u));  // 1 KB per CTA reserved by the runtime
+    return std::max(1, std::min(std::min(32, by_regs), by_smem));
+}
+
 cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& tune, cudaStream_t st) {
     if (J.njobs < 1 || J.njobs > kMaxJobs) return cudaErrorInvalidValue;
     if (J.total <= 0) return cudaSuccess;

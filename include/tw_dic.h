@@ -317,6 +317,38 @@ TWDIC_API int twdic_server_resume(twdic_server* s);
 TWDIC_API int twdic_server_stats(twdic_server* s, twdic_server_counters* out);
 TWDIC_API int twdic_server_destroy(twdic_server* s);
 
+/* ---- tracking loop (FFTCCTWorkerThread::processFrameFFTCC /
+ * processFrameFFTCC_ICGN, TW/TW_Core/fftcctworkerthread.cpp:219-330, :399-481;
+ * TW/TW_Core/cuda_utils.cu:109-240) ----
+ * One camera's frame sequence.  Frame k (counted from 1) with
+ * (k - 1) % refresh_interval == 0 becomes the reference (the reference uses
+ * 50); at such a frame after the first, the last frame's displacements are
+ * added to the accumulated ones (cuAccumulateUV) and every POI moves by their
+ * truncation, y += int(v), x += int(u) (cuUpdatePOIpos), held so that its
+ * subset stays in the ROI.  Every frame runs FFT-CC, and IC-GN when
+ * with_icgn, at the current POIs against the current reference.
+ *   u, v        this frame's displacement at the current POIs (n floats each)
+ *   acc_u/v     accumulated displacement of the current POIs (total = acc + u)
+ *   poi_yx      current POI positions, (y, x) pairs
+ *   flags       IC-GN flags (FFT-CC status without IC-GN)
+ * Any output may be NULL. */
+typedef struct twdic_tracker twdic_tracker;
+TWDIC_API int twdic_tracker_create(const twdic_params* p, int32_t refresh_interval, int32_t with_icgn,
+                                   twdic_tracker** out);
+TWDIC_API int twdic_tracker_num_pois(const twdic_tracker* t, int32_t* n);
+TWDIC_API int twdic_tracker_process(twdic_tracker* t, const uint8_t* img, int32_t stride, int mem_in, float* u,
+                                    float* v, float* acc_u, float* acc_v, int32_t* poi_yx, uint8_t* flags,
+                                    int mem_out);
+/* constructTextImageFixedMinMax (TW/TW_Core/cuda_utils.cu:109-172) after the
+ * last process call: each POI is drawn at its displayed position (current
+ * POI + truncated displacement, cuAccumulatePOI) as a 3x3 block coloured by
+ * its total displacement clamped to [min, max], into two ROI-sized RGBA
+ * images (uint32, red in the lowest byte; a 256-entry jet map).  Pixels not
+ * drawn keep their contents; pixels outside the ROI are skipped. */
+TWDIC_API int twdic_tracker_colormap(twdic_tracker* t, uint32_t* tex_u, uint32_t* tex_v, float min_u, float max_u,
+                                     float min_v, float max_v, int mem);
+TWDIC_API int twdic_tracker_destroy(twdic_tracker* t);
+
 #ifdef __cplusplus
 }
 #endif

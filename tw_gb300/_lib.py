@@ -45,6 +45,8 @@ EXPORTED = (
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
     "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
     "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
+    "twdic_tracker_create", "twdic_tracker_num_pois", "twdic_tracker_process", "twdic_tracker_colormap",
+    "twdic_tracker_destroy",
 )
 
 
@@ -160,6 +162,12 @@ def load():
         "twdic_frame_set_fftcc_tuning": ([_VP, _I, _I, _I], _I),
         "twdic_frame_get_tuning": ([_VP, ctypes.POINTER(Tuning)], _I),
         "twdic_frame_autotune": ([_VP, _VP, ctypes.c_int32, _I, ctypes.c_char_p, ctypes.POINTER(Tuning)], _I),
+        "twdic_tracker_create": ([P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_VP)], _I),
+        "twdic_tracker_num_pois": ([_VP, _I32P], _I),
+        "twdic_tracker_process": ([_VP, _VP, ctypes.c_int32, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I], _I),
+        "twdic_tracker_colormap": ([_VP, _VP, _VP, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                    _I], _I),
+        "twdic_tracker_destroy": ([_VP], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

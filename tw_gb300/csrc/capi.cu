@@ -1197,3 +1197,124 @@ int twdic_batch_destroy(twdic_batch* b) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ tracking ----
+// The reference's per-camera loop (FFTCCTWorkerThread::processFrameFFTCC /
+// processFrameFFTCC_ICGN, TW/TW_Core/fftcctworkerthread.cpp:219-330,
+// :399-481): frame k (counted from 1) with (k - 1) % interval == 0 becomes the
+// reference; at such a frame after the first, the last frame's displacements
+// are accumulated and every POI moves by their truncation; every frame runs
+// FFT-CC (and IC-GN) at the current POIs against the current reference.
+struct twdic_tracker {
+    Engine e;
+    int interval = 50;
+    int with_icgn = 1;
+    int64_t frame = 0;
+    DevBuf d_acc_u, d_acc_v, d_last_u, d_last_v;
+};
+
+extern "C" {
+
+int twdic_tracker_create(const twdic_params* p, int32_t refresh_interval, int32_t with_icgn, twdic_tracker** out) {
+    if (!out) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle output");
+    *out = nullptr;
+    if (refresh_interval < 1) return fail(TWDIC_ERR_INVALID_ARG, "refresh_interval must be >= 1");
+    std::unique_ptr<twdic_tracker> t(new (std::nothrow) twdic_tracker);
+    if (!t) return fail(TWDIC_ERR_NO_MEMORY, "host allocation failed");
+    TW_TRY(engine_grid_init(t->e, p, true));
+    t->interval = refresh_interval;
+    t->with_icgn = with_icgn ? 1 : 0;
+    const size_t b = sizeof(float) * (size_t)t->e.n;
+    TW_TRY(t->d_acc_u.ensure(b));
+    TW_TRY(t->d_acc_v.ensure(b));
+    TW_TRY(t->d_last_u.ensure(b));
+    TW_TRY(t->d_last_v.ensure(b));
+    TW_CUDA(cudaMemsetAsync(t->d_acc_u.p, 0, b, t->e.stream));
+    TW_CUDA(cudaMemsetAsync(t->d_acc_v.p, 0, b, t->e.stream));
+    TW_CUDA(cudaStreamSynchronize(t->e.stream));
+    *out = t.release();
+    return TWDIC_OK;
+}
+
+int twdic_tracker_num_pois(const twdic_tracker* t, int32_t* n) {
+    if (!t || !n) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    *n = t->e.n;
+    return TWDIC_OK;
+}
+
+int twdic_tracker_process(twdic_tracker* t, const uint8_t* img, int32_t stride, int mem_in, float* u, float* v,
+                          float* acc_u, float* acc_v, int32_t* poi_yx, uint8_t* flags, int mem_out) {
+    if (!t || !img) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem_in));
+    TW_TRY(check_mem(mem_out));
+    Engine& e = t->e;
+    const size_t n = (size_t)e.n;
+    t->frame += 1;
+    if ((t->frame - 1) % t->interval == 0) {
+        if (t->frame > t->interval) {
+            const Geom& g = e.g;
+            TW_CUDA(launch_track_update(e.d_poi.as<int2>(), t->d_last_u.as<float>(), t->d_last_v.as<float>(),
+                                        t->d_acc_u.as<float>(), t->d_acc_v.as<float>(), e.n, g.sy + g.ry,
+                                        g.sy + g.rh - 1 - g.ry, g.sx + g.rx, g.sx + g.rw - 1 - g.rx, e.stream));
+        }
+        TW_TRY(e.set_ref(img, stride, mem_in));  // also drops the per-reference cache (the POIs moved)
+    }
+    TW_TRY(e.set_tar(img, stride, mem_in));
+    float* du = t->d_last_u.as<float>();
+    float* dv = t->d_last_v.as<float>();
+    TW_CUDA(cudaMemsetAsync(du, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(dv, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(e.d_zncc.p, 0, 4 * n, e.stream));
+    TW_CUDA(cudaMemsetAsync(e.d_iters.p, 0, 4 * n, e.stream));
+    TW_TRY(e.ensure_cache(nullptr));
+    TW_TRY(e.fftcc(du, dv, e.d_zncc.as<float>(), e.d_fst.as<uint8_t>()));
+    if (t->with_icgn) {
+        TW_TRY(e.icgn(du, dv, e.d_p6.as<float>(), e.d_iters.as<int>(), e.d_flags.as<uint8_t>()));
+    } else {
+        TW_CUDA(cudaMemsetAsync(e.d_flags.p, 0, n, e.stream));
+    }
+    TW_TRY(copy_out(u, du, 4 * n, mem_out, e.stream));
+    TW_TRY(copy_out(v, dv, 4 * n, mem_out, e.stream));
+    TW_TRY(copy_out(acc_u, t->d_acc_u.p, 4 * n, mem_out, e.stream));
+    TW_TRY(copy_out(acc_v, t->d_acc_v.p, 4 * n, mem_out, e.stream));
+    TW_TRY(copy_out(poi_yx, e.d_poi.p, 8 * n, mem_out, e.stream));
+    TW_TRY(copy_out(flags, t->with_icgn ? e.d_flags.p : e.d_fst.p, n, mem_out, e.stream));
+    if (mem_out == TWDIC_MEM_HOST) return e.check_err();
+    return TWDIC_OK;
+}
+
+int twdic_tracker_colormap(twdic_tracker* t, uint32_t* tex_u, uint32_t* tex_v, float min_u, float max_u,
+                           float min_v, float max_v, int mem) {
+    if (!t || !tex_u || !tex_v) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    TW_TRY(check_mem(mem));
+    if (!(max_u > min_u) || !(max_v > min_v)) return fail(TWDIC_ERR_INVALID_ARG, "colour range must be non-empty");
+    Engine& e = t->e;
+    const size_t px = (size_t)e.g.rw * e.g.rh;
+    uint32_t* du = tex_u;
+    uint32_t* dv = tex_v;
+    DevBuf tmp;
+    if (mem == TWDIC_MEM_HOST) {
+        // draw into device copies of the caller's images, then copy back
+        TW_TRY(tmp.ensure(8 * px));
+        du = tmp.as<uint32_t>();
+        dv = du + px;
+        TW_CUDA(cudaMemcpyAsync(du, tex_u, 4 * px, cudaMemcpyHostToDevice, e.stream));
+        TW_CUDA(cudaMemcpyAsync(dv, tex_v, 4 * px, cudaMemcpyHostToDevice, e.stream));
+    }
+    TW_CUDA(launch_colormap(du, dv, e.d_poi.as<int2>(), t->d_last_u.as<float>(), t->d_last_v.as<float>(),
+                            t->d_acc_u.as<float>(), t->d_acc_v.as<float>(), e.n, e.g, min_u, max_u, min_v, max_v,
+                            e.stream));
+    if (mem == TWDIC_MEM_HOST) {
+        TW_CUDA(cudaMemcpyAsync(tex_u, du, 4 * px, cudaMemcpyDeviceToHost, e.stream));
+        TW_CUDA(cudaMemcpyAsync(tex_v, dv, 4 * px, cudaMemcpyDeviceToHost, e.stream));
+        TW_CUDA(cudaStreamSynchronize(e.stream));
+    }
+    return TWDIC_OK;
+}
+
+int twdic_tracker_destroy(twdic_tracker* t) {
+    delete t;
+    return TWDIC_OK;
+}
+
+}  // extern "C"

@@ -110,4 +110,11 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
                                  cudaStream_t st);
 bool fftcc_tc_supported(const Geom& g);
 
+// ---- tracking loop (kernels_track.cu)
+cudaError_t launch_track_update(int2* poi, const float* u, const float* v, float* acc_u, float* acc_v, int n,
+                                int lo_y, int hi_y, int lo_x, int hi_x, cudaStream_t st);
+cudaError_t launch_colormap(uint32_t* tex_u, uint32_t* tex_v, const int2* poi, const float* u, const float* v,
+                            const float* acc_u, const float* acc_v, int n, const Geom& g, float min_u, float max_u,
+                            float min_v, float max_v, cudaStream_t st);
+
 }  // namespace twdic

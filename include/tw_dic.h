@@ -178,6 +178,17 @@ TWDIC_API int twdic_frame_set_stream(twdic_frame* h, void* stream);
 TWDIC_API int twdic_frame_phase_times(const twdic_frame* h, float* t6);
 TWDIC_API int twdic_frame_destroy(twdic_frame* h);
 
+/* IC-GN target interpolation, ICGN2DInterpolationFLag (TW/TW_Engine/TW_paDIC.h:89-93),
+ * the Iflag of the ICGN2D_CPU / cuICGN2D constructors (TW_paDIC_ICGN2D_CPU.h:23-44):
+ * TWDIC_INTERP_BICUBIC, the Hermite bicubic LUT (BicubicCoefficients_s,
+ * TW_utils.cpp:604-700; the default), or TWDIC_INTERP_BSPLINE, the bicubic
+ * B-spline LUT (BicubicSplineCoefficients_s, TW_utils.cpp:521-602; every ROI
+ * pixel has coefficients, image pixels outside the image read as 0). */
+#define TWDIC_INTERP_BICUBIC 0
+#define TWDIC_INTERP_BSPLINE 1
+TWDIC_API int twdic_icgn_set_interpolation(twdic_icgn* h, int mode);
+TWDIC_API int twdic_frame_set_interpolation(twdic_frame* h, int mode);
+
 /* Launch-shape tuning of a frame handle (no counterpart in the reference;
  * set by the autotuner).  icgn_threads: 32, 64, 128 or 256 threads per IC-GN CTA;
  * icgn_ctas_per_sm: persistent CTAs per SM (0 = occupancy limit);

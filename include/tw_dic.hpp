@@ -21,7 +21,6 @@
  *     double-free them (TW_paDIC_cuICGN2D.cu:719-729 frees borrowed arrays);
  *   - SetTarImg sets the target (the reference's cuICGN2D::SetTarImg writes
  *     into the reference buffer, TW_paDIC_cuICGN2D.cu:805);
- *   - ICGN2DInterpolationFLag::BicubicSpline is not built yet and throws.
  * real_t is float (the reference's default build). */
 #ifndef TW_DIC_HPP
 #define TW_DIC_HPP
@@ -332,8 +331,10 @@ public:
                ICGN2DInterpolationFLag Iflag, paDICThreadFlag /*Tflag*/)
         : ICGN2D(iImgWidth, iImgHeight, iStartX, iStartY, iROIWidth, iROIHeight, iSubsetX, iSubsetY, iNumberX,
                  iNumberY, iNumIterations, fDeltaP) {
-        if (Iflag != ICGN2DInterpolationFLag::Bicubic)
-            throw std::logic_error("ICGN2D_CPU: only ICGN2DInterpolationFLag::Bicubic is built");
+        detail::check_ctor(twdic_icgn_set_interpolation(m_h, Iflag == ICGN2DInterpolationFLag::BicubicSpline
+                                                                ? TWDIC_INTERP_BSPLINE
+                                                                : TWDIC_INTERP_BICUBIC),
+                           "interpolation");
     }
     ICGN2D_CPU(const ImageView& refImg, int_t iImgWidth, int_t iImgHeight, int_t iStartX, int_t iStartY,
                int_t iROIWidth, int_t iROIHeight, int_t iSubsetX, int_t iSubsetY, int_t iNumberX, int_t iNumberY,
@@ -392,8 +393,10 @@ public:
              ICGN2DInterpolationFLag Iflag)
         : ICGN2D(iImgWidth, iImgHeight, iStartX, iStartY, iROIWidth, iROIHeight, iSubsetX, iSubsetY, iNumberX,
                  iNumberY, iNumIterations, fDeltaP) {
-        if (Iflag != ICGN2DInterpolationFLag::Bicubic)
-            throw std::logic_error("cuICGN2D: only ICGN2DInterpolationFLag::Bicubic is built");
+        detail::check_ctor(twdic_icgn_set_interpolation(m_h, Iflag == ICGN2DInterpolationFLag::BicubicSpline
+                                                                ? TWDIC_INTERP_BSPLINE
+                                                                : TWDIC_INTERP_BICUBIC),
+                           "interpolation");
     }
 
     /* Device reference image, already filled (copied into the handle). */

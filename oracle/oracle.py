@@ -93,8 +93,9 @@ def exact_surface(ref, tar, py, px, r):
     return c
 
 
-def icgn(ref, tar, geom, poi_yx, u0, v0, precision="f32", nthreads=0, iters_init=0):
-    """IC-GN over all POIs.  Returns (p6 [n,6], iters [n], flags [n])."""
+def icgn(ref, tar, geom, poi_yx, u0, v0, precision="f32", nthreads=0, iters_init=0, interp="bicubic"):
+    """IC-GN over all POIs.  Returns (p6 [n,6], iters [n], flags [n]).
+    interp: "bicubic" (the Hermite LUT) or "bspline" (the B-spline LUT)."""
     ref = np.ascontiguousarray(ref, np.uint8)
     tar = np.ascontiguousarray(tar, np.uint8)
     poi_yx = np.ascontiguousarray(poi_yx, np.int32)
@@ -110,9 +111,11 @@ def icgn(ref, tar, geom, poi_yx, u0, v0, precision="f32", nthreads=0, iters_init
     fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p] + [ctypes.c_int] * 8 + [ctypes.c_void_p, ctypes.c_int,
                                                                                ctypes.c_int, ctypes.c_float,
                                                                                ctypes.c_int, ctypes.c_void_p,
-                                                                               ctypes.c_void_p, ctypes.c_void_p]
+                                                                               ctypes.c_void_p, ctypes.c_void_p,
+                                                                               ctypes.c_int]
+    mode = {"bicubic": 0, "bspline": 1}[interp]
     rc = fn(_p(ref), _p(tar), W, H, geom.start_x, geom.start_y, geom.roi_w, geom.roi_h, geom.subset_r,
-            geom.subset_r, _p(poi_yx), n, geom.max_iter, geom.delta_p, nthreads, _p(p6), _p(iters), _p(flags))
+            geom.subset_r, _p(poi_yx), n, geom.max_iter, geom.delta_p, nthreads, _p(p6), _p(iters), _p(flags), mode)
     if rc != 0:
         raise ValueError("ROI leaves no one-pixel border")
     return p6, iters, flags
@@ -143,3 +146,14 @@ def dft2d(x, inverse=False):
 
 def max_threads():
     return lib().or_max_threads()
+
+
+def bspline_lut(tar, sx, sy, rw, rh):
+    """The target's B-spline coefficient LUT, float32 [rh, rw, 16]."""
+    tar = np.ascontiguousarray(tar, np.uint8)
+    H, W = tar.shape
+    out = np.zeros((rh, rw, 16), np.float32)
+    fn = lib().or_bspline_lut_f32
+    fn.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 6 + [ctypes.c_void_p]
+    fn(_p(tar), W, H, sx, sy, rw, rh, _p(out))
+    return out

@@ -311,6 +311,56 @@ void bicubic_lut(IcgnImages<T>& c) {
     for (int k = 0; k < 16; ++k) c.lut[((size_t)(rh - 1) * rw + (rw - 1)) * 16 + k] = 0;
 }
 
+// BicubicSplineCoefficients_s (TW_utils.cpp:521-602): per ROI pixel, the 4x4
+// neighbourhood Omega (rows y-1..y+2, columns x-1..x+2) is prefiltered by
+// the local B-spline interpolation matrix CP on both sides (Beta), mapped to
+// polynomial coefficients by the cubic B-spline basis matrix (Base), and the
+// 4x4 result is reversed in both indices so that entry [k][l] multiplies
+// fy^k fx^l.  All ROI pixels are written.  Pixels outside the image read as 0
+// (the reference reads one row and column past a one-pixel border).  The
+// matrices are rounded to T once, then every product and sum is rounded in
+// the reference's order.
+template <typename T>
+void bspline_lut(IcgnImages<T>& c) {
+    const T CP[4][4] = {{T(71 / 56.0), T(-19 / 56.0), T(5 / 56.0), T(-1 / 56.0)},
+                        {T(-19 / 56.0), T(95 / 56.0), T(-25 / 56.0), T(5 / 56.0)},
+                        {T(5 / 56.0), T(-25 / 56.0), T(95 / 56.0), T(-19 / 56.0)},
+                        {T(-1 / 56.0), T(5 / 56.0), T(-19 / 56.0), T(71 / 56.0)}};
+    const T Base[4][4] = {{T(-1 / 6.0), T(3 / 6.0), T(-3 / 6.0), T(1 / 6.0)},
+                          {T(3 / 6.0), T(-6 / 6.0), T(3 / 6.0), T(0)},
+                          {T(-3 / 6.0), T(0), T(3 / 6.0), T(0)},
+                          {T(1 / 6.0), T(4 / 6.0), T(1 / 6.0), T(0)}};
+    const int rw = c.roi_w, rh = c.roi_h, W = c.img_w, H = c.img_h;
+    c.lut.assign((size_t)rw * rh * 16, 0);
+    for (int i = 0; i < rh; ++i) {
+        for (int j = 0; j < rw; ++j) {
+            T om[4][4], be[4][4], bs[4][4];
+            for (int k = 0; k < 4; ++k)
+                for (int l = 0; l < 4; ++l) {
+                    const int y = i + c.sy - 1 + k, x = j + c.sx - 1 + l;
+                    om[k][l] = (y >= 0 && y < H && x >= 0 && x < W) ? (T)c.tar[(size_t)y * W + x] : T(0);
+                }
+            for (int k = 0; k < 4; ++k)
+                for (int l = 0; l < 4; ++l) {
+                    T a = 0;
+                    for (int m = 0; m < 4; ++m)
+                        for (int n = 0; n < 4; ++n) a += CP[k][m] * CP[l][n] * om[n][m];
+                    be[k][l] = a;
+                }
+            for (int k = 0; k < 4; ++k)
+                for (int l = 0; l < 4; ++l) {
+                    T a = 0;
+                    for (int m = 0; m < 4; ++m)
+                        for (int n = 0; n < 4; ++n) a += Base[k][m] * Base[l][n] * be[n][m];
+                    bs[k][l] = a;
+                }
+            const size_t o = (size_t)i * rw + j;
+            for (int k = 0; k < 4; ++k)
+                for (int l = 0; l < 4; ++l) c.lut[o * 16 + k * 4 + l] = bs[3 - k][3 - l];
+        }
+    }
+}
+
 template <typename T>
 inline T warp_coord(int base, T a, int d0, T b, int d1, T c) {
     // iPOIx + W[0][0]*(m - r) + W[0][1]*(l - r) + W[0][2], left to right
@@ -484,14 +534,17 @@ inline int set_threads(int nthreads) {
 template <typename T>
 int icgn_run(const uint8_t* ref, const uint8_t* tar, int W, int H, int sx, int sy, int rw, int rh, int rx, int ry,
              const int32_t* poi_yx, int n_poi, int max_iter, float delta_p, int nthreads, T* p6, int32_t* iters,
-             uint8_t* flags) {
+             uint8_t* flags, int interp = 0) {
     // ROI must leave a one-pixel border for the gradients and the LUT
     // (TW_utils.cpp:254-257, :615-619).
     if (sx < 1 || sy < 1 || sx + rw + 1 > W || sy + rh + 1 > H) return -1;
     IcgnImages<T> c;
     c.ref = ref; c.tar = tar; c.img_w = W; c.img_h = H; c.sx = sx; c.sy = sy; c.roi_w = rw; c.roi_h = rh;
     gradients(c);
-    bicubic_lut(c);
+    if (interp == 1)
+        bspline_lut(c);  // ICGN2DInterpolationFLag::BicubicSpline (TW_paDIC_ICGN2D_CPU.cpp:322-345)
+    else
+        bicubic_lut(c);
     set_threads(nthreads);
     const int S = (2 * rx + 1) * (2 * ry + 1);
 #pragma omp parallel
@@ -606,15 +659,24 @@ void or_fftcc_exact_surface(const uint8_t* ref, const uint8_t* tar, int W, int p
 // reference updates it; flags[i] receives the ICGN2DFlag value.
 int or_icgn_f32(const uint8_t* ref, const uint8_t* tar, int W, int H, int sx, int sy, int rw, int rh, int rx, int ry,
                 const int32_t* poi_yx, int n_poi, int max_iter, float delta_p, int nthreads, float* p6, int32_t* iters,
-                uint8_t* flags) {
+                uint8_t* flags, int interp) {
     return icgn_run<float>(ref, tar, W, H, sx, sy, rw, rh, rx, ry, poi_yx, n_poi, max_iter, delta_p, nthreads, p6,
-                           iters, flags);
+                           iters, flags, interp);
+}
+
+// The target's B-spline coefficient LUT, float32 ([rh][rw][16], entry 4k+l
+// multiplies fy^k fx^l), for KATs and the GPU table's equality test.
+void or_bspline_lut_f32(const uint8_t* tar, int W, int H, int sx, int sy, int rw, int rh, float* lut) {
+    IcgnImages<float> c;
+    c.ref = tar; c.tar = tar; c.img_w = W; c.img_h = H; c.sx = sx; c.sy = sy; c.roi_w = rw; c.roi_h = rh;
+    bspline_lut(c);
+    std::memcpy(lut, c.lut.data(), (size_t)rw * rh * 64);
 }
 int or_icgn_f64(const uint8_t* ref, const uint8_t* tar, int W, int H, int sx, int sy, int rw, int rh, int rx, int ry,
                 const int32_t* poi_yx, int n_poi, int max_iter, float delta_p, int nthreads, double* p6,
-                int32_t* iters, uint8_t* flags) {
+                int32_t* iters, uint8_t* flags, int interp) {
     return icgn_run<double>(ref, tar, W, H, sx, sy, rw, rh, rx, ry, poi_yx, n_poi, max_iter, delta_p, nthreads, p6,
-                            iters, flags);
+                            iters, flags, interp);
 }
 
 // Restated LAPACK kernels, exported so tests can pin them against LAPACK.

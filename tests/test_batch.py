@@ -94,3 +94,25 @@ def test_batch_graph_replay_reads_refreshed_inputs():
         f.process(p2.tar, **w)
         for k in w:
             np.testing.assert_array_equal(o[k].cpu().numpy(), w[k])
+
+
+def test_batch_with_a_bspline_frame_equals_alone():
+    from tw_gb300 import INTERP_BSPLINE
+    frames, tars, want = [], [], []
+    for k, (h, w, r, grid, seed, path) in enumerate(CASES[:3]):
+        pair, g = synth.small_case(h=h, w=w, r=r, grid=grid, seed=seed)
+        f = _frame(g, path)
+        if k == 1:
+            f.set_interpolation(INTERP_BSPLINE)
+        f.set_reference(pair.ref)
+        o = f.alloc_outputs()
+        f.process(pair.tar, **o)
+        frames.append(f)
+        tars.append(pair.tar)
+        want.append(o)
+    b = dic.DICBatch()
+    outs = [f.alloc_outputs() for f in frames]
+    b.process(frames, tars, outs)
+    for o, w in zip(outs, want):
+        for k in w:
+            np.testing.assert_array_equal(o[k], w[k])

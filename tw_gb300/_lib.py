@@ -24,6 +24,7 @@ ERR = {
     -9: "TWDIC_ERR_BUSY",
 }
 PENDING = 1  # twdic_poll: not done yet
+INTERP_BICUBIC, INTERP_BSPLINE = 0, 1  # IC-GN target interpolation
 MEM_HOST = 0
 MEM_DEVICE = 1
 PATH_PLAIN = 0
@@ -46,7 +47,7 @@ EXPORTED = (
     "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
     "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
     "twdic_tracker_create", "twdic_tracker_num_pois", "twdic_tracker_process", "twdic_tracker_colormap",
-    "twdic_tracker_destroy",
+    "twdic_tracker_destroy", "twdic_icgn_set_interpolation", "twdic_frame_set_interpolation",
 )
 
 
@@ -168,6 +169,8 @@ def load():
         "twdic_tracker_colormap": ([_VP, _VP, _VP, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                     _I], _I),
         "twdic_tracker_destroy": ([_VP], _I),
+        "twdic_icgn_set_interpolation": ([_VP, _I], _I),
+        "twdic_frame_set_interpolation": ([_VP, _I], _I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -145,6 +145,7 @@ struct Engine {
     bool have_ref = false, have_tar = false;
     IcgnTune icgn_tune;
     FftccTune fftcc_tune;
+    int interp = TWDIC_INTERP_BICUBIC;  // target interpolation of IC-GN (ICGN2DInterpolationFLag)
 
     DevBuf d_ref, d_tar, d_poi;
     DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work, d_tw;
@@ -293,7 +294,10 @@ struct Engine {
     // (TW_utils.cpp:604-700), when the IC-GN variant reads one.
     int prepare_target() {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
-        if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.sampler == kSampLut) {
+        if (interp == TWDIC_INTERP_BSPLINE) {
+            TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_bspline_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
+        } else if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.sampler == kSampLut) {
             TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
             TW_CUDA(launch_bicubic_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
         } else if (icgn_tune.sampler == kSampNbhd) {
@@ -301,6 +305,13 @@ struct Engine {
             TW_CUDA(launch_nbhd_table(g, d_tar.as<uint8_t>(), d_lut.as<uint4>(), stream));
         }
         return TWDIC_OK;
+    }
+
+    // the fast IC-GN launch shape; the B-spline interpolant is only in a LUT
+    IcgnTune solve_tune() const {
+        IcgnTune t = icgn_tune;
+        if (interp == TWDIC_INTERP_BSPLINE) t.sampler = kSampLut;
+        return t;
     }
 
     int icgn_solve(float* u, float* v, float* p6, int* iters, uint8_t* flags) {
@@ -314,7 +325,7 @@ struct Engine {
         } else {
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.p,
-                                     d_work.as<int>(), u, v, p6, iters, flags, icgn_tune, stream));
+                                     d_work.as<int>(), u, v, p6, iters, flags, solve_tune(), stream));
         }
         return TWDIC_OK;
     }
@@ -659,6 +670,23 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
     return TWDIC_OK;
 }
 
+// ICGN2DInterpolationFLag (TW/TW_Engine/TW_paDIC.h:89-93), the Iflag of the
+// ICGN2D_CPU / cuICGN2D constructors.
+static int set_interp(Engine& e, int mode) {
+    if (mode != TWDIC_INTERP_BICUBIC && mode != TWDIC_INTERP_BSPLINE)
+        return fail(TWDIC_ERR_INVALID_ARG, "interpolation must be TWDIC_INTERP_BICUBIC or TWDIC_INTERP_BSPLINE");
+    e.interp = mode;
+    return TWDIC_OK;
+}
+int twdic_icgn_set_interpolation(twdic_icgn* h, int mode) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return set_interp(h->e, mode);
+}
+int twdic_frame_set_interpolation(twdic_frame* h, int mode) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    return set_interp(h->e, mode);
+}
+
 // Tuning (internal to the Python autotuner; not part of the reference interface).
 int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                            int fftcc_use_tc) {
@@ -963,7 +991,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             fast_tc.push_back(i);
         else
             TW_TRY(e.fftcc(o.u, o.v, o.z, e.d_fst.as<uint8_t>()));
-        if (fast) fast_ic.push_back(i);
+        if (fast && e.interp == TWDIC_INTERP_BICUBIC) fast_ic.push_back(i);
     }
     // tensor-core FFT-CC: one launch per window size (and per kMaxJobs frames)
     std::vector<bool> used(fast_tc.size(), false);
@@ -992,7 +1020,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
     // target tables, then one persistent IC-GN launch over the fast frames
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
-        if (e.prm.path == TWDIC_PATH_FAST)
+        if (e.prm.path == TWDIC_PATH_FAST && e.interp == TWDIC_INTERP_BICUBIC)
             TW_TRY(prepare_target_for(e, b->tune.sampler));
         else
             TW_TRY(e.prepare_target());
@@ -1036,7 +1064,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
     }
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
-        if (e.prm.path == TWDIC_PATH_FAST) continue;
+        if (e.prm.path == TWDIC_PATH_FAST && e.interp == TWDIC_INTERP_BICUBIC) continue;
         const FrameOut o = frame_out(e, a, i);
         TW_TRY(e.icgn_solve(o.u, o.v, o.p6, o.it, o.fl));
     }

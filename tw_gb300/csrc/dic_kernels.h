@@ -64,6 +64,8 @@ cudaError_t launch_fftcc_plain(const Geom& g, const uint8_t* ref, const uint8_t*
 cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* subR,
                                         float2* sd, float* chol, float* refnorm, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
+// B-spline coefficient LUT of the target, same layout (kernels_plain.cu)
+cudaError_t launch_bspline_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
 // 4x4 byte neighbourhoods of every ROI pixel of the target (kernels_icgn_fast.cu)
 cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st);
 cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi, int n, const float* subR,

@@ -428,6 +428,75 @@ cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const
     return cudaGetLastError();
 }
 
+// BicubicSplineCoefficients_s (TW_utils.cpp:521-602): the B-spline
+// coefficient LUT of the target, same layout as k_bicubic_lut (plane k holds
+// the coefficients of fy^k fx^0..3).  Per ROI pixel the 4x4 neighbourhood is
+// prefiltered on both sides by the local B-spline interpolation matrix and
+// mapped to polynomial coefficients by the cubic B-spline basis, then both
+// indices are reversed.  Every product and sum is rounded separately, in the
+// reference's order, so the table equals the reference's FP32 table.  Pixels
+// outside the image read as 0 (the reference reads one row and column past a
+// one-pixel border); all ROI pixels are written.
+namespace {
+__device__ const float kBsCP[4][4] = {{(float)(71 / 56.0), (float)(-19 / 56.0), (float)(5 / 56.0), (float)(-1 / 56.0)},
+                                      {(float)(-19 / 56.0), (float)(95 / 56.0), (float)(-25 / 56.0), (float)(5 / 56.0)},
+                                      {(float)(5 / 56.0), (float)(-25 / 56.0), (float)(95 / 56.0), (float)(-19 / 56.0)},
+                                      {(float)(-1 / 56.0), (float)(5 / 56.0), (float)(-19 / 56.0), (float)(71 / 56.0)}};
+__device__ const float kBsBase[4][4] = {{(float)(-1 / 6.0), (float)(3 / 6.0), (float)(-3 / 6.0), (float)(1 / 6.0)},
+                                        {(float)(3 / 6.0), (float)(-6 / 6.0), (float)(3 / 6.0), 0.f},
+                                        {(float)(-3 / 6.0), 0.f, (float)(3 / 6.0), 0.f},
+                                        {(float)(1 / 6.0), (float)(4 / 6.0), (float)(1 / 6.0), 0.f}};
+}  // namespace
+
+__global__ void k_bspline_lut(Geom g, const uint8_t* __restrict__ tar, float4* __restrict__ lut) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.rh || j >= g.rw) return;
+    float om[4][4], be[4][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int y = i + g.sy - 1 + k, x = j + g.sx - 1 + l;
+            om[k][l] = (y >= 0 && y < g.img_h && x >= 0 && x < g.img_w) ? (float)tar[(size_t)y * g.pitch + x] : 0.f;
+        }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            float a = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int n = 0; n < 4; ++n) a = __fadd_rn(a, __fmul_rn(__fmul_rn(kBsCP[k][m], kBsCP[l][n]), om[n][m]));
+            be[k][l] = a;
+        }
+    const size_t plane = (size_t)g.rw * g.rh;
+    const size_t o = (size_t)i * g.rw + j;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+        float c[4];
+#pragma unroll
+        for (int ll = 0; ll < 4; ++ll) {
+            const int k = 3 - kk, l = 3 - ll;  // reversed indices
+            float a = 0.f;
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+#pragma unroll
+                for (int n = 0; n < 4; ++n)
+                    a = __fadd_rn(a, __fmul_rn(__fmul_rn(kBsBase[k][m], kBsBase[l][n]), be[n][m]));
+            c[ll] = a;
+        }
+        lut[kk * plane + o] = make_float4(c[0], c[1], c[2], c[3]);
+    }
+}
+
+cudaError_t launch_bspline_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st) {
+    dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
+    k_bspline_lut<<<grd, blk, 0, st>>>(g, tar, lut);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st) {
     dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
     k_bicubic_lut<<<grd, blk, 0, st>>>(g, tar, lut);

@@ -25,7 +25,8 @@ from typing import Optional, Tuple
 import numpy as np
 
 from . import _lib
-from ._lib import MEM_DEVICE, MEM_HOST, PATH_FAST, PATH_PLAIN, Params, TWDICError, check
+from ._lib import (INTERP_BICUBIC, INTERP_BSPLINE, MEM_DEVICE, MEM_HOST, PATH_FAST, PATH_PLAIN,  # noqa: F401
+                   Params, TWDICError, check)
 
 ICGN_FLAGS = ("Success", "DarkSubset", "SingularHessian", "SingularWarp", "OutofROI")
 
@@ -184,12 +185,14 @@ class cuICGN2D:
     """First-order IC-GN over a POI list (cuICGN2D / ICGN2D_CPU drop-in)."""
 
     def __init__(self, iImgWidth, iImgHeight, iStartX, iStartY, iROIWidth, iROIHeight, iSubsetX, iSubsetY,
-                 iNumberX, iNumberY, iNumIterations=20, fDeltaP=0.001, path=PATH_FAST):
+                 iNumberX, iNumberY, iNumIterations=20, fDeltaP=0.001, path=PATH_FAST, Iflag=INTERP_BICUBIC):
         self._lib = _lib.load()
         self.params = make_params(iImgWidth, iImgHeight, iStartX, iStartY, iROIWidth, iROIHeight, iSubsetX,
                                   iSubsetY, 1, 1, 0, 0, iNumIterations, fDeltaP, path)
         h = ctypes.c_void_p()
         check(self._lib.twdic_icgn_create(ctypes.byref(self.params), iNumberX, iNumberY, ctypes.byref(h)))
+        if Iflag != INTERP_BICUBIC:
+            check(self._lib.twdic_icgn_set_interpolation(h, Iflag))
         self._h = h
         self.m_iPOINumber = iNumberX * iNumberY
         self.last_p6 = None
@@ -265,6 +268,10 @@ class DICFrame:
         """Bind to a torch.cuda.Stream (or None for the handle's own stream)."""
         ptr = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
         check(self._lib.twdic_frame_set_stream(self._h, ptr))
+
+    def set_interpolation(self, mode):
+        """INTERP_BICUBIC (Hermite bicubic LUT, default) or INTERP_BSPLINE."""
+        check(self._lib.twdic_frame_set_interpolation(self._h, mode))
 
     def set_tuning(self, icgn_threads=128, icgn_ctas_per_sm=0, icgn_sampler=0, fftcc_use_tc=1):
         """icgn_sampler: SAMPLER_WINDOW, SAMPLER_LUT or SAMPLER_NBHD."""

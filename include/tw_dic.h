@@ -197,6 +197,12 @@ TWDIC_API int twdic_frame_set_interpolation(twdic_frame* h, int mode);
  * table; fftcc_use_tc: 1 = tensor-core FFT-CC when available. */
 TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                                      int fftcc_use_tc);
+/* IC-GN work layout of the fast path.  chunk = 0: one POI per CTA (threads
+ * 32 to 256).  chunk > 0: one POI per warp; the warps of a CTA (threads 128
+ * to 1024, a table sampler) take POIs from runs of `chunk` consecutive POIs,
+ * so the subsets in flight on an SM overlap and are re-read from L1, and the
+ * reference gradients come from a per-reference image (4 B per ROI pixel). */
+TWDIC_API int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk);
 
 /* FFT-CC tile of a frame handle: use_tc (tensor-core kernel), groups (0 = as
  * many 128-thread groups per CTA as fit, 1 = one), pois_per_group (POIs per
@@ -208,6 +214,7 @@ typedef struct {
     int32_t fftcc_use_tc, fftcc_groups, fftcc_pois_per_group;
     float fftcc_ms, icgn_ms; /* phase times of the chosen shapes (target preparation included in icgn_ms) */
     int32_t from_cache;      /* 1: read from the cache file, not measured */
+    int32_t icgn_chunk;      /* IC-GN work layout (twdic_frame_set_icgn_layout) */
 } twdic_tuning;
 TWDIC_API int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out);
 /* Autotuner (no reference counterpart): times the FFT-CC tile shapes and the
@@ -271,6 +278,8 @@ typedef struct twdic_batch twdic_batch;
 TWDIC_API int twdic_batch_create(twdic_batch** out);
 TWDIC_API int twdic_batch_set_stream(twdic_batch* b, void* stream);
 TWDIC_API int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler);
+/* IC-GN work layout of the batch's launches (twdic_frame_set_icgn_layout). */
+TWDIC_API int twdic_batch_set_icgn_layout(twdic_batch* b, int chunk);
 TWDIC_API int twdic_batch_set_graph(twdic_batch* b, int enable);
 /* Arrays of `count` entries; zncc, p6, iters, flags (the arrays) may be NULL,
  * strides may be NULL (contiguous images); replayed may be NULL. */

@@ -88,16 +88,24 @@ def test_frame_parity(request, case, path):
         np.testing.assert_array_equal(out[k], out2[k])
 
 
-@pytest.mark.parametrize("threads", [32, 64, 128, 256])
+# (threads per CTA, chunk): one POI per CTA (chunk 0), or one POI per warp
+# over runs of `chunk` consecutive POIs
+ICGN_SHAPES = [(32, 0), (64, 0), (128, 0), (256, 0), (1024, 32), (512, 16), (128, 4)]
+
+
+@pytest.mark.parametrize("shape", ICGN_SHAPES, ids=lambda s: f"t{s[0]}c{s[1]}")
 @pytest.mark.parametrize("sampler", [SAMPLER_WINDOW, SAMPLER_LUT, SAMPLER_NBHD])
-def test_fast_icgn_samplers(plain512, sampler, threads):
+def test_fast_icgn_samplers(plain512, sampler, shape):
     """Every launch shape and target sampler of the fast IC-GN meets the
     parity bar against the oracle (staged window and neighbourhood table
     evaluate the Catmull-Rom form, the LUT sampler the reference's Hermite
     coefficients)."""
+    threads, chunk = shape
+    if chunk > 0 and sampler == SAMPLER_WINDOW:
+        pytest.skip("one POI per warp reads a per-frame table")
     pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = plain512
     fr = dic.DICFrame(params_of(g, PATH_FAST))
-    fr.set_tuning(threads, 0, sampler, 1)
+    fr.set_tuning(threads, 0, sampler, 1, icgn_chunk=chunk)
     fr.set_reference(pair.ref)
     out = fr.alloc_outputs()
     fr.process(pair.tar, **out)
@@ -108,7 +116,41 @@ def test_fast_icgn_samplers(plain512, sampler, threads):
     same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
     rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start,
                         r=g.subset_r)
-    assert rep.ok(), (sampler, threads, rep)
+    assert rep.ok(), (sampler, shape, rep)
+
+
+@pytest.mark.parametrize("sampler", [SAMPLER_LUT, SAMPLER_NBHD])
+def test_warp_layout_matches_one_warp_cta(plain512, sampler):
+    """One POI per warp (per-reference gradient image, runs of consecutive
+    POIs) does per POI exactly the arithmetic of the one-warp CTA: same
+    sample order per lane, sums, solve and update, so every output is
+    bit-identical, whatever the run length and CTA size."""
+    pair, g, poi, _ = plain512
+    outs = []
+    for threads, chunk in [(32, 0), (1024, 32), (512, 7), (128, 1)]:
+        fr = dic.DICFrame(params_of(g, PATH_FAST))
+        fr.set_tuning(threads, 0, sampler, 1, icgn_chunk=chunk)
+        fr.set_reference(pair.ref)
+        o = fr.alloc_outputs()
+        fr.process(pair.tar, **o)
+        outs.append(o)
+    for o in outs[1:]:
+        for k in o:
+            np.testing.assert_array_equal(o[k], outs[0][k], err_msg=k)
+
+
+def test_layout_rejects_bad_shapes(small):
+    pair, g, poi, _ = small
+    fr = dic.DICFrame(params_of(g, PATH_FAST))
+    with pytest.raises(Exception):
+        fr.set_icgn_layout(-1)
+    with pytest.raises(Exception):
+        fr.set_tuning(96, 0, SAMPLER_NBHD, 1)
+    # 1024 threads need the one-POI-per-warp layout: the launch is refused
+    fr.set_tuning(1024, 0, SAMPLER_NBHD, 1, icgn_chunk=0)
+    fr.set_reference(pair.ref)
+    with pytest.raises(Exception):
+        fr.process(pair.tar, **fr.alloc_outputs())
 
 
 @pytest.mark.parametrize("path", PATHS)

@@ -34,6 +34,8 @@ int fail(int code, const char* fmt, ...) {
     return code;
 }
 
+bool valid_icgn_threads(int t) { return t == 32 || t == 64 || t == 128 || t == 256 || t == 512 || t == 1024; }
+
 #define TW_CUDA(call)                                                                                   \
     do {                                                                                                \
         cudaError_t e_ = (call);                                                                        \
@@ -154,7 +156,7 @@ struct Engine {
     const void* cache_poi_key = nullptr;
     std::vector<int32_t> cache_poi_host;
     DevBuf c_subR, c_sd, c_chol, c_norm, c_flag;  // plain
-    DevBuf c_stat, c_chol64, c_flag64;            // fast
+    DevBuf c_stat, c_chol64, c_flag64, c_grad;    // fast
     DevBuf d_lut;
     cudaEvent_t ev[7] = {};
     cudaEvent_t ev_sync = nullptr;  // orders this handle's stream with a batch stream
@@ -171,9 +173,11 @@ struct Engine {
     int init(const twdic_params& p, int num_pois) {
         prm = p;
         // fastest measured IC-GN shape on GB300 at 41x41 subsets: one warp
-        // per POI gathering the per-frame 4x4 neighbourhood table (16 B per
-        // ROI pixel; the autotuner may change it)
-        icgn_tune.threads = 32;
+        // per POI, one 32-warp CTA per SM walking runs of 32 consecutive
+        // POIs, gathering the per-frame 4x4 neighbourhood table (16 B per ROI
+        // pixel) through L1 (the autotuner may change it)
+        icgn_tune.threads = 1024;
+        icgn_tune.chunk = 32;
         icgn_tune.sampler = kSampNbhd;
         g = make_geom(p);
         n = num_pois;
@@ -278,6 +282,8 @@ struct Engine {
             TW_TRY(c_flag64.ensure((size_t)n));
             TW_CUDA(launch_ref_precompute_fast(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_stat.as<float>(),
                                                c_chol64.as<double>(), c_flag64.as<uint8_t>(), stream));
+            TW_TRY(c_grad.ensure(sizeof(__half2) * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_ref_grad(g, d_ref.as<uint8_t>(), c_grad.as<__half2>(), stream));
         }
         cache_valid = true;
         if (t_pre) *t_pre = 1.f;
@@ -325,7 +331,8 @@ struct Engine {
         } else {
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.p,
-                                     d_work.as<int>(), u, v, p6, iters, flags, solve_tune(), stream));
+                                     d_work.as<int>(), u, v, p6, iters, flags, solve_tune(), stream,
+                                     c_grad.as<__half2>()));
         }
         return TWDIC_OK;
     }
@@ -691,8 +698,8 @@ int twdic_frame_set_interpolation(twdic_frame* h, int mode) {
 int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler,
                            int fftcc_use_tc) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (icgn_threads != 32 && icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
-        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
+    if (!valid_icgn_threads(icgn_threads))
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128, 256, 512 or 1024");
     h->e.icgn_tune.threads = icgn_threads;
     h->e.icgn_tune.ctas_per_sm = icgn_ctas_per_sm;
     if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
@@ -702,6 +709,13 @@ int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_ctas_per_s
     return TWDIC_OK;
 }
 
+
+int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (chunk < 0) return fail(TWDIC_ERR_INVALID_ARG, "chunk must be >= 0");
+    h->e.icgn_tune.chunk = chunk;
+    return TWDIC_OK;
+}
 
 int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
@@ -718,6 +732,7 @@ int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out) {
     out->icgn_threads = h->e.icgn_tune.threads;
     out->icgn_ctas_per_sm = h->e.icgn_tune.ctas_per_sm;
     out->icgn_sampler = h->e.icgn_tune.sampler;
+    out->icgn_chunk = h->e.icgn_tune.chunk;
     out->fftcc_use_tc = h->e.fftcc_tune.use_tc;
     out->fftcc_groups = h->e.fftcc_tune.groups;
     out->fftcc_pois_per_group = h->e.fftcc_tune.pois_per_group;
@@ -757,8 +772,9 @@ bool cache_lookup(const char* path, const std::string& key, twdic_tuning* t) {
         if (std::strncmp(line, key.c_str(), k) != 0 || line[k] != ' ') continue;
         twdic_tuning c;
         std::memset(&c, 0, sizeof(c));
-        if (std::sscanf(line + k, " %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm, &c.icgn_sampler,
-                        &c.fftcc_use_tc, &c.fftcc_groups, &c.fftcc_pois_per_group, &c.fftcc_ms, &c.icgn_ms) == 8) {
+        if (std::sscanf(line + k, " %d %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm,
+                        &c.icgn_sampler, &c.icgn_chunk, &c.fftcc_use_tc, &c.fftcc_groups, &c.fftcc_pois_per_group,
+                        &c.fftcc_ms, &c.icgn_ms) == 9) {
             *t = c;  // the last entry for a key wins
             found = true;
         }
@@ -789,6 +805,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
         e.icgn_tune.threads = t.icgn_threads;
         e.icgn_tune.ctas_per_sm = t.icgn_ctas_per_sm;
         e.icgn_tune.sampler = t.icgn_sampler;
+        e.icgn_tune.chunk = t.icgn_chunk;
         e.fftcc_tune.use_tc = t.fftcc_use_tc;
         e.fftcc_tune.groups = t.fftcc_groups;
         e.fftcc_tune.pois_per_group = t.fftcc_pois_per_group;
@@ -846,10 +863,15 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     IcgnTune best_i = icgn0;
     float best_ims = 1e30f, fms = best_fms;
     if (e.prm.path == TWDIC_PATH_FAST) {
-        for (int threads : {32, 64, 128, 256}) {
+        // (threads, chunk): one POI per warp over runs of consecutive POIs,
+        // then one POI per CTA
+        const int shapes[][2] = {{1024, 32}, {1024, 64}, {512, 32}, {32, 0}, {64, 0}, {128, 0}, {256, 0}};
+        for (const auto& sh : shapes) {
             for (int sampler : {kSampNbhd, kSampLut, kSampWindow}) {
+                if (sh[1] > 0 && sampler == kSampWindow) continue;
                 IcgnTune c;
-                c.threads = threads;
+                c.threads = sh[0];
+                c.chunk = sh[1];
                 c.ctas_per_sm = 0;
                 c.sampler = sampler;
                 e.icgn_tune = c;
@@ -877,6 +899,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     t.icgn_threads = best_i.threads;
     t.icgn_ctas_per_sm = best_i.ctas_per_sm;
     t.icgn_sampler = best_i.sampler;
+    t.icgn_chunk = best_i.chunk;
     t.fftcc_use_tc = e.fftcc_tune.use_tc;
     t.fftcc_groups = e.fftcc_tune.groups;
     t.fftcc_pois_per_group = e.fftcc_tune.pois_per_group;
@@ -886,9 +909,9 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     if (cache_path) {
         FILE* f = std::fopen(cache_path, "a");
         if (f) {
-            std::fprintf(f, "%s %d %d %d %d %d %d %.4f %.4f\n", key.c_str(), t.icgn_threads, t.icgn_ctas_per_sm,
-                         t.icgn_sampler, t.fftcc_use_tc, t.fftcc_groups, t.fftcc_pois_per_group, t.fftcc_ms,
-                         t.icgn_ms);
+            std::fprintf(f, "%s %d %d %d %d %d %d %d %.4f %.4f\n", key.c_str(), t.icgn_threads, t.icgn_ctas_per_sm,
+                         t.icgn_sampler, t.icgn_chunk, t.fftcc_use_tc, t.fftcc_groups, t.fftcc_pois_per_group,
+                         t.fftcc_ms, t.icgn_ms);
             std::fclose(f);
         }
     }
@@ -1050,6 +1073,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             jb.hinv = e.c_chol64.as<double>();
             jb.rflag = e.c_flag64.as<uint8_t>();
             jb.table = b->tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
+            jb.grad = e.c_grad.as<__half2>();
             jb.u = o.u;
             jb.v = o.v;
             jb.p6 = o.p6;
@@ -1084,7 +1108,8 @@ int twdic_batch_create(twdic_batch** out) {
     TW_TRY(b->d_work.ensure(sizeof(int) * 4));
     TW_TRY(b->d_err.ensure(sizeof(unsigned)));
     TW_CUDA(cudaMemset(b->d_err.p, 0, sizeof(unsigned)));
-    b->tune.threads = 32;
+    b->tune.threads = 1024;
+    b->tune.chunk = 32;
     b->tune.sampler = kSampNbhd;
     *out = b.release();
     return TWDIC_OK;
@@ -1099,13 +1124,23 @@ int twdic_batch_set_stream(twdic_batch* b, void* stream) {
 
 int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler) {
     if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (icgn_threads != 32 && icgn_threads != 64 && icgn_threads != 128 && icgn_threads != 256)
-        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
+    if (!valid_icgn_threads(icgn_threads))
+        return fail(TWDIC_ERR_INVALID_ARG, "threads must be 32, 64, 128, 256, 512 or 1024");
     if (icgn_sampler < kSampWindow || icgn_sampler > kSampNbhd)
         return fail(TWDIC_ERR_INVALID_ARG, "sampler must be 0, 1 or 2");
     b->tune.threads = icgn_threads;
     b->tune.ctas_per_sm = icgn_ctas_per_sm;
     b->tune.sampler = icgn_sampler;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->key.clear();
+    return TWDIC_OK;
+}
+
+int twdic_batch_set_icgn_layout(twdic_batch* b, int chunk) {
+    if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (chunk < 0) return fail(TWDIC_ERR_INVALID_ARG, "chunk must be >= 0");
+    b->tune.chunk = chunk;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
     b->key.clear();

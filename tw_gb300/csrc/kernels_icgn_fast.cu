@@ -193,32 +193,62 @@ __global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __r
 }
 
 // Catmull-Rom interpolation along one row of four pixels v0..v3 (bytes of
-// w, v0 lowest) at fraction t, times two:
-//   2 h(t) = e0 + t (e1 + t (e2 + t e3)),
-//   e0 = 2 v1, e1 = v2 - v0, e2 = 2 v0 - 5 v1 + 4 v2 - v3, e3 = -v0 + 3 v1 - 3 v2 + v3,
+// w, v0 lowest) at fraction t:
+//   h(t) = v1 + (t/2) (e1 + t (e2 + t e3)),
+//   e1 = v2 - v0, e2 = 2 v0 - 5 v1 + 4 v2 - v3, e3 = -v0 + 3 v1 - 3 v2 + v3,
 // the integer coefficients by one DP4A each (unsigned pixel bytes times signed
-// weight bytes), exact; then Horner in FP32.
+// weight bytes), exact; then Horner in FP32, two rows at a time on the
+// packed FP32 pipe (f32x2).  The conversions are split between pipes: the
+// coefficients by I2F; v1 by a byte permute into the low mantissa bits of
+// 1.5 * 2^23 and one exact packed subtraction of 1.5 * 2^23 for both rows.
 __device__ __forceinline__ int dp4a_us(uint32_t a, uint32_t b) {
     int d;
     asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(0));
     return d;
 }
-__device__ __forceinline__ float cr_row2(uint32_t w, float t) {
-    const float e0 = (float)dp4a_us(w, 0x00000200u);  // (0, 2, 0, 0)
-    const float e1 = (float)dp4a_us(w, 0x000100FFu);  // (-1, 0, 1, 0)
-    const float e2 = (float)dp4a_us(w, 0xFF04FB02u);  // (2, -5, 4, -1)
-    const float e3 = (float)dp4a_us(w, 0x01FD03FFu);  // (-1, 3, -3, 1)
-    return fmaf(fmaf(fmaf(e3, t, e2), t, e1), t, e0);
+__device__ __forceinline__ float v1_biased(uint32_t w) {
+    return __int_as_float((int)__byte_perm(w, 0x4B400000u, 0x7651));  // bytes (v1, 0x00, 0x40, 0x4B)
 }
-// Catmull-Rom combination in fraction t of four row values given times two
-// (H_a = 2 h_a): the interpolated value.
-__device__ __forceinline__ float cr_combine4(const float* H, float t) {
-    const float f1 = H[2] - H[0];
-    const float f2 = fmaf(2.f, H[0], fmaf(-5.f, H[1], fmaf(4.f, H[2], -H[3])));
-    const float f3 = fmaf(3.f, H[1] - H[2], H[3] - H[0]);
-    const float f0 = 2.f * H[1];
-    return 0.25f * fmaf(fmaf(fmaf(f3, t, f2), t, f1), t, f0);
+__device__ __forceinline__ float2 cr_row_pair(uint32_t wa, uint32_t wb, float t) {
+    const float2 v1 = __fadd2_rn(make_float2(v1_biased(wa), v1_biased(wb)), make_float2(-12582912.0f, -12582912.0f));
+    const float2 e1 = make_float2((float)dp4a_us(wa, 0x000100FFu), (float)dp4a_us(wb, 0x000100FFu));  // (-1, 0, 1, 0)
+    const float2 e2 = make_float2((float)dp4a_us(wa, 0xFF04FB02u), (float)dp4a_us(wb, 0xFF04FB02u));  // (2, -5, 4, -1)
+    const float2 e3 = make_float2((float)dp4a_us(wa, 0x01FD03FFu), (float)dp4a_us(wb, 0x01FD03FFu));  // (-1, 3, -3, 1)
+    const float2 tt = make_float2(t, t), th = make_float2(0.5f * t, 0.5f * t);
+    return __ffma2_rn(__ffma2_rn(__ffma2_rn(e3, tt, e2), tt, e1), th, v1);
 }
+// Catmull-Rom combination in fraction t of four row values
+// (H01 = (h_0, h_1), H23 = (h_2, h_3)): twice the interpolated value.
+__device__ __forceinline__ float cr_combine4x4(float2 H01, float2 H23, float t) {
+    const float f1 = H23.x - H01.x;
+    const float f2 = fmaf(2.f, H01.x, fmaf(-5.f, H01.y, fmaf(4.f, H23.x, -H23.y)));
+    const float f3 = fmaf(3.f, H01.y - H23.x, H23.y - H01.x);
+    const float f0 = 2.f * H01.y;
+    return fmaf(fmaf(fmaf(f3, t, f2), t, f1), t, f0);
+}
+
+// Per-sample sums of one IC-GN pass on packed FP32: (sum t', sum t'^2),
+// (sum R_x t', sum R_y t'), (sum R_x t' dx, sum R_y t' dx),
+// (sum R_x t' dy, sum R_y t' dy), t' = T - mean(R).
+struct PassSums {
+    float2 s01 = make_float2(0.f, 0.f), s25 = make_float2(0.f, 0.f);
+    float2 s36 = make_float2(0.f, 0.f), s47 = make_float2(0.f, 0.f);
+    __device__ __forceinline__ void add(float tp, float2 gr, float2 d) {
+        const float2 tt = make_float2(tp, tp);
+        s01 = __ffma2_rn(tt, make_float2(1.f, tp), s01);
+        const float2 ab = __fmul2_rn(gr, tt);
+        s25 = __fadd2_rn(s25, ab);
+        s36 = __ffma2_rn(ab, make_float2(d.x, d.x), s36);
+        s47 = __ffma2_rn(ab, make_float2(d.y, d.y), s47);
+    }
+    // the eight sums in the order sum t', sum t'^2, R_x t', R_x t' dx,
+    // R_x t' dy, R_y t', R_y t' dx, R_y t' dy
+    __device__ __forceinline__ void unpack(float* s) const {
+        s[0] = s01.x; s[1] = s01.y;
+        s[2] = s25.x; s[3] = s36.x; s[4] = s47.x;
+        s[5] = s25.y; s[6] = s36.y; s[7] = s47.y;
+    }
+};
 
 // Catmull-Rom weights (the Hermite bicubic with central differences).
 __device__ __forceinline__ void cr_weights(float t, float& w0, float& w1, float& w2, float& w3) {
@@ -374,60 +404,64 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
         __syncthreads();
         int it = 0;  // solves completed; abort/counter rule as in the plain kernel
         while (!done) {
-            float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float s[8];
+            PassSums ps;
             const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
             // uniform over the CTA: every thread evaluates the same corners
             const bool oor = pass_out_of_roi(g, Wm, bx, by);
             if (!oor) {
-                float dxf = dx_first, dyf = dy_first;
+                // (dx, dy) of the current sample; warp_x / warp_y on packed FP32
+                float2 d = make_float2(dx_first, dy_first);
+                const float2 dd = make_float2(ddx, ddy), wrap = make_float2(-swf, 1.f);
+                const float2 w03 = make_float2(Wm[0], Wm[3]), w14 = make_float2(Wm[1], Wm[4]);
+                const float2 bxy = make_float2(bx, by);
                 const __half2* gp = grad + tid;
                 if (it == 0) {
                     // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
 #pragma unroll 4
                     for (int k = tid; k < S; k += THREADS) {
-                        const int ix = (int)warp_x(Wm, bx, dxf, dyf), iy = (int)warp_y(Wm, by, dxf, dyf);
+                        const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
+                                                      __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
+                        const int ix = (int)wxy.x, iy = (int)wxy.y;
                         const int lx = ix - wx0, ly = iy - wy0;
                         const float t = (SAMPLER == kSampWindow && lx >= 0 && ly >= 0 && lx < ws && ly < ws)
                                             ? win[ly * ws + lx]
                                             : (float)tar[(size_t)iy * g.pitch + ix];
-                        const float2 gr = __half22float2(*gp);
-                        const float tp = t - c;
-                        const float a = gr.x * tp, b = gr.y * tp;
-                        s[0] += tp;
-                        s[1] = fmaf(tp, tp, s[1]);
-                        s[2] += a; s[3] = fmaf(a, dxf, s[3]); s[4] = fmaf(a, dyf, s[4]);
-                        s[5] += b; s[6] = fmaf(b, dxf, s[6]); s[7] = fmaf(b, dyf, s[7]);
+                        ps.add(t - c, __half22float2(*gp), d);
                         gp += THREADS;
-                        dxf += ddx;
-                        dyf += ddy;
-                        if (dxf > rxf) { dxf -= swf; dyf += 1.f; }
+                        d = __fadd2_rn(d, dd);
+                        if (d.x > rxf) d = __fadd2_rn(d, wrap);
                     }
                 } else {
 #pragma unroll 4
                     for (int k = tid; k < S; k += THREADS) {
-                        const float wx = warp_x(Wm, bx, dxf, dyf), wy = warp_y(Wm, by, dxf, dyf);
-                        const int ix = (int)wx, iy = (int)wy;
-                        const float fx = wx - (float)ix, fy = wy - (float)iy;
-                        float t;
+                        const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
+                                                      __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
+                        const int ix = (int)wxy.x, iy = (int)wxy.y;
+                        const float2 fxy = __fadd2_rn(wxy, make_float2(-(float)ix, -(float)iy));
+                        const float fx = fxy.x, fy = fxy.y;
+                        float tp;
                         if (SAMPLER == kSampNbhd) {
                             // 4x4 pixels around (ix, iy), row-major bytes; zero on the
                             // ROI's last row and column, as the reference LUT is there
                             const uint4 q = nb0[(size_t)iy * g.rw + ix];
-                            const uint32_t wr[4] = {q.x, q.y, q.z, q.w};
-                            float hr[4];
-#pragma unroll
-                            for (int a = 0; a < 4; ++a) hr[a] = cr_row2(wr[a], fx);
-                            t = cr_combine4(hr, fy);
+                            const float2 h01 = cr_row_pair(q.x, q.y, fx), h23 = cr_row_pair(q.z, q.w, fx);
+                            tp = fmaf(0.5f, cr_combine4x4(h01, h23, fy), -c);
                         } else if (SAMPLER == kSampLut) {
                             const float4* q = lut0 + ((size_t)iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
-                            const float r0 = ((a0.w * fx + a0.z) * fx + a0.y) * fx + a0.x;
-                            const float r1 = ((a1.w * fx + a1.z) * fx + a1.y) * fx + a1.x;
-                            const float r2 = ((a2.w * fx + a2.z) * fx + a2.y) * fx + a2.x;
-                            const float r3 = ((a3.w * fx + a3.z) * fx + a3.y) * fx + a3.x;
-                            t = ((r3 * fy + r2) * fy + r1) * fy + r0;
+                            const float2 tx = make_float2(fx, fx);
+                            const float2 r01 = __ffma2_rn(
+                                __ffma2_rn(__ffma2_rn(make_float2(a0.w, a1.w), tx, make_float2(a0.z, a1.z)), tx,
+                                           make_float2(a0.y, a1.y)),
+                                tx, make_float2(a0.x, a1.x));
+                            const float2 r23 = __ffma2_rn(
+                                __ffma2_rn(__ffma2_rn(make_float2(a2.w, a3.w), tx, make_float2(a2.z, a3.z)), tx,
+                                           make_float2(a2.y, a3.y)),
+                                tx, make_float2(a2.x, a3.x));
+                            tp = (((r23.y * fy + r23.x) * fy + r01.y) * fy + r01.x) - c;
                         } else if (iy - g.sy == g.rh - 1 || ix - g.sx == g.rw - 1) {
-                            t = 0.f;  // the reference LUT's never-written last row / column
+                            tp = 0.f - c;  // the reference LUT's never-written last row / column
                         } else {
                             const int lx = ix - wx0, ly = iy - wy0;
                             float cx0, cx1, cx2, cx3, cy0, cy1, cy2, cy3;
@@ -450,21 +484,15 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                                             cx3 * (float)w[3];
                                 }
                             }
-                            t = cy0 * rr[0] + cy1 * rr[1] + cy2 * rr[2] + cy3 * rr[3];
+                            tp = (cy0 * rr[0] + cy1 * rr[1] + cy2 * rr[2] + cy3 * rr[3]) - c;
                         }
-                        const float2 gr = __half22float2(*gp);
-                        const float tp = t - c;
-                        const float a = gr.x * tp, b = gr.y * tp;
-                        s[0] += tp;
-                        s[1] = fmaf(tp, tp, s[1]);
-                        s[2] += a; s[3] = fmaf(a, dxf, s[3]); s[4] = fmaf(a, dyf, s[4]);
-                        s[5] += b; s[6] = fmaf(b, dxf, s[6]); s[7] = fmaf(b, dyf, s[7]);
+                        ps.add(tp, __half22float2(*gp), d);
                         gp += THREADS;
-                        dxf += ddx;
-                        dyf += ddy;
-                        if (dxf > rxf) { dxf -= swf; dyf += 1.f; }
+                        d = __fadd2_rn(d, dd);
+                        if (d.x > rxf) d = __fadd2_rn(d, wrap);
                     }
                 }
+                ps.unpack(s);
                 // ---- one reduction (FP32)
 #pragma unroll
                 for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
@@ -543,6 +571,218 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
     }
 }
 
+// Reference gradients of every ROI pixel as half2 (R_x, R_y): central
+// differences (TW_utils.cpp:232-305), half integers of magnitude <= 127.5,
+// exact in FP16.  The ROI has one pixel of border on every side, so every
+// neighbour read lies in the image.
+__global__ void k_ref_grad(Geom g, const uint8_t* __restrict__ ref, __half2* __restrict__ grad) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.rh || j >= g.rw) return;
+    const uint8_t* r = ref + (size_t)(i + g.sy) * g.pitch + (j + g.sx);
+    grad[(size_t)i * g.rw + j] = __floats2half2_rn(0.5f * (float)((int)r[1] - (int)r[-1]),
+                                                   0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
+}
+
+// Persistent IC-GN kernel, one POI per warp.  The warps of a CTA walk runs
+// of CHUNK consecutive POIs (CTA b takes runs b, b + gridDim.x, ...; its
+// warps draw POIs from them in order through a shared counter), so the
+// subsets a CTA has in flight overlap and their target-table entries and
+// reference gradients (global, per-reference half2 image) are re-read from
+// L1 across neighbouring POIs and across iterations.  The arithmetic per
+// POI is that of k_icgn_fast<32, ...>: the same sample order per lane, the
+// same sums, reduction, solve and update, so the results are identical.
+template <int NW, int SAMPLER, bool MULTI>
+__global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
+    k_icgn_warp(const __grid_constant__ IcgnJobs J, int chunk) {
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ int s_next;
+    __shared__ double s_h[NW][36];  // rows of H^-1 of each warp's POI
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    double* hw = s_h[wid];
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&s_next, 1);
+        t = __shfl_sync(FULL, t, 0);
+        const long long pgl = ((long long)blockIdx.x + (long long)(t / chunk) * gridDim.x) * chunk + t % chunk;
+        if (pgl >= J.total) break;
+        const int pg = (int)pgl;
+        int jj = 0;
+        if (MULTI) {
+            while (jj + 1 < J.njobs && pg >= J.job[jj + 1].begin) ++jj;
+        }
+        const IcgnJob& jb = J.job[jj];
+        const Geom& g = jb.g;
+        const int p = pg - jb.begin;
+        const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
+        const float inv_s = 1.0f / (float)S;
+        const float rxf = (float)g.rx, swf = (float)SW;
+        const size_t plane = (size_t)g.rw * g.rh;
+        const float4* lut0 = static_cast<const float4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
+        const uint4* nb0 = static_cast<const uint4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
+        const int2 pyx = jb.poi[p];
+        const int py = pyx.x, px = pyx.y;
+        const float u0 = jb.u[p], v0 = jb.v[p];
+        const uint8_t rf = jb.rflag[p];
+        float P[6] = {u0, 0.f, 0.f, v0, 0.f, 0.f};  // maintained by lane 0
+        float Wm[6] = {1.f, 0.f, u0, 0.f, 1.f, v0};
+        if (rf == kDarkSubset || rf == kOutofROI) {
+            if (lane == 0) {
+                jb.flags[p] = rf;
+                for (int k = 0; k < 6; ++k) jb.p6[(size_t)p * 6 + k] = P[k];
+            }
+            continue;
+        }
+        // lane k < 6: row k of H^-1 (FP64), sum SD_k and sum SD_k (R - mean)
+        const float* st = jb.stats + (size_t)p * 16;
+        const float c = st[0], rs = st[1];
+        float sumsd = 0.f, qk = 0.f;
+        if (lane < 6) {
+            sumsd = st[2 + lane];
+            qk = st[8 + lane];
+            const double* hi = jb.hinv + (size_t)p * 21;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) hw[lane * 6 + j] = hi[lane >= j ? tri(lane, j) : tri(j, lane)];
+        }
+        __syncwarp();
+        // sample k = lane + 32 j at subset offset (dx, dy); its gradient at
+        // ROI offset gofs, stepped with the same carry
+        const __half2* grad0 = jb.grad + ((size_t)(py - g.ry - g.sy) * g.rw + (px - g.rx - g.sx));
+        const int gofs_first = (lane / SW) * g.rw + lane % SW;
+        const int dgofs = (32 / SW) * g.rw + 32 % SW, gwrap = g.rw - SW;
+        const float2 d_first = make_float2((float)(lane % SW - g.rx), (float)(lane / SW - g.ry));
+        const float2 dd = make_float2((float)(32 % SW), (float)(32 / SW)), wrap = make_float2(-swf, 1.f);
+        int it = 0;
+        for (;;) {
+            const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
+            const bool oor = pass_out_of_roi(g, Wm, bx, by);
+            float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (!oor) {
+                PassSums ps;
+                float2 d = d_first;
+                int gofs = gofs_first;
+                const float2 w03 = make_float2(Wm[0], Wm[3]), w14 = make_float2(Wm[1], Wm[4]);
+                const float2 bxy = make_float2(bx, by);
+                if (it == 0) {
+                    // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
+#pragma unroll 4
+                    for (int k = lane; k < S; k += 32) {
+                        const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
+                                                      __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
+                        const int ix = (int)wxy.x, iy = (int)wxy.y;
+                        ps.add((float)jb.tar[(size_t)iy * g.pitch + ix] - c, __half22float2(grad0[gofs]), d);
+                        gofs += dgofs;
+                        d = __fadd2_rn(d, dd);
+                        if (d.x > rxf) {
+                            d = __fadd2_rn(d, wrap);
+                            gofs += gwrap;
+                        }
+                    }
+                } else {
+#pragma unroll 4
+                    for (int k = lane; k < S; k += 32) {
+                        const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
+                                                      __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
+                        const int ix = (int)wxy.x, iy = (int)wxy.y;
+                        const float2 fxy = __fadd2_rn(wxy, make_float2(-(float)ix, -(float)iy));
+                        const float fx = fxy.x, fy = fxy.y;
+                        float tp;
+                        if (SAMPLER == kSampNbhd) {
+                            const uint4 q = nb0[(size_t)iy * g.rw + ix];
+                            const float2 h01 = cr_row_pair(q.x, q.y, fx), h23 = cr_row_pair(q.z, q.w, fx);
+                            tp = fmaf(0.5f, cr_combine4x4(h01, h23, fy), -c);
+                        } else {
+                            const float4* q = lut0 + ((size_t)iy * g.rw + ix);
+                            const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
+                            const float2 tx = make_float2(fx, fx);
+                            const float2 r01 = __ffma2_rn(
+                                __ffma2_rn(__ffma2_rn(make_float2(a0.w, a1.w), tx, make_float2(a0.z, a1.z)), tx,
+                                           make_float2(a0.y, a1.y)),
+                                tx, make_float2(a0.x, a1.x));
+                            const float2 r23 = __ffma2_rn(
+                                __ffma2_rn(__ffma2_rn(make_float2(a2.w, a3.w), tx, make_float2(a2.z, a3.z)), tx,
+                                           make_float2(a2.y, a3.y)),
+                                tx, make_float2(a2.x, a3.x));
+                            tp = (((r23.y * fy + r23.x) * fy + r01.y) * fy + r01.x) - c;
+                        }
+                        ps.add(tp, __half22float2(grad0[gofs]), d);
+                        gofs += dgofs;
+                        d = __fadd2_rn(d, dd);
+                        if (d.x > rxf) {
+                            d = __fadd2_rn(d, wrap);
+                            gofs += gwrap;
+                        }
+                    }
+                }
+                ps.unpack(s);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
+            }
+            // FP32 scalars, FP64 H^-1 b on lanes 0-5, warp update on lane 0
+            const float S0 = s[0], S1 = s[1];
+            const float Ak = lane == 0 ? s[2] : lane == 1 ? s[3] : lane == 2 ? s[4] : lane == 3 ? s[5]
+                           : lane == 4 ? s[6] : s[7];
+            const float m0 = S0 * inv_s;
+            const float mean_t = c + m0;
+            const float var = S1 - S0 * m0;
+            const float ts = sqrtf(var > 0.f ? var : 0.f);
+            int flag = kSuccess, cont = 0;
+            if (oor) {
+                flag = kOutofROI;
+            } else if (fabsf(mean_t) <= FLT_EPSILON || fabsf(ts) <= FLT_EPSILON) {
+                flag = kDarkSubset;
+            } else if (it == 0 && rf == kSingularHessian) {
+                flag = kSingularHessian;
+            }
+            float dpk = 0.f;
+            if (flag == kSuccess) {
+                const float q = rs / ts;
+                const float bk = (lane < 6) ? q * (Ak - m0 * sumsd) - qk : 0.f;
+                const double bd = (double)bk;
+                double acc = 0.0;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) {
+                    const double bj = __shfl_sync(FULL, bd, j);
+                    if (lane < 6) acc = fma(hw[lane * 6 + j], bj, acc);
+                }
+                dpk = (float)acc;
+            }
+            float dp[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) dp[j] = __shfl_sync(FULL, dpk, j);
+            if (lane == 0) {
+                if (flag == kSuccess) {
+                    if (!update_warp(P, dp, Wm)) {
+                        flag = kSingularWarp;
+                    } else {
+                        // scaled ||dP|| >= delta_p, squared, FP32
+                        const float a1 = dp[1] * (float)g.rx, a2 = dp[2] * (float)g.ry;
+                        const float a4 = dp[4] * (float)g.rx, a5 = dp[5] * (float)g.ry;
+                        const float nrm2 = dp[0] * dp[0] + a1 * a1 + a2 * a2 + dp[3] * dp[3] + a4 * a4 + a5 * a5;
+                        cont = (it + 1 < g.max_iter && nrm2 >= g.delta_p * g.delta_p) ? 1 : 0;
+                    }
+                }
+                if (!(flag == kSuccess && cont)) {
+                    // finish: the counter is it+1 after a solve or an abort in a
+                    // later pass; an abort in the first pass leaves it untouched
+                    jb.flags[p] = (uint8_t)flag;
+                    for (int k = 0; k < 6; ++k) jb.p6[(size_t)p * 6 + k] = P[k];
+                    jb.u[p] = P[0];
+                    jb.v[p] = P[3];
+                    if (flag == kSuccess || it > 0) jb.iters[p] = it + 1;
+                }
+            }
+            cont = __shfl_sync(FULL, (flag == kSuccess && cont) ? 1 : 0, 0);
+            if (!cont) break;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) Wm[k] = __shfl_sync(FULL, Wm[k], 0);
+            ++it;
+        }
+        __syncwarp();  // hw is rewritten by the warp's next POI
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
@@ -591,6 +831,8 @@ static cudaError_t launch_icgn_fast_t(const IcgnJobs& J, int* work, int ctas_per
 }
 
 int icgn_fast_residency(const Geom& g, const IcgnTune& tune) {
+    // one POI per warp: no per-POI shared memory, one residency for all
+    if (tune.chunk > 0 && tune.sampler != kSampWindow && tune.threads >= 128) return 32 * 32 / tune.threads;
     const int S = (2 * g.rx + 1) * (2 * g.ry + 1), ws = icgn_fast_window(g);
     const size_t smem = sizeof(float) * ((size_t)((S + 3) & ~3) + (tune.sampler == kSampWindow ? (size_t)ws * ws : 0));
     const int threads = tune.threads == 32 || tune.threads == 64 || tune.threads == 256 ? tune.threads : 128;
@@ -599,9 +841,64 @@ int icgn_fast_residency(const Geom& g, const IcgnTune& tune) {
     return std::max(1, std::min(std::min(32, by_regs), by_smem));
 }
 
+cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, __half2* grad, cudaStream_t st) {
+    dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
+    k_ref_grad<<<grd, blk, 0, st>>>(g, ref, grad);
+    return cudaGetLastError();
+}
+
+template <int NW, int SAMPLER, bool MULTI>
+static cudaError_t launch_icgn_warp_t(const IcgnJobs& J, int chunk, int ctas_per_sm, cudaStream_t st) {
+    auto kern = k_icgn_warp<NW, SAMPLER, MULTI>;
+    // a few KB of shared memory: leave the rest of the SM's 256 KB to L1
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NW * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
+    if (occ < 1) occ = 1;
+    long long grid = (long long)sms * occ;
+    const long long runs = ((long long)J.total + chunk - 1) / chunk;
+    if (grid > runs) grid = runs;
+    kern<<<(int)grid, NW * 32, 0, st>>>(J, chunk);
+    return cudaGetLastError();
+}
+
+// One POI per warp over a per-reference gradient image: every job needs
+// grad and a table sampler.
+static bool icgn_warp_eligible(const IcgnJobs& J, const IcgnTune& tune) {
+    if (tune.chunk <= 0 || tune.sampler == kSampWindow) return false;
+    if (tune.threads != 128 && tune.threads != 256 && tune.threads != 512 && tune.threads != 1024) return false;
+    for (int j = 0; j < J.njobs; ++j)
+        if (!J.job[j].grad) return false;
+    return true;
+}
+
 cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& tune, cudaStream_t st) {
     if (J.njobs < 1 || J.njobs > kMaxJobs) return cudaErrorInvalidValue;
     if (J.total <= 0) return cudaSuccess;
+    if (icgn_warp_eligible(J, tune)) {
+        for (int j = 0; j < J.njobs; ++j)
+            if (!J.job[j].table) return cudaErrorInvalidValue;
+        const bool multi = J.njobs > 1;
+#define TWDIC_ICGN_WARP(NW, SA)                                                                  \
+    return multi ? launch_icgn_warp_t<NW, SA, true>(J, tune.chunk, tune.ctas_per_sm, st)         \
+                 : launch_icgn_warp_t<NW, SA, false>(J, tune.chunk, tune.ctas_per_sm, st)
+#define TWDIC_ICGN_WARP_N(NW)                                                                    \
+    if (tune.sampler == kSampLut) { TWDIC_ICGN_WARP(NW, kSampLut); }                              \
+    TWDIC_ICGN_WARP(NW, kSampNbhd)
+        if (tune.threads == 128) { TWDIC_ICGN_WARP_N(4); }
+        if (tune.threads == 256) { TWDIC_ICGN_WARP_N(8); }
+        if (tune.threads == 512) { TWDIC_ICGN_WARP_N(16); }
+        TWDIC_ICGN_WARP_N(32);
+#undef TWDIC_ICGN_WARP_N
+#undef TWDIC_ICGN_WARP
+    }
+    if (tune.threads != 32 && tune.threads != 64 && tune.threads != 128 && tune.threads != 256)
+        return cudaErrorInvalidValue;  // one POI per CTA: 32 to 256 threads
     for (int j = 0; j < J.njobs; ++j)
         if (tune.sampler != kSampWindow && !J.job[j].table) return cudaErrorInvalidValue;
     const bool multi = J.njobs > 1;
@@ -623,7 +920,7 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                              const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
-                             const IcgnTune& tune, cudaStream_t st) {
+                             const IcgnTune& tune, cudaStream_t st, const __half2* grad) {
     if (n <= 0) return cudaSuccess;
     IcgnJobs J;
     J.njobs = 1;
@@ -637,6 +934,7 @@ cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* t
     jb.hinv = chol;
     jb.rflag = rflag;
     jb.table = table;
+    jb.grad = grad;
     jb.u = u;
     jb.v = v;
     jb.p6 = p6;

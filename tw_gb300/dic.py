@@ -273,10 +273,18 @@ class DICFrame:
         """INTERP_BICUBIC (Hermite bicubic LUT, default) or INTERP_BSPLINE."""
         check(self._lib.twdic_frame_set_interpolation(self._h, mode))
 
-    def set_tuning(self, icgn_threads=128, icgn_ctas_per_sm=0, icgn_sampler=0, fftcc_use_tc=1):
-        """icgn_sampler: SAMPLER_WINDOW, SAMPLER_LUT or SAMPLER_NBHD."""
+    def set_tuning(self, icgn_threads=128, icgn_ctas_per_sm=0, icgn_sampler=0, fftcc_use_tc=1, icgn_chunk=0):
+        """icgn_sampler: SAMPLER_WINDOW, SAMPLER_LUT or SAMPLER_NBHD;
+        icgn_chunk: the IC-GN work layout (set_icgn_layout; None keeps it)."""
         check(self._lib.twdic_frame_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler,
                                                fftcc_use_tc))
+        if icgn_chunk is not None:
+            self.set_icgn_layout(icgn_chunk)
+
+    def set_icgn_layout(self, chunk):
+        """0: one POI per CTA; > 0: one POI per warp over runs of `chunk`
+        consecutive POIs (threads 128 to 1024, a table sampler)."""
+        check(self._lib.twdic_frame_set_icgn_layout(self._h, chunk))
 
     def set_fftcc_tuning(self, use_tc=1, groups=0, pois_per_group=0):
         check(self._lib.twdic_frame_set_fftcc_tuning(self._h, use_tc, groups, pois_per_group))
@@ -352,8 +360,13 @@ class DICBatch:
         ptr = None if stream is None else ctypes.c_void_p(stream.cuda_stream)
         check(self._lib.twdic_batch_set_stream(self._h, ptr))
 
-    def set_tuning(self, icgn_threads=32, icgn_ctas_per_sm=0, icgn_sampler=2):
+    def set_tuning(self, icgn_threads=1024, icgn_ctas_per_sm=0, icgn_sampler=2, icgn_chunk=32):
         check(self._lib.twdic_batch_set_tuning(self._h, icgn_threads, icgn_ctas_per_sm, icgn_sampler))
+        if icgn_chunk is not None:
+            self.set_icgn_layout(icgn_chunk)
+
+    def set_icgn_layout(self, chunk):
+        check(self._lib.twdic_batch_set_icgn_layout(self._h, chunk))
 
     def process(self, frames, tars, outs):
         """frames: list of DICFrame; tars: their target images; outs: list of

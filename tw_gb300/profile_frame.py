@@ -1,6 +1,7 @@
 """Run a few frames of the 2048x2048 / 41x41-subset workload for profilers.
 
     python -m tw_gb300.profile_frame [--frames 3] [--path fast|plain]
+        [--icgn THREADS:SAMPLER:CHUNK]
 
 Sets the reference once (per-reference precompute), then processes `frames`
 target frames with device-resident buffers and prints the phase times of the
@@ -25,6 +26,7 @@ def main(argv=None):
     ap.add_argument("--frames", type=int, default=3)
     ap.add_argument("--path", default="fast", choices=["fast", "plain"])
     ap.add_argument("--workload", default="2048", choices=["2048", "512"])
+    ap.add_argument("--icgn", default=None, help="IC-GN launch shape threads:sampler:chunk (default: the frame's)")
     args = ap.parse_args(argv)
     pair, g = synth.scale_2048() if args.workload == "2048" else synth.plain_512()
     path = PATH_FAST if args.path == "fast" else PATH_PLAIN
@@ -34,6 +36,10 @@ def main(argv=None):
     with torch.cuda.stream(s):
         fr = dic.DICFrame(prm)
         fr.set_stream(s)
+        if args.icgn:
+            th, sa, ch = (int(x) for x in args.icgn.split(":"))
+            fr.set_tuning(th, 0, sa, 1)
+            fr.set_icgn_layout(ch)
         fr.set_reference(torch.from_numpy(pair.ref).cuda())
         tar = torch.from_numpy(pair.tar).cuda()
         outs = fr.alloc_outputs("cuda")

@@ -18,7 +18,7 @@
 // shift within 2% of the approximate maximum is re-evaluated as the exact
 // integer correlation sum_x f(x) g(x + k) (whose order is the order of the
 // mean-subtracted correlation), with the reference's first-maximum rule.
-// ZNCC is computed from the exact integer sums in FP64.
+// ZNCC is the quotient of the exact integer sums, evaluated in FP32.
 //
 // One CTA of 128 threads (one warpgroup) per SM slot, persistent over POI
 // batches; thread 0 issues the MMAs, completion is signalled through an
@@ -199,7 +199,9 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 __device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast<__half*>(p) = __float2half_rn(v); }
 
 // Optional phase timing (compiled only with -DTWDIC_TC_TRACE): thread 0 of
-// every group adds the clock64() cycles of each phase of each batch.
+// every group adds the clock64() cycles of each phase of each batch; with
+// -DTWDIC_TC_TRACE_ERR as well, slot 14 records the largest error of the
+// approximate surface at any candidate.
 #ifdef TWDIC_TC_TRACE
 __device__ unsigned long long g_tc_trace[16];
 #define TC_MARK(i)                                                           \
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             const long long numg = (long long)n2 * wsum[grp][wg][1] - (long long)wsum[grp][wg][0] * wsum[grp][wg][0];
             const bool dark = b0 + t >= n_job || numf == 0 || numg == 0;
             sdark[grp][t] = dark ? 1 : 0;
-            sscale[grp][t] = dark ? 0.f : (float)((double)n2 / sqrt((double)numf * (double)numg));
+            sscale[grp][t] = dark ? 0.f : (float)n2 * rsqrtf((float)numf) * rsqrtf((float)numg);
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
@@ -662,6 +664,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         const uint32_t mi = __reduce_min_sync(seg, (live && f32_ord(bv) == pv) ? (uint32_t)bi : 0xffffffffu);
         if (live && lane == __ffs(seg) - 1 && mi != 0xffffffffu) atomicMin(&smaxi[grp][p4], (int)mi);
         group_sync(bar_id);
+        TC_MARK(15);
         // candidates: every shift within kCandZncc (ZNCC units; the surface is
         // N^2 ZNCC) of the approximate peak; slot 0 holds the approximate argmax
         {
@@ -671,6 +674,9 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 ps->cand[p4][0] = first;
                 ps->candV[p4][0] = f32_unord(pv);
             }
+            // a row holds a candidate only if its maximum reaches the
+            // threshold: warps with no such row skip the second read
+            if (__any_sync(kFull, live && bv >= th)) {
 #pragma unroll
             for (int y0 = 0; y0 < NP; y0 += 8) {
                 float cv[8];
@@ -689,6 +695,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                         }
                     }
                 }
+            }
             }
         }
         tc_fence_before();
@@ -741,6 +748,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             }
         }
         group_sync(bar_id);
+        TC_MARK(11);
         if (t < PB && b0 + t < n_job) {
             const int gp = b0 + t;
             float* u = jb.u;
@@ -766,12 +774,17 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const long long sf = wsum[grp][2 * t][0], sg = wsum[grp][2 * t + 1][0];
                 const long long numf = (long long)n2 * wsum[grp][2 * t][1] - sf * sf;
                 const long long numg = (long long)n2 * wsum[grp][2 * t + 1][1] - sg * sg;
-                const double cnum = (double)((long long)n2 * bs - sf * sg);
+                // exact integer numerator and norms; the quotient in FP32
+                // (relative error below 5e-7: GB300's FP64 divide and square
+                // root are slow)
+                const long long cnum = (long long)n2 * bs - sf * sg;
                 u[gp] = (float)iu;
                 v[gp] = (float)iv;
-                zncc[gp] = (float)(cnum / sqrt((double)numf * (double)numg));
-#ifdef TWDIC_TC_TRACE
-                // largest error of the approximate surface at the candidates, ZNCC units x 1e6
+                zncc[gp] = (float)cnum * rsqrtf((float)numf) * rsqrtf((float)numg);
+#ifdef TWDIC_TC_TRACE_ERR
+                // largest error of the approximate surface at the candidates,
+                // ZNCC units x 1e6 (a separate switch: its FP64 work would
+                // distort the phase timing)
                 for (int c = 0; c < nc; ++c) {
                     const double zk = (double)((long long)n2 * ps->candS[t][c] - sf * sg) /
                                       sqrt((double)numf * (double)numg);

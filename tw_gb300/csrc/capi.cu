@@ -256,7 +256,7 @@ struct Engine {
         const int2* poi = d_poi.as<int2>();
         if (prm.path == TWDIC_PATH_FAST && fftcc_tune.use_tc && fftcc_tc_supported(g)) {
             TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st,
-                                    d_err.as<unsigned>(), fftcc_tune, stream));
+                                    d_err.as<unsigned>(), d_work.as<int>() + 1, fftcc_tune, stream));
         } else {
             TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, d_tw.as<float2>(), u, v, z,
                                        st, stream));
@@ -1032,13 +1032,13 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             used[m] = true;
             if ((int)jobs.size() == kMaxJobs) {
                 TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
-                                             b->stream));
+                                             b->d_work.as<int>() + 1, b->stream));
                 jobs.clear();
             }
         }
         if (!jobs.empty())
             TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
-                                         b->stream));
+                                         b->d_work.as<int>() + 1, b->stream));
     }
     // target tables, then one persistent IC-GN launch over the fast frames
     for (int i = 0; i < count; ++i) {

@@ -101,9 +101,10 @@ int icgn_fast_residency(const Geom& g, const IcgnTune& tune);
 cudaError_t launch_icgn_fast_jobs(const IcgnJobs& jobs, int* work, const IcgnTune& tune, cudaStream_t st);
 
 // ---- tensor-core FFT-CC (kernels_fftcc_tc.cu)
+// err: error flags; work: one int of scratch (the batch counter, zeroed by the launcher)
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, const FftccTune& tune,
-                            cudaStream_t st);
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
+                            const FftccTune& tune, cudaStream_t st);
 // One image pair of a batched tensor-core FFT-CC launch (all jobs share rx = ry).
 struct FftccJob {
     Geom g;
@@ -116,7 +117,7 @@ struct FftccJob {
     float* zncc;
     uint8_t* status;
 };
-cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err,
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* work,
                                  cudaStream_t st);
 bool fftcc_tc_supported(const Geom& g);
 

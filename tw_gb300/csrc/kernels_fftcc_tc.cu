@@ -227,7 +227,8 @@ __device__ unsigned long long g_tc_trace[16];
 // the MMA that reads the previous one has completed.
 template <int NP, int HP, bool MULTI>
 __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
-                                                                 const uint4* __restrict__ tables, unsigned* err) {
+                                                                 const uint4* __restrict__ tables, unsigned* err,
+                                                                 int* work) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ __align__(8) uint64_t mbar_mma[kMaxGroups];
     __shared__ __align__(8) uint64_t mbar_tma[kMaxGroups];
@@ -240,6 +241,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     __shared__ int smaxi[kMaxGroups][kMaxPB];       // its first index
     __shared__ int2 spoi[kMaxGroups][kMaxPB];
     __shared__ int smis[kMaxGroups][2 * kMaxPB];
+    __shared__ int snext[kMaxGroups];
 
     const int grp = threadIdx.x >> 7;
     const int t = threadIdx.x & 127, warp = t >> 5, lane = t & 31;
@@ -295,7 +297,13 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     long long tmark_ = clock64();
 #endif
 
-    for (int batch = blockIdx.x * s.groups + grp; batch < J.nbatch; batch += gridDim.x * s.groups) {
+    // batches: the first of every group by position, then the next free one
+    // from a launch-wide counter (taken by thread 0 at the start of a batch,
+    // so the atomic's latency is hidden by the batch), which evens out the
+    // groups' finishing times
+    int nxt = 0;
+    for (int batch = blockIdx.x * s.groups + grp; batch < J.nbatch; batch = snext[grp]) {
+        if (t == 0) nxt = gridDim.x * s.groups + atomicAdd(work, 1);
         // the job (image pair, POI set) of this batch: batches of job j are
         // [batch_begin_j, batch_begin_j + ceil(n_j / PB))
         int jj = 0;
@@ -795,6 +803,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 status[gp] = 0;
             }
         }
+        if (t == 0) snext[grp] = nxt;
         group_sync(bar_id);
         TC_MARK(10);
     }
@@ -971,7 +980,7 @@ bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape&
 
 }  // namespace
 
-cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err,
+cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* work,
                                  cudaStream_t st) {
     if (njobs < 1 || njobs > kMaxJobs) return cudaErrorInvalidValue;
     TcShape s;
@@ -1010,7 +1019,7 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    void (*kern)(const TcJobs, TcShape, const uint4*, unsigned*) = nullptr;
+    void (*kern)(const TcJobs, TcShape, const uint4*, unsigned*, int*) = nullptr;
     const bool multi = njobs > 1;
 #define TWDIC_TC_CASE(NPV, HPV)                                                   \
     case NPV * 100 + HPV:                                                         \
@@ -1038,16 +1047,18 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     int occ = 1;
     if (s.groups == 1 && 2 * (s.smem_bytes + 2048) <= 228 * 1024) occ = 2;
     const int grid = std::max(1, std::min(sms * occ, (nb + s.groups - 1) / s.groups));
-    kern<<<grid, threads, s.smem_bytes, st>>>(*J, s, tables, err);
+    e = cudaMemsetAsync(work, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, threads, s.smem_bytes, st>>>(*J, s, tables, err, work);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, const FftccTune& tune,
-                            cudaStream_t st) {
+                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
+                            const FftccTune& tune, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     FftccJob job{g, ref, tar, poi, n, u, v, zncc, status};
-    return launch_fftcc_tc_jobs(&job, 1, tune, err, st);
+    return launch_fftcc_tc_jobs(&job, 1, tune, err, work, st);
 }
 
 }  // namespace twdic

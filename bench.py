@@ -336,7 +336,7 @@ def _run_gpu(args, world, rank, local, torch):
             "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(pair.tar.nbytes),
                     "d2h_bytes_per_step": d2h, "p50_ms": round(pct(e2e_ms, 50), 4),
                     "p99_ms": round(pct(e2e_ms, 99), 4)},
-            # per frame: k_fftcc_tc, k_bicubic_lut, k_icgn_fast
+            # per frame: k_fftcc_tc, k_nbhd_table, k_icgn_warp
             "gpu_launches": 3 * args.steps,
             "clocks": clk,
             "wall_s_timed_region": round(t_wall, 3)}
@@ -357,28 +357,29 @@ def _run_gpu(args, world, rank, local, torch):
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
-# profiles/k_icgn_fast_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
-NCU_TRAFFIC = {"k_icgn_fast": 111.91e6 + 5.94e6, "k_fftcc_tc": 9.65e6 + 0.0}
-# L2 -> SM bandwidth implied by an ncu capture of the float-LUT IC-GN sampler (53.78 GB in
-# 4.119 ms at 53.6 % of the L2 throughput peak); there is no measured L2 peak
-L2_PEAK_GBS_NCU = 53.78e9 / 4.119e-3 / 0.536 / 1e9
+# profiles/k_icgn_warp_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
+NCU_TRAFFIC = {"k_icgn_warp": 123.79e6 + 7.68e6, "k_fftcc_tc": 9.61e6 + 0.0}
+# from the same IC-GN capture: L1 hit rate of its gathers and the FMA-heavy
+# pipe's share of cycles (the kernel's limiter)
+NCU_ICGN_L1_HIT = 0.872
+NCU_ICGN_FMAHEAVY = 0.666
 
 
 def roofline(g, P, ph, kbar):
-    """Roofline of the dominant kernel, the fast IC-GN (k_icgn_fast), timed by
-    the per-phase CUDA events of the frame (the IC-GN phase holds that kernel
-    and the memset of its work counter).
+    """Roofline of the dominant kernel, the fast IC-GN (k_icgn_warp), timed by
+    the per-phase CUDA events of the frame.
 
     HBM view (the one reported as `frac`): algorithmic bytes per launch are
     the compulsory ones -- the target's 4x4 neighbourhood table read once
-    (16 B per ROI pixel), both
-    images once, and per POI the reference cache entry (statistics 64 B, FP64
-    inverse Hessian 168 B, flag 1 B), the POI (8 B), u/v in (8 B) and out
-    (8 B), p6 (24 B), iteration count (4 B) and flag (1 B).  The kernel is not
-    HBM bound: its gathers of the table are served by L2, so the L2 view below
-    (k*S*16 B of table gathers per POI, k = mean iterations) and the FP32 view
-    (k*S*64 flops per POI) are reported beside it, with the tensor-core view of
-    the FFT-CC kernel (48 N^3 flops per POI)."""
+    (16 B per ROI pixel), the per-reference gradient image (4 B per ROI
+    pixel), the target image once, and per POI the reference cache entry
+    (statistics 64 B, FP64 inverse Hessian 168 B, flag 1 B), the POI (8 B),
+    u/v in (8 B) and out (8 B), p6 (24 B), iteration count (4 B) and flag
+    (1 B).  The kernel is not HBM bound: its per-sample gathers (k*S*20 B per
+    POI, k = mean iterations) are served by L1 (87 % hits) and L2, and it is
+    limited by the SM's FP32 / integer pipes (FMA-heavy pipe busy 67 % of
+    cycles); the gather and FP32 views are reported beside it, with the
+    tensor-core view of the FFT-CC kernel (48 N^3 flops per POI)."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -392,26 +393,26 @@ def roofline(g, P, ph, kbar):
     t_icgn = ph["icgn"] / 1000.0
     t_fftcc = ph["fftcc"] / 1000.0
     per_poi = 64 + 168 + 1 + 8 + 8 + 8 + 24 + 4 + 1
-    bytes_icgn = P * per_poi + 16 * g.roi_w * g.roi_h + 2 * g.img_w * g.img_h
+    bytes_icgn = P * per_poi + (16 + 4) * g.roi_w * g.roi_h + g.img_w * g.img_h
     achieved = bytes_icgn / t_icgn / 1e9
-    gather = kbar * S * 16 * P
+    gather = kbar * S * 20 * P
     flops_fftcc = 48 * N ** 3 * P
     fft_tflops = flops_fftcc / t_fftcc / 1e12
-    return {"kernel": "k_icgn_fast (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
-            "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": NCU_TRAFFIC["k_icgn_fast"],
+    return {"kernel": "k_icgn_warp (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
+            "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": NCU_TRAFFIC["k_icgn_warp"],
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)",
             "algorithmic_bytes_per_launch": int(bytes_icgn), "kernel_ms": round(ph["icgn"], 4),
-            "l2_view": {"gather_bytes_per_launch": int(gather), "achieved_gbs": round(gather / t_icgn / 1e9, 1),
-                        "peak_gbs": round(L2_PEAK_GBS_NCU, 1),
-                        "frac": round(gather / t_icgn / 1e9 / L2_PEAK_GBS_NCU, 4),
-                        "peak_source": "implied by the ncu capture (no measured L2 peak)"},
+            "gather_view": {"gather_bytes_per_launch": int(gather), "achieved_gbs": round(gather / t_icgn / 1e9, 1),
+                            "l1_hit_rate_ncu": NCU_ICGN_L1_HIT},
             "fp32_view": {"flops_per_launch": int(kbar * S * 64 * P),
-                          "achieved_tflops": round(kbar * S * 64 * P / t_icgn / 1e12, 2)},
+                          "achieved_tflops": round(kbar * S * 64 * P / t_icgn / 1e12, 2),
+                          "fmaheavy_pipe_busy_ncu": NCU_ICGN_FMAHEAVY},
             "fftcc_tensor_view": {"kernel": "k_fftcc_tc", "flops_per_launch": int(flops_fftcc),
                                   "achieved_tflops": round(fft_tflops, 2), "peak_tflops": tc,
                                   "frac": round(fft_tflops / tc, 4), "kernel_ms": round(ph["fftcc"], 4),
                                   "traffic": NCU_TRAFFIC["k_fftcc_tc"]},
-            "note": "frac is against HBM; the IC-GN kernel is bound by L2 gather latency and issue, see l2_view"}
+            "note": "frac is against HBM; the IC-GN kernel is bound by the SM's FP32/integer pipes "
+                    "(gathers served by L1), see gather_view and fp32_view"}
 
 
 def main(argv=None):

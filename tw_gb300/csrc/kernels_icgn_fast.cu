@@ -597,10 +597,12 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ int s_next;
     __shared__ double s_h[NW][36];  // rows of H^-1 of each warp's POI
+    __shared__ float s_p[NW][6];     // each warp's warp parameters P (lane 0)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (threadIdx.x == 0) s_next = 0;
     __syncthreads();
     double* hw = s_h[wid];
+    float* pw = s_p[wid];
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(&s_next, 1);
@@ -625,22 +627,24 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
         const int py = pyx.x, px = pyx.y;
         const float u0 = jb.u[p], v0 = jb.v[p];
         const uint8_t rf = jb.rflag[p];
-        float P[6] = {u0, 0.f, 0.f, v0, 0.f, 0.f};  // maintained by lane 0
         float Wm[6] = {1.f, 0.f, u0, 0.f, 1.f, v0};
         if (rf == kDarkSubset || rf == kOutofROI) {
             if (lane == 0) {
                 jb.flags[p] = rf;
-                for (int k = 0; k < 6; ++k) jb.p6[(size_t)p * 6 + k] = P[k];
+                const float P0[6] = {u0, 0.f, 0.f, v0, 0.f, 0.f};
+                for (int k = 0; k < 6; ++k) jb.p6[(size_t)p * 6 + k] = P0[k];
             }
             continue;
         }
-        // lane k < 6: row k of H^-1 (FP64), sum SD_k and sum SD_k (R - mean)
+        // P in shared memory (lane 0 updates it); lane k < 6: row k of H^-1
+        // (FP64); the statistics are re-read at each solve, not held in
+        // registers through the sample loop
+        if (lane == 0) {
+            pw[0] = u0; pw[1] = 0.f; pw[2] = 0.f; pw[3] = v0; pw[4] = 0.f; pw[5] = 0.f;
+        }
         const float* st = jb.stats + (size_t)p * 16;
-        const float c = st[0], rs = st[1];
-        float sumsd = 0.f, qk = 0.f;
+        const float c = st[0];
         if (lane < 6) {
-            sumsd = st[2 + lane];
-            qk = st[8 + lane];
             const double* hi = jb.hinv + (size_t)p * 21;
 #pragma unroll
             for (int j = 0; j < 6; ++j) hw[lane * 6 + j] = hi[lane >= j ? tri(lane, j) : tri(j, lane)];
@@ -737,7 +741,8 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
             }
             float dpk = 0.f;
             if (flag == kSuccess) {
-                const float q = rs / ts;
+                const float q = st[1] / ts;  // ||R - mean(R)|| / ||T - mean(T)||
+                const float sumsd = lane < 6 ? st[2 + lane] : 0.f, qk = lane < 6 ? st[8 + lane] : 0.f;
                 const float bk = (lane < 6) ? q * (Ak - m0 * sumsd) - qk : 0.f;
                 const double bd = (double)bk;
                 double acc = 0.0;
@@ -752,6 +757,9 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
 #pragma unroll
             for (int j = 0; j < 6; ++j) dp[j] = __shfl_sync(FULL, dpk, j);
             if (lane == 0) {
+                float P[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) P[k] = pw[k];
                 if (flag == kSuccess) {
                     if (!update_warp(P, dp, Wm)) {
                         flag = kSingularWarp;
@@ -772,6 +780,8 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                     jb.v[p] = P[3];
                     if (flag == kSuccess || it > 0) jb.iters[p] = it + 1;
                 }
+#pragma unroll
+                for (int k = 0; k < 6; ++k) pw[k] = P[k];
             }
             cont = __shfl_sync(FULL, (flag == kSuccess && cont) ? 1 : 0, 0);
             if (!cont) break;

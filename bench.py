@@ -411,8 +411,47 @@ def roofline(g, P, ph, kbar):
                                   "achieved_tflops": round(fft_tflops, 2), "peak_tflops": tc,
                                   "frac": round(fft_tflops / tc, 4), "kernel_ms": round(ph["fftcc"], 4),
                                   "traffic": NCU_TRAFFIC["k_fftcc_tc"]},
+            "frame_roofline": frame_roofline(g, P, ph, kbar, peaks, bytes_icgn),
             "note": "frac is against HBM; the IC-GN kernel is bound by the SM's FP32/integer pipes "
                     "(gathers served by L1), see gather_view and fp32_view"}
+
+
+def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
+    """Frame-level bound T_roof = P F_a / Peak_TC + max(P F_c / Peak_FP32,
+    B_compulsory / Peak_HBM) with F_a = 48 N^3 (FFT-CC, credited flops only)
+    and F_c = k S 64 (IC-GN); achieved = T_roof / T_measured.  B_compulsory is
+    this design's: both images, the neighbourhood table and gradient image,
+    and the per-POI cache and outputs.  (A 64 B/px coefficient LUT and S*28 B
+    of per-POI reference data, the reference's layout, are never moved here,
+    so they are not in the bound.)  Peak_FP32 is not in MEASURED_PEAKS.json:
+    it is 128 FP32 lanes x 2 flops per SM and clock at the measured maximum SM
+    clock."""
+    N = 2 * g.subset_r
+    S = (2 * g.subset_r + 1) ** 2
+    sms = 152
+    try:
+        import torch
+        if torch.cuda.is_available():
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    peak_tc = peaks.get("bf16_tflops", 1900.0) * 1e12
+    peak_fp32 = sms * 128 * 2 * sm_mhz * 1e6
+    peak_hbm = peaks.get("hbm_gbs", 6800.0) * 1e9
+    t_tc = P * 48 * N ** 3 / peak_tc
+    t_fp32 = P * kbar * S * 64 / peak_fp32
+    b_comp = bytes_icgn + 2 * g.img_w * g.img_h  # IC-GN's bytes plus FFT-CC's image reads
+    t_hbm = b_comp / peak_hbm
+    t_roof = t_tc + max(t_fp32, t_hbm)
+    t_meas = (ph["fftcc"] + ph["prepare"] + ph["icgn"]) / 1000.0
+    return {"t_roof_ms": round(t_roof * 1e3, 4), "t_measured_ms": round(t_meas * 1e3, 4),
+            "achieved": round(t_roof / t_meas, 4),
+            "terms_ms": {"fftcc_tensor": round(t_tc * 1e3, 4), "icgn_fp32": round(t_fp32 * 1e3, 4),
+                         "hbm_compulsory": round(t_hbm * 1e3, 4)},
+            "peaks": {"tensor_tflops": peak_tc / 1e12, "fp32_tflops": round(peak_fp32 / 1e12, 1),
+                      "hbm_gbs": peak_hbm / 1e9,
+                      "fp32_source": f"{sms} SMs x 128 lanes x 2 flops x {sm_mhz:.0f} MHz (derived, not measured)"}}
 
 
 def main(argv=None):

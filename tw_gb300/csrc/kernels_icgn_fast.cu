@@ -250,6 +250,33 @@ struct PassSums {
     }
 };
 
+// The eight sums of a warp by recursive halving: each exchange sends half of
+// the values still held and adds the received half, so after the exchanges
+// at lane distances 16, 8 and 4 a lane holds partial sums of one value, and
+// two butterfly steps finish it.  Lane l returns sum number (l >> 2) & 7
+// (12 shuffles instead of 40).
+__device__ __forceinline__ float warp_reduce8(const float* s) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    float t4[4], t2[2];
+    const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float keep = b16 ? s[i + 4] : s[i], send = b16 ? s[i] : s[i + 4];
+        t4[i] = keep + __shfl_xor_sync(FULL, send, 16);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float keep = b8 ? t4[i + 2] : t4[i], send = b8 ? t4[i] : t4[i + 2];
+        t2[i] = keep + __shfl_xor_sync(FULL, send, 8);
+    }
+    const float keep = b4 ? t2[1] : t2[0], send = b4 ? t2[0] : t2[1];
+    float v = keep + __shfl_xor_sync(FULL, send, 4);
+    v += __shfl_xor_sync(FULL, v, 2);
+    v += __shfl_xor_sync(FULL, v, 1);
+    return v;
+}
+
 // Catmull-Rom weights (the Hermite bicubic with central differences).
 __device__ __forceinline__ void cr_weights(float t, float& w0, float& w1, float& w2, float& w3) {
     const float t2 = t * t;
@@ -494,12 +521,8 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                 }
                 ps.unpack(s);
                 // ---- one reduction (FP32)
-#pragma unroll
-                for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
-                if (lane == 0) {
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) red[wid][k] = s[k];
-                }
+                const float v8 = warp_reduce8(s);
+                if ((lane & 3) == 0) red[wid][(lane >> 2) & 7] = v8;
                 __syncthreads();
             }
             // ---- warp 0 finishes the iteration: FP32 scalars, FP64 H^-1 b on
@@ -661,7 +684,8 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
         for (;;) {
             const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
             const bool oor = pass_out_of_roi(g, Wm, bx, by);
-            float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float s[8];
+            float v8 = 0.f;
             if (!oor) {
                 PassSums ps;
                 float2 d = d_first;
@@ -720,13 +744,12 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                     }
                 }
                 ps.unpack(s);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) s[k] = warp_sum(s[k]);
+                v8 = warp_reduce8(s);
             }
-            // FP32 scalars, FP64 H^-1 b on lanes 0-5, warp update on lane 0
-            const float S0 = s[0], S1 = s[1];
-            const float Ak = lane == 0 ? s[2] : lane == 1 ? s[3] : lane == 2 ? s[4] : lane == 3 ? s[5]
-                           : lane == 4 ? s[6] : s[7];
+            // FP32 scalars, FP64 H^-1 b on lanes 0-5, warp update on lanes 0-5;
+            // sum k is held by lanes 4k .. 4k+3
+            const float S0 = __shfl_sync(FULL, v8, 0), S1 = __shfl_sync(FULL, v8, 4);
+            const float Ak = __shfl_sync(FULL, v8, 8 + 4 * (lane < 6 ? lane : 0));
             const float m0 = S0 * inv_s;
             const float mean_t = c + m0;
             const float var = S1 - S0 * m0;
@@ -756,14 +779,45 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
             float dp[6];
 #pragma unroll
             for (int j = 0; j < 6; ++j) dp[j] = __shfl_sync(FULL, dpk, j);
+            // W(P) o W(dP)^-1 (update_warp's operations), coefficient k on lane k:
+            // w_k = base_k + (x_k y_k - z_k v_k) / det
+            bool singular = false;
+            float wk = 0.f;
+            if (flag == kSuccess) {
+                const float P0 = pw[0], P1 = pw[1], P2 = pw[2], P3 = pw[3], P4 = pw[4], P5 = pw[5];
+                const float det = __fsub_rn(__fmul_rn(1.f + dp[1], 1.f + dp[5]), __fmul_rn(dp[2], dp[4]));
+                singular = fabsf(det) <= FLT_EPSILON;
+                if (!singular && lane < 6) {
+                    const float a = __fsub_rn(__fsub_rn(__fmul_rn(dp[0], dp[4]), dp[3]), __fmul_rn(dp[3], dp[1]));
+                    const float b = __fsub_rn(__fadd_rn(__fmul_rn(dp[0], dp[5]), dp[0]), __fmul_rn(dp[2], dp[3]));
+                    const int r3 = lane % 3;  // 0: (1+d5, d4), 1: (1+d1, d2), 2: (a, b)
+                    const float y = r3 == 0 ? 1.f + dp[5] : (r3 == 1 ? 1.f + dp[1] : a);
+                    const float v = r3 == 0 ? dp[4] : (r3 == 1 ? dp[2] : b);
+                    const float x = lane == 0 ? 1.f + P1 : (lane <= 2 ? P2 : (lane == 3 ? P4 : 1.f + P5));
+                    const float z = lane == 0 ? P2 : (lane <= 2 ? 1.f + P1 : (lane == 3 ? 1.f + P5 : P4));
+                    const float q = __fdiv_rn(__fsub_rn(__fmul_rn(x, y), __fmul_rn(z, v)), det);
+                    wk = lane == 2 ? __fadd_rn(P0, q) : (lane == 5 ? __fadd_rn(P3, q) : q);
+                }
+            }
+            float Wn[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) Wn[j] = __shfl_sync(FULL, wk, j);
             if (lane == 0) {
                 float P[6];
 #pragma unroll
                 for (int k = 0; k < 6; ++k) P[k] = pw[k];
                 if (flag == kSuccess) {
-                    if (!update_warp(P, dp, Wm)) {
+                    if (singular) {
                         flag = kSingularWarp;
                     } else {
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) Wm[k] = Wn[k];
+                        P[0] = Wn[2];
+                        P[1] = Wn[0] - 1.f;
+                        P[2] = Wn[1];
+                        P[3] = Wn[5];
+                        P[4] = Wn[3];
+                        P[5] = Wn[4] - 1.f;
                         // scaled ||dP|| >= delta_p, squared, FP32
                         const float a1 = dp[1] * (float)g.rx, a2 = dp[2] * (float)g.ry;
                         const float a4 = dp[4] * (float)g.rx, a5 = dp[5] * (float)g.ry;
@@ -785,8 +839,10 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
             }
             cont = __shfl_sync(FULL, (flag == kSuccess && cont) ? 1 : 0, 0);
             if (!cont) break;
+            // every lane has the new warp; lane 0's P is read by all at the next update
 #pragma unroll
-            for (int k = 0; k < 6; ++k) Wm[k] = __shfl_sync(FULL, Wm[k], 0);
+            for (int k = 0; k < 6; ++k) Wm[k] = Wn[k];
+            __syncwarp();
             ++it;
         }
         __syncwarp();  // hw is rewritten by the warp's next POI

@@ -314,6 +314,16 @@ __device__ __forceinline__ bool pass_out_of_roi(const Geom& g, const float* Wm, 
     return out;
 }
 
+// The same test with one corner per lane (lanes 0-3) and a warp vote.
+__device__ __forceinline__ bool pass_out_of_roi_warp(const Geom& g, const float* Wm, float bx, float by) {
+    const int lane = threadIdx.x & 31, c = lane & 3;
+    const float rx = (float)g.rx, ry = (float)g.ry;
+    const float dx = (c & 1) ? rx : -rx, dy = (c & 2) ? ry : -ry;
+    const int ix = (int)warp_x(Wm, bx, dx, dy), iy = (int)warp_y(Wm, by, dx, dy);
+    const bool out = lane < 4 && ((unsigned)(ix - g.sx) >= (unsigned)g.rw || (unsigned)(iy - g.sy) >= (unsigned)g.rh);
+    return __any_sync(0xffffffffu, out);
+}
+
 // Persistent IC-GN kernel, one POI per CTA at a time.  The target sampler:
 //   kSampWindow: the target window around the guess is staged in shared
 //     memory and interpolated with the separable Catmull-Rom weights;
@@ -683,7 +693,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
         int it = 0;
         for (;;) {
             const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
-            const bool oor = pass_out_of_roi(g, Wm, bx, by);
+            const bool oor = pass_out_of_roi_warp(g, Wm, bx, by);
             float s[8];
             float v8 = 0.f;
             if (!oor) {

@@ -229,6 +229,27 @@ def test_fftcc_radii_parity(r):
         assert rep.ok(), (r, path, rep)
 
 
+@pytest.mark.parametrize("r", [8, 15, 20, 31])
+def test_fftcc_twiddle_precisions_agree(r):
+    """Single FP16 twiddles (the default) and hi + lo twiddles give the same
+    integer displacements, ZNCC and everything downstream: the candidates of
+    either approximate surface are re-evaluated in exact integers."""
+    pair, g = synth.small_case(h=150, w=170, r=r, grid=9, seed=200 + r)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    if nx <= 0 or ny <= 0:
+        pytest.skip("no POI at this radius")
+    outs = []
+    for hi_lo in (0, 1):
+        fr = dic.DICFrame(params_of(g, PATH_FAST))
+        fr.set_fftcc_twiddles(hi_lo)
+        fr.set_reference(pair.ref)
+        o = fr.alloc_outputs()
+        fr.process(pair.tar, **o)
+        outs.append(o)
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+
+
 def test_fftcc_dark_subset_untouched(small):
     pair, g, _, _ = small
     ref = np.full_like(pair.ref, 50)

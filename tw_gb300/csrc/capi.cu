@@ -726,6 +726,12 @@ int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int poi
     return TWDIC_OK;
 }
 
+int twdic_frame_set_fftcc_twiddles(twdic_frame* h, int hi_lo) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    h->e.fftcc_tune.twiddle_lo = hi_lo ? 1 : 0;
+    return TWDIC_OK;
+}
+
 int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out) {
     if (!h || !out) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
     std::memset(out, 0, sizeof(*out));
@@ -843,6 +849,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
                 c.use_tc = 1;
                 c.groups = groups;
                 c.pois_per_group = ppg;
+                c.twiddle_lo = fft0.twiddle_lo;  // the precision stays the caller's choice
                 e.fftcc_tune = c;
                 float f = 0, ic = 0;
                 const int rc = measure(&f, &ic);

@@ -61,6 +61,7 @@ struct FftccTune {
     int use_tc = 1;          // 0: FP32 SIMT DFT kernel
     int groups = 0;          // tensor-core kernel: 128-thread groups per CTA (0 = as many as fit, up to 4)
     int pois_per_group = 0;  // POIs per group batch (0 = the most the tiles hold)
+    int twiddle_lo = 0;      // 1: FP16 hi + lo twiddles (two MMAs per product), 0: hi only
 };
 
 // ---- plain FP32 path (kernels_plain.cu)

@@ -12,12 +12,13 @@
 // Every stage is D[128 x n] += A[128 x k] B[k x n] with the data as A
 // (rows = window rows / spectrum rows of several POIs, K-major in shared
 // memory) and constant twiddle matrices as B (K-major), FP16 operands, FP32
-// accumulators in tensor memory.  Twiddles are split hi + lo (two MMAs); the
-// data operands are single FP16.  The resulting surface is accurate to
-// ~1e-3 of its range, so the integer peak is then decided exactly: every
-// shift within 2% of the approximate maximum is re-evaluated as the exact
-// integer correlation sum_x f(x) g(x + k) (whose order is the order of the
-// mean-subtracted correlation), with the reference's first-maximum rule.
+// accumulators in tensor memory.  Twiddles are single FP16 by default, or
+// split hi + lo (two MMAs per product); the data operands are single FP16.
+// The resulting surface is accurate to ~1e-3 in ZNCC units, so the integer
+// peak is then decided exactly: every shift within kCandZncc of the
+// approximate maximum is re-evaluated as the exact integer correlation
+// sum_x f(x) g(x + k) (whose order is the order of the mean-subtracted
+// correlation), with the reference's first-maximum rule.
 // ZNCC is the quotient of the exact integer sums, evaluated in FP32.
 //
 // One CTA of 128 threads (one warpgroup) per SM slot, persistent over POI
@@ -48,8 +49,9 @@ constexpr int kMaxGroups = 4;     // 128-thread groups per CTA (upper bound)
 // Candidate window of the approximate correlation surface, in ZNCC units.
 // The exact peak lies within twice the surface's error of the approximate
 // maximum; the largest error measured at any evaluated candidate on the
-// 2048x2048 / r = 20 workload (155,236 POIs) is 4.7e-4 (FP16 operands,
-// FP32 accumulation), so 0.01 keeps a tenfold margin.
+// 2048x2048 / r = 20 workload (155,236 POIs, FP16 operands, FP32
+// accumulation) is 8.9e-4 with single FP16 twiddles and 4.7e-4 with hi + lo
+// twiddles, so 0.01 keeps a margin of five or more.
 constexpr float kCandZncc = 0.01f;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
@@ -58,6 +60,7 @@ constexpr unsigned kWaitLimit = 1u << 24;
 struct TcShape {
     int N, H, HP, NP, PB, tiles1, K4, BW, WS, groups;
     int NW4;  // 32-bit words per window row in the exact re-evaluation
+    int lo;   // 1: twiddles as FP16 hi + lo (two MMAs per product), 0: hi only
     // shared twiddle tables
     int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
     // per-group operand regions, relative to the group's base
@@ -225,7 +228,7 @@ __device__ unsigned long long g_tc_trace[16];
 // latency overlaps other groups' epilogues.  A group's GEMM operands A1, A2,
 // A3, A4 and its peak scratch share one region: each is written only after
 // the MMA that reads the previous one has completed.
-template <int NP, int HP, bool MULTI>
+template <int NP, int HP, bool MULTI, bool LO>
 __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
                                                                  const uint4* __restrict__ tables, unsigned* err,
                                                                  int* work) {
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                     const uint64_t bh = sdesc(sbase + s.off_b1h + kk * 256, 128, 16 * K1);
                     const uint64_t bl = sdesc(sbase + s.off_b1l + kk * 256, 128, 16 * K1);
                     mma_f16(tm + tile * 2 * HP, a, bh, idesc_f16(2 * HP, false), kk > 0);
-                    mma_f16(tm + tile * 2 * HP, a, bl, idesc_f16(2 * HP, false), 1);
+                    if (LO) mma_f16(tm + tile * 2 * HP, a, bl, idesc_f16(2 * HP, false), 1);
                 }
             }
             mma_commit(mbar);
@@ -475,13 +478,13 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const uint64_t sl = sdesc(sbase + s.off_s2l + kk * 256, 128, 16 * NP);
                 const uint32_t acc = kk > 0;
                 mma_f16(tm, ar, ch, idesc_f16(NP, false), acc);  // Re = Yr cos + Yi sin
-                mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
                 mma_f16(tm, ai, sh, idesc_f16(NP, false), 1);
-                mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
                 mma_f16(tm + NP, ar, sh, idesc_f16(NP, true), acc);  // Im = -Yr sin + Yi cos
-                mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
+                if (LO) mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
                 mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
-                mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
             }
             mma_commit(mbar);
         }
@@ -562,13 +565,13 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const uint64_t sl = sdesc(sbase + s.off_s2l + kk * 256, 128, 16 * NP);
                 const uint32_t acc = kk > 0;
                 mma_f16(tm, ar, ch, idesc_f16(NP, false), acc);
-                mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm, ar, cl, idesc_f16(NP, false), 1);
                 mma_f16(tm, ai, sh, idesc_f16(NP, false), 1);
-                mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm, ai, sl, idesc_f16(NP, false), 1);
                 mma_f16(tm + NP, ar, sh, idesc_f16(NP, true), acc);
-                mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
+                if (LO) mma_f16(tm + NP, ar, sl, idesc_f16(NP, true), 1);
                 mma_f16(tm + NP, ai, ch, idesc_f16(NP, false), 1);
-                mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm + NP, ai, cl, idesc_f16(NP, false), 1);
             }
             mma_commit(mbar);
         }
@@ -633,7 +636,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
                 const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
                 mma_f16(tm, a, bh, idesc_f16(NP, false), kk > 0);
-                mma_f16(tm, a, bl, idesc_f16(NP, false), 1);
+                if (LO) mma_f16(tm, a, bl, idesc_f16(NP, false), 1);
             }
             mma_commit(mbar);
         }
@@ -856,6 +859,7 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     // peak scratch, then the windows
     s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
     s.NW4 = (N + 3) / 4;
+    s.lo = tune.twiddle_lo ? 1 : 0;
     const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 16 * K4;
     const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
                                 128);
@@ -1021,9 +1025,12 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void (*kern)(const TcJobs, TcShape, const uint4*, unsigned*, int*) = nullptr;
     const bool multi = njobs > 1;
-#define TWDIC_TC_CASE(NPV, HPV)                                                   \
-    case NPV * 100 + HPV:                                                         \
-        kern = multi ? k_fftcc_tc<NPV, HPV, true> : k_fftcc_tc<NPV, HPV, false>; \
+#define TWDIC_TC_CASE(NPV, HPV)                                                                      \
+    case NPV * 100 + HPV:                                                                            \
+        if (s.lo)                                                                                    \
+            kern = multi ? k_fftcc_tc<NPV, HPV, true, true> : k_fftcc_tc<NPV, HPV, false, true>;     \
+        else                                                                                         \
+            kern = multi ? k_fftcc_tc<NPV, HPV, true, false> : k_fftcc_tc<NPV, HPV, false, false>;   \
         break;
     switch (s.NP * 100 + s.HP) {
         TWDIC_TC_CASE(16, 8)

@@ -286,6 +286,10 @@ class DICFrame:
         consecutive POIs (threads 128 to 1024, a table sampler)."""
         check(self._lib.twdic_frame_set_icgn_layout(self._h, chunk))
 
+    def set_fftcc_twiddles(self, hi_lo):
+        """1: FP16 hi + lo twiddles in the tensor-core FFT-CC, 0: hi only."""
+        check(self._lib.twdic_frame_set_fftcc_twiddles(self._h, hi_lo))
+
     def set_fftcc_tuning(self, use_tc=1, groups=0, pois_per_group=0):
         check(self._lib.twdic_frame_set_fftcc_tuning(self._h, use_tc, groups, pois_per_group))
 

@@ -203,6 +203,9 @@ TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_
  * so the subsets in flight on an SM overlap and are re-read from L1, and the
  * reference gradients come from a per-reference image (4 B per ROI pixel). */
 TWDIC_API int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk);
+/* Unrolling of the IC-GN sample loop (2, 4 or 8; default 8) for the one-POI-per-warp
+ * layout with 1024-thread CTAs (other shapes unroll by 4). */
+TWDIC_API int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll);
 
 /* FFT-CC tile of a frame handle: use_tc (tensor-core kernel), groups (0 = as
  * many 128-thread groups per CTA as fit, 1 = one), pois_per_group (POIs per
@@ -223,10 +226,11 @@ typedef struct {
     float fftcc_ms, icgn_ms; /* phase times of the chosen shapes (target preparation included in icgn_ms) */
     int32_t from_cache;      /* 1: read from the cache file, not measured */
     int32_t icgn_chunk;      /* IC-GN work layout (twdic_frame_set_icgn_layout) */
+    int32_t icgn_unroll;     /* IC-GN sample-loop unrolling (twdic_frame_set_icgn_unroll) */
 } twdic_tuning;
 TWDIC_API int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out);
 /* Autotuner (no reference counterpart): times the FFT-CC tile shapes and the
- * IC-GN launch shapes and samplers on this handle's reference and the given
+ * IC-GN launch shapes, samplers and sample-loop unrolling on this handle's reference and the given
  * target (one warm-up and three timed frames each, median), keeps the fastest
  * and returns it.  cache_path (may be NULL): a text file of earlier choices
  * keyed by GPU name, SM count and every geometry parameter; a hit is applied
@@ -288,6 +292,8 @@ TWDIC_API int twdic_batch_set_stream(twdic_batch* b, void* stream);
 TWDIC_API int twdic_batch_set_tuning(twdic_batch* b, int icgn_threads, int icgn_ctas_per_sm, int icgn_sampler);
 /* IC-GN work layout of the batch's launches (twdic_frame_set_icgn_layout). */
 TWDIC_API int twdic_batch_set_icgn_layout(twdic_batch* b, int chunk);
+/* IC-GN sample-loop unrolling of the batch's launches (twdic_frame_set_icgn_unroll). */
+TWDIC_API int twdic_batch_set_icgn_unroll(twdic_batch* b, int unroll);
 TWDIC_API int twdic_batch_set_graph(twdic_batch* b, int enable);
 /* Arrays of `count` entries; zncc, p6, iters, flags (the arrays) may be NULL,
  * strides may be NULL (contiguous images); replayed may be NULL. */

@@ -45,7 +45,7 @@ def test_autotune_choice_meets_parity_and_is_cached(tmp_path):
     f.set_reference(pair.ref)
     t = f.autotune(pair.tar, cache_path=cache)
     assert t["from_cache"] == 0 and t["icgn_threads"] in (32, 64, 128, 256, 512, 1024)
-    assert t["icgn_sampler"] in (0, 1, 2) and t["icgn_chunk"] in (0, 32, 64)
+    assert t["icgn_sampler"] in (0, 1, 2) and t["icgn_chunk"] in (0, 32, 64) and t["icgn_unroll"] in (2, 4, 8)
     assert t["icgn_ms"] > 0 and t["fftcc_ms"] > 0
     assert f.tuning()["icgn_threads"] == t["icgn_threads"]
     o = f.alloc_outputs()
@@ -59,6 +59,6 @@ def test_autotune_choice_meets_parity_and_is_cached(tmp_path):
     f2.set_reference(pair.ref)
     t2 = f2.autotune(pair.tar, cache_path=cache)
     assert t2["from_cache"] == 1
-    for k in ("icgn_threads", "icgn_sampler", "icgn_chunk", "fftcc_groups", "fftcc_pois_per_group"):
+    for k in ("icgn_threads", "icgn_sampler", "icgn_chunk", "icgn_unroll", "fftcc_groups", "fftcc_pois_per_group"):
         assert t2[k] == t[k]
     assert len(cache.read_text().strip().splitlines()) == 1

@@ -124,12 +124,14 @@ def test_warp_layout_matches_one_warp_cta(plain512, sampler):
     """One POI per warp (per-reference gradient image, runs of consecutive
     POIs) does per POI exactly the arithmetic of the one-warp CTA: same
     sample order per lane, sums, solve and update, so every output is
-    bit-identical, whatever the run length and CTA size."""
+    bit-identical, whatever the run length, CTA size and loop unrolling."""
     pair, g, poi, _ = plain512
     outs = []
-    for threads, chunk in [(32, 0), (1024, 32), (512, 7), (128, 1)]:
+    for threads, chunk, unroll in [(32, 0, 4), (1024, 32, 4), (1024, 32, 2), (1024, 32, 8), (512, 7, 4),
+                                   (128, 1, 4)]:
         fr = dic.DICFrame(params_of(g, PATH_FAST))
         fr.set_tuning(threads, 0, sampler, 1, icgn_chunk=chunk)
+        fr.set_icgn_unroll(unroll)
         fr.set_reference(pair.ref)
         o = fr.alloc_outputs()
         fr.process(pair.tar, **o)
@@ -146,6 +148,8 @@ def test_layout_rejects_bad_shapes(small):
         fr.set_icgn_layout(-1)
     with pytest.raises(Exception):
         fr.set_tuning(96, 0, SAMPLER_NBHD, 1)
+    with pytest.raises(Exception):
+        fr.set_icgn_unroll(3)
     # 1024 threads need the one-POI-per-warp layout: the launch is refused
     fr.set_tuning(1024, 0, SAMPLER_NBHD, 1, icgn_chunk=0)
     fr.set_reference(pair.ref)

@@ -40,8 +40,8 @@ EXPORTED = (
     "twdic_icgn_create", "twdic_icgn_reset_ref", "twdic_icgn_compute", "twdic_icgn_destroy",
     "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
-    "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
-    "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_graph",
+    "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_icgn_unroll", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
+    "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_icgn_unroll", "twdic_batch_set_graph",
     "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
     "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
@@ -88,7 +88,7 @@ class Tuning(ctypes.Structure):
         ("icgn_threads", ctypes.c_int32), ("icgn_ctas_per_sm", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32),
         ("fftcc_use_tc", ctypes.c_int32), ("fftcc_groups", ctypes.c_int32), ("fftcc_pois_per_group", ctypes.c_int32),
         ("fftcc_ms", ctypes.c_float), ("icgn_ms", ctypes.c_float), ("from_cache", ctypes.c_int32),
-        ("icgn_chunk", ctypes.c_int32),
+        ("icgn_chunk", ctypes.c_int32), ("icgn_unroll", ctypes.c_int32),
     ]
 
 
@@ -143,12 +143,14 @@ def load():
         "twdic_frame_destroy": ([_VP], _I),
         "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
         "twdic_frame_set_icgn_layout": ([_VP, _I], _I),
+        "twdic_frame_set_icgn_unroll": ([_VP, _I], _I),
         "twdic_frame_set_fftcc_twiddles": ([_VP, _I], _I),
         "twdic_icgn_compute_noalloc": ([P, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP], _I),
         "twdic_batch_create": ([ctypes.POINTER(_VP)], _I),
         "twdic_batch_set_stream": ([_VP, _VP], _I),
         "twdic_batch_set_tuning": ([_VP, _I, _I, _I], _I),
         "twdic_batch_set_icgn_layout": ([_VP, _I], _I),
+        "twdic_batch_set_icgn_unroll": ([_VP, _I], _I),
         "twdic_batch_set_graph": ([_VP, _I], _I),
         "twdic_batch_process": ([_VP, ctypes.c_int32, _VP, _VP, _VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I,
                                  _I32P], _I),

@@ -717,6 +717,13 @@ int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk) {
     return TWDIC_OK;
 }
 
+int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (unroll != 2 && unroll != 4 && unroll != 8) return fail(TWDIC_ERR_INVALID_ARG, "unroll must be 2, 4 or 8");
+    h->e.icgn_tune.unroll = unroll;
+    return TWDIC_OK;
+}
+
 int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
     if (groups < 0 || groups > 2 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
@@ -739,6 +746,7 @@ int twdic_frame_get_tuning(const twdic_frame* h, twdic_tuning* out) {
     out->icgn_ctas_per_sm = h->e.icgn_tune.ctas_per_sm;
     out->icgn_sampler = h->e.icgn_tune.sampler;
     out->icgn_chunk = h->e.icgn_tune.chunk;
+    out->icgn_unroll = h->e.icgn_tune.unroll;
     out->fftcc_use_tc = h->e.fftcc_tune.use_tc;
     out->fftcc_groups = h->e.fftcc_tune.groups;
     out->fftcc_pois_per_group = h->e.fftcc_tune.pois_per_group;
@@ -778,9 +786,9 @@ bool cache_lookup(const char* path, const std::string& key, twdic_tuning* t) {
         if (std::strncmp(line, key.c_str(), k) != 0 || line[k] != ' ') continue;
         twdic_tuning c;
         std::memset(&c, 0, sizeof(c));
-        if (std::sscanf(line + k, " %d %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm,
-                        &c.icgn_sampler, &c.icgn_chunk, &c.fftcc_use_tc, &c.fftcc_groups, &c.fftcc_pois_per_group,
-                        &c.fftcc_ms, &c.icgn_ms) == 9) {
+        if (std::sscanf(line + k, " %d %d %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm,
+                        &c.icgn_sampler, &c.icgn_chunk, &c.icgn_unroll, &c.fftcc_use_tc, &c.fftcc_groups,
+                        &c.fftcc_pois_per_group, &c.fftcc_ms, &c.icgn_ms) == 10) {
             *t = c;  // the last entry for a key wins
             found = true;
         }
@@ -812,6 +820,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
         e.icgn_tune.ctas_per_sm = t.icgn_ctas_per_sm;
         e.icgn_tune.sampler = t.icgn_sampler;
         e.icgn_tune.chunk = t.icgn_chunk;
+        e.icgn_tune.unroll = t.icgn_unroll;
         e.fftcc_tune.use_tc = t.fftcc_use_tc;
         e.fftcc_tune.groups = t.fftcc_groups;
         e.fftcc_tune.pois_per_group = t.fftcc_pois_per_group;
@@ -896,6 +905,25 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
                 }
             }
         }
+        // sample-loop unrolling of the chosen one-POI-per-warp shape
+        if (best_i.chunk > 0 && best_i.threads == 1024) {
+            for (int unroll : {2, 4}) {
+                IcgnTune c = best_i;
+                c.unroll = unroll;
+                e.icgn_tune = c;
+                float f = 0, ic = 0;
+                const int rc = measure(&f, &ic);
+                if (rc != TWDIC_OK) {
+                    e.fftcc_tune = fft0;
+                    e.icgn_tune = icgn0;
+                    return rc;
+                }
+                if (ic < best_ims) {
+                    best_ims = ic;
+                    best_i = c;
+                }
+            }
+        }
     } else {
         float f = 0, ic = 0;
         TW_TRY(measure(&f, &ic));
@@ -907,6 +935,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     t.icgn_ctas_per_sm = best_i.ctas_per_sm;
     t.icgn_sampler = best_i.sampler;
     t.icgn_chunk = best_i.chunk;
+    t.icgn_unroll = best_i.unroll;
     t.fftcc_use_tc = e.fftcc_tune.use_tc;
     t.fftcc_groups = e.fftcc_tune.groups;
     t.fftcc_pois_per_group = e.fftcc_tune.pois_per_group;
@@ -916,9 +945,9 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     if (cache_path) {
         FILE* f = std::fopen(cache_path, "a");
         if (f) {
-            std::fprintf(f, "%s %d %d %d %d %d %d %d %.4f %.4f\n", key.c_str(), t.icgn_threads, t.icgn_ctas_per_sm,
-                         t.icgn_sampler, t.icgn_chunk, t.fftcc_use_tc, t.fftcc_groups, t.fftcc_pois_per_group,
-                         t.fftcc_ms, t.icgn_ms);
+            std::fprintf(f, "%s %d %d %d %d %d %d %d %d %.4f %.4f\n", key.c_str(), t.icgn_threads,
+                         t.icgn_ctas_per_sm, t.icgn_sampler, t.icgn_chunk, t.icgn_unroll, t.fftcc_use_tc,
+                         t.fftcc_groups, t.fftcc_pois_per_group, t.fftcc_ms, t.icgn_ms);
             std::fclose(f);
         }
     }
@@ -1148,6 +1177,16 @@ int twdic_batch_set_icgn_layout(twdic_batch* b, int chunk) {
     if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
     if (chunk < 0) return fail(TWDIC_ERR_INVALID_ARG, "chunk must be >= 0");
     b->tune.chunk = chunk;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->key.clear();
+    return TWDIC_OK;
+}
+
+int twdic_batch_set_icgn_unroll(twdic_batch* b, int unroll) {
+    if (!b) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (unroll != 2 && unroll != 4 && unroll != 8) return fail(TWDIC_ERR_INVALID_ARG, "unroll must be 2, 4 or 8");
+    b->tune.unroll = unroll;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
     b->key.clear();

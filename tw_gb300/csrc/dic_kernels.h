@@ -25,6 +25,7 @@ struct IcgnTune {
     // consecutive POIs over the per-reference gradient image (threads 128 to
     // 1024, a table sampler); 0: one POI per CTA
     int chunk = 0;
+    int unroll = 8;  // sample-loop unrolling of the one-POI-per-warp kernel (2, 4 or 8)
 };
 
 // Image pairs (jobs) of one batched launch: each job has its own geometry,

@@ -624,7 +624,7 @@ __global__ void k_ref_grad(Geom g, const uint8_t* __restrict__ ref, __half2* __r
 // L1 across neighbouring POIs and across iterations.  The arithmetic per
 // POI is that of k_icgn_fast<32, ...>: the same sample order per lane, the
 // same sums, reduction, solve and update, so the results are identical.
-template <int NW, int SAMPLER, bool MULTI>
+template <int NW, int SAMPLER, bool MULTI, int UNROLL>
 __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
     k_icgn_warp(const __grid_constant__ IcgnJobs J, int chunk) {
     constexpr unsigned FULL = 0xffffffffu;
@@ -704,7 +704,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                 const float2 bxy = make_float2(bx, by);
                 if (it == 0) {
                     // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
-#pragma unroll 4
+#pragma unroll UNROLL
                     for (int k = lane; k < S; k += 32) {
                         const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
                                                       __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
@@ -718,7 +718,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                         }
                     }
                 } else {
-#pragma unroll 4
+#pragma unroll UNROLL
                     for (int k = lane; k < S; k += 32) {
                         const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
                                                       __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
@@ -924,8 +924,11 @@ cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, __half2* grad, cu
 }
 
 template <int NW, int SAMPLER, bool MULTI>
-static cudaError_t launch_icgn_warp_t(const IcgnJobs& J, int chunk, int ctas_per_sm, cudaStream_t st) {
-    auto kern = k_icgn_warp<NW, SAMPLER, MULTI>;
+static cudaError_t launch_icgn_warp_t(const IcgnJobs& J, int chunk, int ctas_per_sm, int unroll, cudaStream_t st) {
+    // sample-loop unrolling: 2, 4 or 8 for the one-CTA-per-SM shape, 4 otherwise
+    auto kern = k_icgn_warp<NW, SAMPLER, MULTI, 4>;
+    if (NW == 32 && unroll == 2) kern = k_icgn_warp<NW, SAMPLER, MULTI, (NW == 32 ? 2 : 4)>;
+    if (NW == 32 && unroll == 8) kern = k_icgn_warp<NW, SAMPLER, MULTI, (NW == 32 ? 8 : 4)>;
     // a few KB of shared memory: leave the rest of the SM's 256 KB to L1
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
     if (e != cudaSuccess) return e;
@@ -961,8 +964,8 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
             if (!J.job[j].table) return cudaErrorInvalidValue;
         const bool multi = J.njobs > 1;
 #define TWDIC_ICGN_WARP(NW, SA)                                                                  \
-    return multi ? launch_icgn_warp_t<NW, SA, true>(J, tune.chunk, tune.ctas_per_sm, st)         \
-                 : launch_icgn_warp_t<NW, SA, false>(J, tune.chunk, tune.ctas_per_sm, st)
+    return multi ? launch_icgn_warp_t<NW, SA, true>(J, tune.chunk, tune.ctas_per_sm, tune.unroll, st)  \
+                 : launch_icgn_warp_t<NW, SA, false>(J, tune.chunk, tune.ctas_per_sm, tune.unroll, st)
 #define TWDIC_ICGN_WARP_N(NW)                                                                    \
     if (tune.sampler == kSampLut) { TWDIC_ICGN_WARP(NW, kSampLut); }                              \
     TWDIC_ICGN_WARP(NW, kSampNbhd)

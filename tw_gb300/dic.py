@@ -286,6 +286,10 @@ class DICFrame:
         consecutive POIs (threads 128 to 1024, a table sampler)."""
         check(self._lib.twdic_frame_set_icgn_layout(self._h, chunk))
 
+    def set_icgn_unroll(self, unroll):
+        """Unrolling of the IC-GN sample loop: 2, 4 or 8 (default)."""
+        check(self._lib.twdic_frame_set_icgn_unroll(self._h, unroll))
+
     def set_fftcc_twiddles(self, hi_lo):
         """1: FP16 hi + lo twiddles in the tensor-core FFT-CC, 0: hi only."""
         check(self._lib.twdic_frame_set_fftcc_twiddles(self._h, hi_lo))
@@ -371,6 +375,9 @@ class DICBatch:
 
     def set_icgn_layout(self, chunk):
         check(self._lib.twdic_batch_set_icgn_layout(self._h, chunk))
+
+    def set_icgn_unroll(self, unroll):
+        check(self._lib.twdic_batch_set_icgn_unroll(self._h, unroll))
 
     def process(self, frames, tars, outs):
         """frames: list of DICFrame; tars: their target images; outs: list of

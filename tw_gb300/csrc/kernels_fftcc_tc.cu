@@ -581,17 +581,18 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         tc_fence_after();
         TC_MARK(6);
 
-        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (part, ky)), c2r weights
-        // folded in.  A4 overwrites A3 (stage 3 has completed), so the K
-        // padding ky in [H, HP) of the data rows is zeroed first
+        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (ky, part) interleaved:
+        // k = 2 ky + part, so a POI row's Re and Im of one ky are one 32-bit
+        // store), c2r weights folded in; core matrices 144 B apart along K so
+        // the lanes' stores to one row fall in distinct banks.  A4 overwrites
+        // A3 (stage 3 has completed), so the K padding k in [2H, 2HP) of the
+        // data rows is zeroed first
         {
-            const int c0 = H >> 3, nc = HP / 8 - c0;
+            const int c0 = (2 * H) >> 3, nc = K4 / 8 - c0;
             const int rows = PB * N;
-            for (int i = t; i < rows * 2 * nc; i += 128) {
-                const int r4 = i / (2 * nc), rem = i - r4 * (2 * nc);
-                const int part = rem / nc, c = c0 + rem - part * nc;
-                *reinterpret_cast<uint4*>(gbase + s.off_a4 + kmaj(r4, part * HP + 8 * c, K4)) =
-                    make_uint4(0, 0, 0, 0);
+            for (int i = t; i < rows * nc; i += 128) {
+                const int r4 = i / nc, c = c0 + i - r4 * nc;
+                *reinterpret_cast<uint4*>(gbase + s.off_a4 + kmaj144(r4, 8 * c, K4)) = make_uint4(0, 0, 0, 0);
             }
             group_sync(bar_id);
             const bool rowv = t < PB * H;
@@ -600,10 +601,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             // rows r4 = p N + x step by 1: +16 B inside an 8-row group,
             // +SBO - 112 B when the step crosses into the next group
             int r4 = p * N;
-            uint8_t* rowp = gbase + s.off_a4 + kmaj(r4, 0, K4);
-            const int kre = (ky >> 3) * 128 + (ky & 7) * 2;
-            const int kim = ((HP + ky) >> 3) * 128 + ((HP + ky) & 7) * 2;
-            const int sbo = 16 * K4;
+            uint8_t* rowp = gbase + s.off_a4 + kmaj144(r4, 2 * ky, K4);
+            const int sbo = 18 * K4;
 #pragma unroll
             for (int x0 = 0; x0 < NP; x0 += 8) {
                 float re[8], im[8];
@@ -614,8 +613,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         if (x0 + j < N) {
-                            st_half(rowp + kre, wgt * re[j]);
-                            st_half(rowp + kim, -wgt * im[j]);  // Zi = -D_i
+                            *reinterpret_cast<uint32_t*>(rowp) = pack2(wgt * re[j], -wgt * im[j]);  // Zi = -D_i
                             ++r4;
                             rowp += ((r4 & 7) == 0) ? (sbo - 112) : 16;
                         }
@@ -632,7 +630,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         if (t == 0) {
             tc_fence_after();
             for (int kk = 0; kk < K4 / 16; ++kk) {
-                const uint64_t a = sdesc(gaddr + s.off_a4 + kk * 256, 128, 16 * K4);
+                const uint64_t a = sdesc(gaddr + s.off_a4 + kk * 288, 144, 18 * K4);
                 const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
                 const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
                 mma_f16(tm, a, bh, idesc_f16(NP, false), kk > 0);
@@ -860,7 +858,7 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
     s.NW4 = (N + 3) / 4;
     s.lo = tune.twiddle_lo ? 1 : 0;
-    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 16 * K4;
+    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 18 * K4;
     const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
                                 128);
     s.off_a13 = 0;
@@ -896,8 +894,8 @@ std::vector<uint8_t> make_tables(const TcShape& s) {
         for (int y = 0; y < N; ++y) {
             put(s.off_b1h, s.off_b1l, ky, y, K1, std::cos(ang(ky, y)));        // Re part row
             put(s.off_b1h, s.off_b1l, HP + ky, y, K1, -std::sin(ang(ky, y)));  // Im part row
-            put(s.off_b4h, s.off_b4l, y, ky, K4, std::cos(ang(ky, y)));
-            put(s.off_b4h, s.off_b4l, y, HP + ky, K4, -std::sin(ang(ky, y)));
+            put(s.off_b4h, s.off_b4l, y, 2 * ky, K4, std::cos(ang(ky, y)));       // K = (ky, part) interleaved
+            put(s.off_b4h, s.off_b4l, y, 2 * ky + 1, K4, -std::sin(ang(ky, y)));
         }
     for (int kx = 0; kx < N; ++kx)
         for (int x = 0; x < N; ++x) {

@@ -63,6 +63,9 @@ struct TcShape {
     int lo;   // 1: twiddles as FP16 hi + lo (two MMAs per product), 0: hi only
     // shared twiddle tables
     int off_b1h, off_b1l, off_c2h, off_c2l, off_s2h, off_s2l, off_b4h, off_b4l, tab_bytes;
+    // single-FP16 twiddles: the stage-2/3 matrices with K = (x, part) interleaved,
+    // rows kx: [cos, sin] (real part of the product) and [-sin, cos] (imaginary)
+    int off_w2re, off_w2im;
     // per-group operand regions, relative to the group's base
     int off_a13, off_a2, off_a4, off_win, group_bytes;
     int smem_bytes;
@@ -416,17 +419,27 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         tc_fence_after();
         TC_MARK(2);
 
-        // ---- epilogue 1: Y -> A2 (rows (p, ky, w), K = (part, x)), FP16.  A2
-        // overwrites A1 (the region is shared), so the K padding x in [N, NP)
-        // of the data rows is zeroed first, then the data is written
+        // ---- epilogue 1: Y -> A2 (rows (p, ky, w); K = (part, x) with split
+        // twiddles, K = (x, part) interleaved with single ones, so that a row's
+        // Re and Im of one x are one 32-bit store), FP16.  A2 overwrites A1 (the
+        // region is shared), so the K padding x in [N, NP) of the data rows is
+        // zeroed first, then the data is written
         {
-            const int c0 = N >> 3, nc = NP / 8 - c0;  // 8-column chunks holding padding
             const int rows = 2 * PB * H;
-            for (int i = t; i < rows * 2 * nc; i += 128) {
-                const int r2 = i / (2 * nc), rem = i - r2 * (2 * nc);
-                const int part = rem / nc, c = c0 + rem - part * nc;
-                *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, part * NP + 8 * c, 2 * NP)) =
-                    make_uint4(0, 0, 0, 0);
+            if (LO) {
+                const int c0 = N >> 3, nc = NP / 8 - c0;  // 8-column chunks holding padding
+                for (int i = t; i < rows * 2 * nc; i += 128) {
+                    const int r2 = i / (2 * nc), rem = i - r2 * (2 * nc);
+                    const int part = rem / nc, c = c0 + rem - part * nc;
+                    *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, part * NP + 8 * c, 2 * NP)) =
+                        make_uint4(0, 0, 0, 0);
+                }
+            } else {
+                const int c0 = (2 * N) >> 3, nc = 2 * NP / 8 - c0;
+                for (int i = t; i < rows * nc; i += 128) {
+                    const int r2 = i / nc, c = c0 + i - r2 * nc;
+                    *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, 8 * c, 2 * NP)) = make_uint4(0, 0, 0, 0);
+                }
             }
             group_sync(bar_id);
         }
@@ -439,7 +452,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             // group, +SBO - 96 B when the step crosses into the next group
             int r2 = (p * H) * 2 + wsel;
             uint8_t* rowp = gbase + s.off_a2 + kmaj144(data ? r2 : 0, 0, 2 * NP);
-            const int kre = (x >> 3) * 144 + (x & 7) * 2;
+            const int kre = LO ? (x >> 3) * 144 + (x & 7) * 2 : ((2 * x) >> 3) * 144 + ((2 * x) & 7) * 2;
             const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
             const int sbo = 36 * NP;
 #pragma unroll
@@ -452,8 +465,12 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         if (ky0 + j < H) {
-                            st_half(rowp + kre, dre[j]);
-                            st_half(rowp + kim, dim[j]);
+                            if (LO) {
+                                st_half(rowp + kre, dre[j]);
+                                st_half(rowp + kim, dim[j]);
+                            } else {
+                                *reinterpret_cast<uint32_t*>(rowp + kre) = pack2(dre[j], dim[j]);
+                            }
                             r2 += 2;
                             rowp += ((r2 & 7) < 2) ? (sbo - 96) : 32;
                         }
@@ -469,7 +486,17 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         // ---- stage 2: F = Y * W (rows (p,ky,w); columns Re kx | Im kx)
         if (t == 0) {
             tc_fence_after();
-            for (int kk = 0; kk < NP / 16; ++kk) {
+            if (!LO) {
+                // K = (x, part) interleaved: one MMA per output part and K step
+                for (int kk = 0; kk < 2 * NP / 16; ++kk) {
+                    const uint64_t a = sdesc(gaddr + s.off_a2 + kk * 288, 144, 36 * NP);
+                    const uint64_t wr = sdesc(sbase + s.off_w2re + kk * 256, 128, 32 * NP);
+                    const uint64_t wi = sdesc(sbase + s.off_w2im + kk * 256, 128, 32 * NP);
+                    mma_f16(tm, a, wr, idesc_f16(NP, false), kk > 0);       // Re = Yr cos + Yi sin
+                    mma_f16(tm + NP, a, wi, idesc_f16(NP, false), kk > 0);  // Im = -Yr sin + Yi cos
+                }
+            }
+            for (int kk = 0; LO && kk < NP / 16; ++kk) {
                 const uint64_t ar = sdesc(gaddr + s.off_a2 + kk * 288, 144, 36 * NP);
                 const uint64_t ai = sdesc(gaddr + s.off_a2 + (NP / 8 + 2 * kk) * 144, 144, 36 * NP);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
@@ -534,12 +561,21 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 if (rowv) {
                     const int k0 = (wsel ? HALF : 0) + c;
                     uint4 q;
-                    q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
-                    q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
-                    *reinterpret_cast<uint4*>(a3 + kmaj(r3, k0, 2 * NP)) = q;
-                    q.x = pack2(bi[0], bi[1]); q.y = pack2(bi[2], bi[3]);
-                    q.z = pack2(bi[4], bi[5]); q.w = pack2(bi[6], bi[7]);
-                    *reinterpret_cast<uint4*>(a3 + kmaj(r3, NP + k0, 2 * NP)) = q;
+                    if (LO) {  // K = (part, kx)
+                        q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
+                        q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
+                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, k0, 2 * NP)) = q;
+                        q.x = pack2(bi[0], bi[1]); q.y = pack2(bi[2], bi[3]);
+                        q.z = pack2(bi[4], bi[5]); q.w = pack2(bi[6], bi[7]);
+                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, NP + k0, 2 * NP)) = q;
+                    } else {  // K = (kx, part) interleaved
+                        q.x = pack2(br[0], bi[0]); q.y = pack2(br[1], bi[1]);
+                        q.z = pack2(br[2], bi[2]); q.w = pack2(br[3], bi[3]);
+                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, 2 * k0, 2 * NP)) = q;
+                        q.x = pack2(br[4], bi[4]); q.y = pack2(br[5], bi[5]);
+                        q.z = pack2(br[6], bi[6]); q.w = pack2(br[7], bi[7]);
+                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, 2 * k0 + 8, 2 * NP)) = q;
+                    }
                 }
             }
             // rows of A3 past the data are zero (A3 shares memory with A1, A2)
@@ -556,7 +592,16 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         // ---- stage 3: conj(Z) = conj(C) * W (rows (p,ky); columns Re x | Im x)
         if (t == 0) {
             tc_fence_after();
-            for (int kk = 0; kk < NP / 16; ++kk) {
+            if (!LO) {
+                for (int kk = 0; kk < 2 * NP / 16; ++kk) {
+                    const uint64_t a = sdesc(gaddr + s.off_a13 + kk * 256, 128, 32 * NP);
+                    const uint64_t wr = sdesc(sbase + s.off_w2re + kk * 256, 128, 32 * NP);
+                    const uint64_t wi = sdesc(sbase + s.off_w2im + kk * 256, 128, 32 * NP);
+                    mma_f16(tm, a, wr, idesc_f16(NP, false), kk > 0);
+                    mma_f16(tm + NP, a, wi, idesc_f16(NP, false), kk > 0);
+                }
+            }
+            for (int kk = 0; LO && kk < NP / 16; ++kk) {
                 const uint64_t ar = sdesc(gaddr + s.off_a13 + kk * 256, 128, 32 * NP);
                 const uint64_t ai = sdesc(gaddr + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 32 * NP);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
@@ -842,22 +887,28 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     if (s.tiles1 * 2 * s.HP > kTmemCols || 2 * s.NP > kTmemCols || s.tiles1 > 2) return false;
     if (2 * pb * s.H > 128 || pb * N > 128) return false;
     const int K1 = s.NP, N1 = 2 * s.HP, NP = s.NP, K4 = s.K4;
+    s.lo = tune.twiddle_lo ? 1 : 0;
     int o = 0;
+    s.off_b1l = s.off_c2h = s.off_c2l = s.off_s2h = s.off_s2l = s.off_b4l = s.off_w2re = s.off_w2im = 0;
     s.off_b1h = o; o += N1 * K1 * 2;
-    s.off_b1l = o; o += N1 * K1 * 2;
-    s.off_c2h = o; o += NP * NP * 2;
-    s.off_c2l = o; o += NP * NP * 2;
-    s.off_s2h = o; o += NP * NP * 2;
-    s.off_s2l = o; o += NP * NP * 2;
+    if (s.lo) {
+        s.off_b1l = o; o += N1 * K1 * 2;
+        s.off_c2h = o; o += NP * NP * 2;
+        s.off_c2l = o; o += NP * NP * 2;
+        s.off_s2h = o; o += NP * NP * 2;
+        s.off_s2l = o; o += NP * NP * 2;
+    } else {
+        s.off_w2re = o; o += NP * 2 * NP * 2;
+        s.off_w2im = o; o += NP * 2 * NP * 2;
+    }
     s.off_b4h = o; o += NP * K4 * 2;
-    s.off_b4l = o; o += NP * K4 * 2;
+    if (s.lo) { s.off_b4l = o; o += NP * K4 * 2; }
     s.tab_bytes = round_up(o, 1024);
     o = s.tab_bytes;
     // per-group regions: one operand region shared by A1, A2, A3, A4 and the
     // peak scratch, then the windows
     s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
     s.NW4 = (N + 3) / 4;
-    s.lo = tune.twiddle_lo ? 1 : 0;
     const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 18 * K4;
     const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
                                 128);
@@ -883,11 +934,18 @@ std::vector<uint8_t> make_tables(const TcShape& s) {
     std::vector<uint8_t> blob(s.tab_bytes, 0);
     const int N = s.N, H = s.H, HP = s.HP, NP = s.NP, K1 = s.NP, K4 = s.K4;
     const double two_pi = 6.283185307179586476925286766559;
+    // the hi part (and with split twiddles the lo part) of entry (r, k)
     auto put = [&](int off_h, int off_l, int r, int k, int K, double val) {
         const __half h = __double2half(val);
-        const __half l = __double2half(val - (double)__half2float(h));
         std::memcpy(&blob[off_h + kmaj(r, k, K)], &h, 2);
-        std::memcpy(&blob[off_l + kmaj(r, k, K)], &l, 2);
+        if (s.lo) {
+            const __half l = __double2half(val - (double)__half2float(h));
+            std::memcpy(&blob[off_l + kmaj(r, k, K)], &l, 2);
+        }
+    };
+    auto put1 = [&](int off, int r, int k, int K, double val) {
+        const __half h = __double2half(val);
+        std::memcpy(&blob[off + kmaj(r, k, K)], &h, 2);
     };
     auto ang = [&](int a, int b) { return two_pi * (double)((long long)a * b % N) / N; };
     for (int ky = 0; ky < H; ++ky)
@@ -899,8 +957,15 @@ std::vector<uint8_t> make_tables(const TcShape& s) {
         }
     for (int kx = 0; kx < N; ++kx)
         for (int x = 0; x < N; ++x) {
-            put(s.off_c2h, s.off_c2l, kx, x, NP, std::cos(ang(kx, x)));
-            put(s.off_s2h, s.off_s2l, kx, x, NP, std::sin(ang(kx, x)));
+            if (s.lo) {
+                put(s.off_c2h, s.off_c2l, kx, x, NP, std::cos(ang(kx, x)));
+                put(s.off_s2h, s.off_s2l, kx, x, NP, std::sin(ang(kx, x)));
+            } else {
+                put1(s.off_w2re, kx, 2 * x, 2 * NP, std::cos(ang(kx, x)));
+                put1(s.off_w2re, kx, 2 * x + 1, 2 * NP, std::sin(ang(kx, x)));
+                put1(s.off_w2im, kx, 2 * x, 2 * NP, -std::sin(ang(kx, x)));
+                put1(s.off_w2im, kx, 2 * x + 1, 2 * NP, std::cos(ang(kx, x)));
+            }
         }
     return blob;
 }
@@ -910,7 +975,7 @@ std::vector<uint8_t> make_tables(const TcShape& s) {
 // allocate: a launch captured into a CUDA graph must not.
 struct TablesCache {
     std::mutex mu;
-    std::map<std::pair<int, int>, uint4*> dev;
+    std::map<std::pair<int, int>, uint4*> dev;  // (device, 2 N + lo)
 };
 TablesCache& tables_cache() {
     static TablesCache* c = new TablesCache();  // never destroyed: may outlive the CUDA context
@@ -923,7 +988,8 @@ cudaError_t tables_for(const TcShape& s, const uint4** out) {
     if (e != cudaSuccess) return e;
     TablesCache& c = tables_cache();
     std::lock_guard<std::mutex> lock(c.mu);
-    auto it = c.dev.find({device, s.N});
+    const int key = 2 * s.N + s.lo;
+    auto it = c.dev.find({device, key});
     if (it != c.dev.end()) {
         *out = it->second;
         return cudaSuccess;
@@ -937,7 +1003,7 @@ cudaError_t tables_for(const TcShape& s, const uint4** out) {
         cudaFree(d);
         return e;
     }
-    c.dev[{device, s.N}] = d;
+    c.dev[{device, key}] = d;
     *out = d;
     return cudaSuccess;
 }

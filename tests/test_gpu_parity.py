@@ -100,9 +100,7 @@ def test_fast_icgn_samplers(plain512, sampler, shape):
     parity bar against the oracle (staged window and neighbourhood table
     evaluate the Catmull-Rom form, the LUT sampler the reference's Hermite
     coefficients)."""
-    threads, chunk = shape
-    if chunk > 0 and sampler == SAMPLER_WINDOW:
-        pytest.skip("one POI per warp reads a per-frame table")
+    threads, chunk = shape  # with the window sampler a one-POI-per-warp shape runs one-POI-per-CTA kernels
     pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = plain512
     fr = dic.DICFrame(params_of(g, PATH_FAST))
     fr.set_tuning(threads, 0, sampler, 1, icgn_chunk=chunk)

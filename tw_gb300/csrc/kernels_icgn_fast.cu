@@ -727,11 +727,11 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                         const float fx = fxy.x, fy = fxy.y;
                         float tp;
                         if (SAMPLER == kSampNbhd) {
-                            const uint4 q = nb0[(size_t)iy * g.rw + ix];
+                            const uint4 q = nb0[(unsigned)(iy * g.rw + ix)];  // < 2^31 entries
                             const float2 h01 = cr_row_pair(q.x, q.y, fx), h23 = cr_row_pair(q.z, q.w, fx);
                             tp = fmaf(0.5f, cr_combine4x4(h01, h23, fy), -c);
                         } else {
-                            const float4* q = lut0 + ((size_t)iy * g.rw + ix);
+                            const float4* q = lut0 + (unsigned)(iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
                             const float2 tx = make_float2(fx, fx);
                             const float2 r01 = __ffma2_rn(
@@ -947,12 +947,16 @@ static cudaError_t launch_icgn_warp_t(const IcgnJobs& J, int chunk, int ctas_per
 }
 
 // One POI per warp over a per-reference gradient image: every job needs
-// grad and a table sampler.
+// grad, a table sampler and table offsets below 2^31 (otherwise the
+// one-POI-per-CTA kernel runs).
 static bool icgn_warp_eligible(const IcgnJobs& J, const IcgnTune& tune) {
     if (tune.chunk <= 0 || tune.sampler == kSampWindow) return false;
     if (tune.threads != 128 && tune.threads != 256 && tune.threads != 512 && tune.threads != 1024) return false;
-    for (int j = 0; j < J.njobs; ++j)
+    for (int j = 0; j < J.njobs; ++j) {
         if (!J.job[j].grad) return false;
+        // the kernel indexes the table with 32-bit image offsets iy * rw + ix
+        if ((long long)J.job[j].g.img_h * J.job[j].g.rw >= (1ll << 31)) return false;
+    }
     return true;
 }
 
@@ -976,21 +980,25 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
 #undef TWDIC_ICGN_WARP_N
 #undef TWDIC_ICGN_WARP
     }
-    if (tune.threads != 32 && tune.threads != 64 && tune.threads != 128 && tune.threads != 256)
-        return cudaErrorInvalidValue;  // one POI per CTA: 32 to 256 threads
+    // one POI per CTA: 32 to 256 threads; where the one-POI-per-warp layout was
+    // asked for but cannot run (window sampler, oversized image), one-warp CTAs
+    IcgnTune t1 = tune;
+    if (t1.chunk > 0 && t1.threads > 256) t1.threads = 32;
+    if (t1.threads != 32 && t1.threads != 64 && t1.threads != 128 && t1.threads != 256)
+        return cudaErrorInvalidValue;
     for (int j = 0; j < J.njobs; ++j)
-        if (tune.sampler != kSampWindow && !J.job[j].table) return cudaErrorInvalidValue;
+        if (t1.sampler != kSampWindow && !J.job[j].table) return cudaErrorInvalidValue;
     const bool multi = J.njobs > 1;
 #define TWDIC_ICGN_FAST(TH, SA)                                                                  \
-    return multi ? launch_icgn_fast_t<TH, SA, true>(J, work, tune.ctas_per_sm, st)               \
-                 : launch_icgn_fast_t<TH, SA, false>(J, work, tune.ctas_per_sm, st)
+    return multi ? launch_icgn_fast_t<TH, SA, true>(J, work, t1.ctas_per_sm, st)               \
+                 : launch_icgn_fast_t<TH, SA, false>(J, work, t1.ctas_per_sm, st)
 #define TWDIC_ICGN_FAST_T(TH)                                                                    \
-    if (tune.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                              \
-    if (tune.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                            \
+    if (t1.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                              \
+    if (t1.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                            \
     TWDIC_ICGN_FAST(TH, kSampWindow)
-    if (tune.threads == 32) { TWDIC_ICGN_FAST_T(32); }
-    if (tune.threads == 64) { TWDIC_ICGN_FAST_T(64); }
-    if (tune.threads == 256) { TWDIC_ICGN_FAST_T(256); }
+    if (t1.threads == 32) { TWDIC_ICGN_FAST_T(32); }
+    if (t1.threads == 64) { TWDIC_ICGN_FAST_T(64); }
+    if (t1.threads == 256) { TWDIC_ICGN_FAST_T(256); }
     TWDIC_ICGN_FAST_T(128);
 #undef TWDIC_ICGN_FAST_T
 #undef TWDIC_ICGN_FAST

@@ -117,6 +117,37 @@ def test_fast_icgn_samplers(plain512, sampler, shape):
     assert rep.ok(), (sampler, shape, rep)
 
 
+@pytest.mark.parametrize("max_iter", [20, 1])
+@pytest.mark.parametrize("sampler", [SAMPLER_NBHD, SAMPLER_LUT, SAMPLER_WINDOW])
+def test_icgn_subsets_touching_the_roi_edge(sampler, max_iter):
+    """Margin 0: the last POIs' subsets end on the ROI's last row and column.
+    The first (integer) pass reads those pixels from the image, while the
+    reference's LUT, and so the table samplers, are zero there; with one
+    iteration the result is the first pass's update alone."""
+    h, w = 156, 191
+    field, grad = synth.affine_field(0.3, 0.25, 0.002, -0.001, 0.001, -0.0015, w / 2, h / 2)
+    pair = synth.make_pair(h, w, int(6000 * h * w / (512 * 512)), field, grad, 77, description="ROI-edge case")
+    g = synth.Geometry(w, h, 1, 1, w - 2, h - 2, 10, 7, 0, max_iter=max_iter)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    assert poi[:, 0].max() + g.subset_r == g.start_y + g.roi_h - 1
+    assert poi[:, 1].max() + g.subset_r == g.start_x + g.roi_w - 1
+    u_or, v_or, z_or, st_or, p6_or, it_or, fl_or = oracle_run(pair, g, poi)
+    fr = dic.DICFrame(params_of(g, PATH_FAST))
+    fr.set_tuning(1024, 0, sampler, 1, icgn_chunk=32)
+    fr.set_reference(pair.ref)
+    out = fr.alloc_outputs()
+    fr.process(pair.tar, **out)
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                      g.grid, g.margin, g.margin, path=PATH_FAST)
+    U, V, Z = f.InitializeFFTCC(pair.ref)
+    f.ComputeFFTCC(U, V, Z, pair.tar)
+    same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
+    rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start,
+                        r=g.subset_r)
+    assert rep.ok(), (sampler, rep)
+
+
 @pytest.mark.parametrize("sampler", [SAMPLER_LUT, SAMPLER_NBHD])
 def test_warp_layout_matches_one_warp_cta(plain512, sampler):
     """One POI per warp (per-reference gradient image, runs of consecutive

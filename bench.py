@@ -158,14 +158,41 @@ def cpu_rate(pair, g, poi, n_sample, nthreads=0):
     return len(poi) / frame_s, t_pre + t_sample, O.max_threads()
 
 
-def cpu_baseline(pair, g, poi, target_s=12.0):
+def cpu_baseline(pair, g, poi, gpu_out=None, target_s=12.0):
     rate, dt, thr = cpu_rate(pair, g, poi, 1500)
     n = int(min(len(poi), max(1500, rate * target_s)))
     rate, dt, thr = cpu_rate(pair, g, poi, n)
-    return {"value": round(rate, 1), "unit": UNIT, "cores": thr, "kind": "port",
+    line = {"value": round(rate, 1), "unit": UNIT, "cores": thr, "kind": "port",
             "sample": f"first {n} POIs (row-major) of the workload, FFT-CC + IC-GN, plus the per-frame whole-ROI "
                       f"gradient/LUT precompute, extrapolated to all {len(poi)} POIs ({dt:.1f} s of CPU work); OpenMP "
                       "over POIs; oracle = C++ restatement of the reference CPU path (MKL/FFTW/LAPACKE not available)"}
+    if gpu_out is not None:
+        line["accuracy_vs_oracle"] = accuracy_vs_oracle(pair, g, poi, gpu_out)
+    return line
+
+
+def accuracy_vs_oracle(pair, g, poi, gpu_out, stride=31):
+    """The GPU frame's results against the oracle on every stride-th POI:
+    FFT-CC in FP32 (integer guesses), then IC-GN in FP32 (the parity
+    reference) and in FP64 from the same guesses.  POIs flagged Success by
+    both sides are compared on u, v and the gradients; flags and iteration
+    counts are compared on all sampled POIs."""
+    from oracle import oracle as O
+    idx = np.arange(0, len(poi), stride)
+    sp = np.ascontiguousarray(poi[idx])
+    u, v, z, st = O.fftcc(pair.ref, pair.tar, sp, g.subset_r)
+    out = {"pois": int(len(idx)), "sample": f"every {stride}-th POI of the frame"}
+    p6g, itg, flg = gpu_out["p6"][idx], gpu_out["iters"][idx], gpu_out["flags"][idx]
+    for prec in ("f32", "f64"):
+        p6o, ito, flo = O.icgn(pair.ref, pair.tar, g, sp, u, v, precision=prec)
+        ok = (flg == 0) & (flo == 0)
+        d = np.abs(p6g[ok].astype(np.float64) - p6o[ok].astype(np.float64))
+        out[prec] = {"compared": int(ok.sum()), "flags_equal": float((flg == flo).mean()),
+                     "iterations_equal": float((itg == ito).mean()),
+                     "max_abs_u": float(d[:, 0].max()), "max_abs_v": float(d[:, 3].max()),
+                     "mean_abs_uv": float(d[:, [0, 3]].mean()),
+                     "max_abs_gradient": float(d[:, [1, 2, 4, 5]].max())}
+    return out
 
 
 def run_reference(args, world, rank):
@@ -297,6 +324,7 @@ def _run_gpu(args, world, rank, local, torch):
     from oracle import compare as C  # test infrastructure: truth error only
     p6 = outs["p6"].cpu().numpy()
     flags = outs["flags"].cpu().numpy()
+    iters_np = outs["iters"].cpu().numpy()
     iters = outs["iters"].cpu().numpy()
     poi = fr.poi_positions()
     acc = C.truth_error(pair, poi, p6, flags)
@@ -349,7 +377,7 @@ def _run_gpu(args, world, rank, local, torch):
         line["batched"] = run_batched(pairs=48, steps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O  # noqa: F401  (CPU baseline leg)
-        line["cpu_baseline"] = cpu_baseline(pair, g, poi)
+        line["cpu_baseline"] = cpu_baseline(pair, g, poi, gpu_out={"p6": p6, "iters": iters_np, "flags": flags})
     if rank == 0:
         print(json.dumps(line))
     return 0

@@ -1,27 +1,31 @@
 // Fast IC-GN path.
 //
-// Per reference image (cached, 256 B per POI): mean(R), ||R - mean(R)||, the
-// sums over the subset of the six steepest-descent images SD_k and of
-// SD_k * (R - mean(R)), and the FP64 Cholesky factor of the 6x6 Hessian
-// (diagonal stored as its reciprocal).  The steepest-descent images
-// themselves are rebuilt on chip from the reference image: R_x and R_y are
-// exact half integers (TW_utils.cpp:232-305) and SD = (R_x, R_x dx, R_x dy,
-// R_y, R_y dx, R_y dy).
+// Per reference image (cached): per POI 16 floats (mean(R), ||R - mean(R)||,
+// the subset sums of the six steepest-descent images SD_k and of
+// SD_k * (R - mean(R))) and the packed FP64 inverse Hessian (21 doubles, from
+// an FP64 Cholesky factor), and per ROI pixel the reference gradients
+// (R_x, R_y) as half2 -- exact half integers (TW_utils.cpp:232-305).  The
+// steepest-descent images are never stored: SD = (R_x, R_x dx, R_x dy, R_y,
+// R_y dx, R_y dy) is formed per sample.
 //
-// Per frame: one persistent kernel.  Each CTA takes the next POI from an
-// atomic work counter (row-major order, so CTAs in flight share image rows in
-// L2), stages the target window around the FFT-CC guess in shared memory and
-// runs the whole Gauss-Newton loop on chip.  One pass over the subset per
-// iteration accumulates, with T' = T - mean(R),
+// Per target frame: the 4x4 byte neighbourhood of every ROI pixel (16 B,
+// k_nbhd_table), then one persistent kernel that runs the whole Gauss-Newton
+// loop of each POI on chip.  Default layout (k_icgn_warp): one POI per warp,
+// the 32 warps of a CTA walking runs of consecutive POIs so that their
+// overlapping subsets are served from L1.  One-POI-per-CTA layout
+// (k_icgn_fast): 32 to 256 threads per POI, gradients staged in shared
+// memory, optionally sampling a target window staged in shared memory
+// instead of a table (the no-allocation entry point).  One pass over the
+// subset per iteration accumulates, with T' = T - mean(R),
 //     S0 = sum T',  S1 = sum T'^2,  A_k = sum SD_k T',
 // from which the reference's two-pass quantities follow exactly in real
 // arithmetic (TW_paDIC_ICGN2D_CPU.cpp:793-826):
 //     mean(T) = mean(R) + S0/S,  ||T - mean(T)||^2 = S1 - S0^2/S,
 //     RHS_k = (Rs/Ts) (A_k - (S0/S) sum SD_k) - sum SD_k (R - mean(R)).
-// The target is interpolated on the fly: the reference's Hermite bicubic LUT
-// with central-difference derivatives (TW_utils.cpp:604-700) is algebraically
-// the separable Catmull-Rom kernel on the 4x4 neighbourhood, so no per-frame
-// LUT is built; the LUT's zero last ROI row and column are reproduced.
+// The reference's Hermite bicubic LUT with central-difference derivatives
+// (TW_utils.cpp:604-700) is algebraically the separable Catmull-Rom kernel on
+// the 4x4 neighbourhood, evaluated from the table's bytes; the LUT's zero
+// last ROI row and column are reproduced by zero table entries.
 #include <cuda_fp16.h>
 
 #include <algorithm>

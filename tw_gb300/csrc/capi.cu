@@ -124,6 +124,7 @@ Geom make_geom(const twdic_params& p) {
     g.sx = p.start_x; g.sy = p.start_y; g.rw = p.roi_width; g.rh = p.roi_height;
     g.rx = p.subset_x; g.ry = p.subset_y;
     g.max_iter = p.max_iterations; g.delta_p = p.delta_p;
+    g.grid_x = p.grid_space_x;
     return g;
 }
 

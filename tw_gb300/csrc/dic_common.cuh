@@ -37,6 +37,7 @@ struct Geom {
     int rx, ry;               // subset half sizes
     int max_iter;
     float delta_p;
+    int grid_x = 0;           // POI grid step along x (0: unknown), sizes FFT-CC window boxes
 };
 
 enum : uint8_t { kSuccess = 0, kDarkSubset = 1, kSingularHessian = 2, kSingularWarp = 3, kOutofROI = 4 };

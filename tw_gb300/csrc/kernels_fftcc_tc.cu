@@ -77,6 +77,12 @@ struct TcShape {
 struct TcJob {
     CUtensorMap map_ref;  // 64-byte aligned
     CUtensorMap map_tar;
+    // boxes [N rows][uw bytes] holding the windows of a whole batch when its
+    // POIs lie on one POI row (uw = 0: not used for this job)
+    CUtensorMap map_ref_u;
+    CUtensorMap map_tar_u;
+    int uw;
+    int utoff;  // offset of the target box in the window region (128-byte aligned)
     Geom g;
     const int2* poi;
     float* u;
@@ -246,7 +252,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     __shared__ uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
     __shared__ int smaxi[kMaxGroups][kMaxPB];       // its first index
     __shared__ int2 spoi[kMaxGroups][kMaxPB];
-    __shared__ int smis[kMaxGroups][2 * kMaxPB];
+    __shared__ int wbase[kMaxGroups][2 * kMaxPB];  // byte offset of each window's (0, 0) in wwin
+    __shared__ int wrs[kMaxGroups];                // row stride of the windows in wwin
     __shared__ int snext[kMaxGroups];
 
     const int grp = threadIdx.x >> 7;
@@ -330,21 +337,47 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         group_sync(bar_id);
 
-        // ---- phase L1: one TMA box per window ([N rows][BW bytes], x aligned
-        // down to 16 bytes; out-of-bounds parts are zero-filled)
+        // ---- phase L1: the windows by TMA (x aligned down to 16 bytes;
+        // out-of-bounds parts are zero-filled).  When the batch's POIs lie on
+        // one POI row, one [N][uw] box per image holds all its windows (two
+        // copies instead of 2 PB); otherwise one [N][BW] box per window
         if (t == 0) {
             fence_async_smem();  // the previous batch's generic reads of the windows come first
-            int nload = 0;
-            for (int wi = 0; wi < 2 * PB; ++wi) nload += spoi[grp][wi >> 1].x >= 0;
-            mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
-            for (int wi = 0; wi < 2 * PB; ++wi) {
-                const int2 pyx = spoi[grp][wi >> 1];
-                smis[grp][wi] = 0;  // read (harmlessly) by the row copies for absent POIs
+            int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
+            for (int p = 0; p < PB; ++p) {
+                const int2 pyx = spoi[grp][p];
                 if (pyx.x < 0) continue;
-                const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
-                const int xa = x0 & ~15;
-                smis[grp][wi] = x0 - xa;
-                tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.map_tar : &jb.map_ref, xa, y0, tbar);
+                ymin = min(ymin, pyx.x); ymax = max(ymax, pyx.x);
+                xmin = min(xmin, pyx.y); xmax = max(xmax, pyx.y);
+            }
+            const int xau = (xmin - g.rx) & ~15;
+            const bool uni = jb.uw > 0 && ymin == ymax && xmax - g.rx + N - xau <= jb.uw;
+            if (uni) {
+                const int y0 = ymin - g.ry;
+                mbar_expect_tx(tbar, (uint32_t)(2 * N * jb.uw));
+                tma_load_2d(wwin, &jb.map_ref_u, xau, y0, tbar);
+                tma_load_2d(wwin + jb.utoff, &jb.map_tar_u, xau, y0, tbar);
+                wrs[grp] = jb.uw;
+                for (int p = 0; p < PB; ++p) {
+                    const int2 pyx = spoi[grp][p];
+                    const int xo = pyx.x < 0 ? 0 : pyx.y - g.rx - xau;
+                    wbase[grp][2 * p] = xo;
+                    wbase[grp][2 * p + 1] = jb.utoff + xo;
+                }
+            } else {
+                int nload = 0;
+                for (int wi = 0; wi < 2 * PB; ++wi) nload += spoi[grp][wi >> 1].x >= 0;
+                mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
+                wrs[grp] = BW;
+                for (int wi = 0; wi < 2 * PB; ++wi) {
+                    const int2 pyx = spoi[grp][wi >> 1];
+                    wbase[grp][wi] = wi * WS;  // read (harmlessly) by the row copies for absent POIs
+                    if (pyx.x < 0) continue;
+                    const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
+                    const int xa = x0 & ~15;
+                    wbase[grp][wi] = wi * WS + x0 - xa;
+                    tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.map_tar : &jb.map_ref, xa, y0, tbar);
+                }
             }
         }
         bool ok = mbar_wait(tbar, tphase);
@@ -357,7 +390,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         for (int rr = t; rr < s.tiles1 * 128; rr += 128) {
             const int wi = rr / N, x = rr - wi * N;
             const bool data = wi < 2 * PB && spoi[grp][wi >> 1].x >= 0;
-            const uint8_t* col = wwin + (data ? wi : 0) * WS + (data ? smis[grp][wi] : 0) + x;
+            const int rs = wrs[grp];
+            const uint8_t* col = wwin + (data ? wbase[grp][wi] : 0) + x;
             uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
             const int row = rr & 127;
             int su = 0, sq = 0;
@@ -367,7 +401,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int y = c * 8 + j;
-                    const int val = (data && y < N) ? (int)col[y * BW] : 0;
+                    const int val = (data && y < N) ? (int)col[y * rs] : 0;
                     su += val;
                     sq += val * val;
                     f[j] = (float)val;
@@ -779,8 +813,9 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const int ky = idx / N, kx = idx - ky * N;
                 int yy = y + ky;
                 if (yy >= N) yy -= N;
-                const uint8_t* fb = wwin + (2 * p) * WS + smis[grp][2 * p] + y * BW;
-                const uint8_t* gb = wwin + (2 * p + 1) * WS + smis[grp][2 * p + 1] + yy * BW;
+                const int rs = wrs[grp];
+                const uint8_t* fb = wwin + wbase[grp][2 * p] + y * rs;
+                const uint8_t* gb = wwin + wbase[grp][2 * p + 1] + yy * rs;
                 const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
                 unsigned acc = 0;
                 int j = rot;
@@ -1034,12 +1069,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // 8-bit image as a 2D tensor (x = column, y = row) read in boxes of
 // BW x N bytes; reads outside the image are zero-filled
-bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape& s) {
+bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape& s, int box_w = 0) {
     auto fn = encode_fn();
     if (!fn) return false;
     const cuuint64_t dims[2] = {(cuuint64_t)g.img_w, (cuuint64_t)g.img_h};
     const cuuint64_t strides[1] = {(cuuint64_t)g.pitch};
-    const cuuint32_t box[2] = {(cuuint32_t)s.BW, (cuuint32_t)s.N};
+    const cuuint32_t box[2] = {(cuuint32_t)(box_w > 0 ? box_w : s.BW), (cuuint32_t)s.N};
     const cuuint32_t estr[2] = {1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(img), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1067,6 +1102,15 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
         TcJob& o = J->job[j];
         if (!image_map(&o.map_ref, g, in.ref, s) || !image_map(&o.map_tar, g, in.tar, s))
             return cudaErrorNotSupported;
+        // one box per image for a batch on one POI row: PB windows at the grid
+        // step apart, x aligned down to 16 bytes; used when both boxes (and 8
+        // bytes of read slack) fit the window region and the box width is at
+        // most 256
+        o.uw = round_up((s.PB - 1) * g.grid_x + s.N + 15, 16);
+        o.utoff = round_up(s.N * o.uw, 128);
+        if (s.PB < 2 || g.grid_x <= 0 || o.uw > 256 || o.utoff + s.N * o.uw + 16 > 2 * s.PB * s.WS ||
+            !image_map(&o.map_ref_u, g, in.ref, s, o.uw) || !image_map(&o.map_tar_u, g, in.tar, s, o.uw))
+            o.uw = 0;
         o.g = g;
         o.poi = in.poi;
         o.u = in.u;

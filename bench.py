@@ -386,11 +386,11 @@ def _run_gpu(args, world, rank, local, torch):
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
 # profiles/k_icgn_warp_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
-NCU_TRAFFIC = {"k_icgn_warp": 123.65e6 + 6.98e6, "k_fftcc_tc": 9.61e6 + 0.0}
+NCU_TRAFFIC = {"k_icgn_warp": 123.65e6 + 6.85e6, "k_fftcc_tc": 9.60e6 + 0.0}
 # from the same IC-GN capture: L1 hit rate of its gathers and the FMA-heavy
 # pipe's share of cycles (the kernel's limiter)
-NCU_ICGN_L1_HIT = 0.897
-NCU_ICGN_FMAHEAVY = 0.709
+NCU_ICGN_L1_HIT = 0.891
+NCU_ICGN_FMAHEAVY = 0.680
 
 
 def roofline(g, P, ph, kbar):
@@ -404,8 +404,8 @@ def roofline(g, P, ph, kbar):
     (statistics 64 B, FP64 inverse Hessian 168 B, flag 1 B), the POI (8 B),
     u/v in (8 B) and out (8 B), p6 (24 B), iteration count (4 B) and flag
     (1 B).  The kernel is not HBM bound: its per-sample gathers (k*S*20 B per
-    POI, k = mean iterations) are served by L1 (90 % hits) and L2, and it is
-    limited by the SM's FP32 / integer pipes (FMA-heavy pipe busy 71 % of
+    POI, k = mean iterations) are served by L1 (89 % hits) and L2, and it is
+    limited by the SM's FP32 / integer pipes (FMA-heavy pipe busy 68 % of
     cycles); the gather and FP32 views are reported beside it, with the
     tensor-core view of the FFT-CC kernel (48 N^3 flops per POI)."""
     peaks = {}

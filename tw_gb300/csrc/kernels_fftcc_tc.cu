@@ -684,6 +684,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             const int sbo = 18 * K4;
 #pragma unroll
             for (int x0 = 0; x0 < NP; x0 += 8) {
+                if (x0 >= N) break;  // columns N .. NP-1 are padding (N is even: N..N+7 too when N % 8)
                 float re[8], im[8];
                 tmem_ld8(tm_warp + x0, re);
                 tmem_ld8(tm_warp + NP + x0, im);
@@ -737,6 +738,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         int bi = 0x7fffffff;
 #pragma unroll
         for (int y0 = 0; y0 < NP; y0 += 8) {
+            if (y0 >= N) break;  // padding columns
             float cv[8];
             tmem_ld8(tm_warp + y0, cv);
             tmem_ld_wait();
@@ -767,6 +769,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             if (__any_sync(kFull, live && bv >= th)) {
 #pragma unroll
             for (int y0 = 0; y0 < NP; y0 += 8) {
+                if (y0 >= N) break;  // padding columns
                 float cv[8];
                 tmem_ld8(tm_warp + y0, cv);
                 tmem_ld_wait();

@@ -15,15 +15,15 @@ def _params(g, path=PATH_FAST):
 
 def test_frame_device_bytes_formula():
     """Host-only estimate used for admission: images padded to 16-byte rows,
-    per-POI buffers and the fast path's cache and neighbourhood table, each
-    rounded up to 2 MiB."""
+    per-POI buffers and the fast path's cache, gradient image and
+    neighbourhood table, each rounded up to 2 MiB."""
     _, g = synth.small_case(h=160, w=197, r=10, grid=7)
     p = _params(g)
     n = dic.num_pois(p)[0] * dic.num_pois(p)[1]
     r = lambda b: -(-b // (2 << 20)) * (2 << 20)  # noqa: E731
     pitch = (197 + 15) // 16 * 16
     want = (2 * r(pitch * 160) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 3 * r(1024)
-            + r(64 * n) + r(168 * n) + r(n) + r(16 * g.roi_w * g.roi_h))
+            + r(64 * n) + r(168 * n) + r(n) + r(4 * g.roi_w * g.roi_h) + r(16 * g.roi_w * g.roi_h))
     assert frame_device_bytes(p) == want
     big = _params(synth.Geometry(2048, 2048, 1, 1, 2046, 2046, 20, 5, 20))
     assert frame_device_bytes(big) > 128 << 20  # 155k POIs: 67 MB neighbourhood table, 36 MB cache

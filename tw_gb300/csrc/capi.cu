@@ -672,6 +672,7 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
         t += r(64 * (uint64_t)p->roi_width * p->roi_height);  // float LUT
     } else {
         t += r(64 * n) + r(168 * n) + r(n);                 // statistics, inverse Hessian, flags
+        t += r(4 * (uint64_t)p->roi_width * p->roi_height);   // reference gradient image (half2)
         t += r(16 * (uint64_t)p->roi_width * p->roi_height);  // neighbourhood table
     }
     *bytes = t;

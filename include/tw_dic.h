@@ -349,6 +349,18 @@ TWDIC_API int twdic_poll(twdic_server* s, uint64_t ticket, int32_t wait, float* 
                          float* p6, int32_t* iters, uint8_t* flags, double* latency_ms);
 TWDIC_API int twdic_server_resume(twdic_server* s);
 TWDIC_API int twdic_server_stats(twdic_server* s, twdic_server_counters* out);
+/* One camera stream's statistics (FFTCCTWorkerThread::updateFPS,
+ * TW/TW_Core/fftcctworkerthread.cpp:574-605): frames completed and dropped,
+ * submit-to-done latency percentiles, and the reference's average processing
+ * rate -- the integer mean of 1000 / (integer milliseconds between two
+ * completed frames) over the last 32 frames, refreshed every 32 frames (0
+ * until the first 32). */
+typedef struct {
+    uint64_t completed, dropped;
+    int32_t average_fps;
+    double p50_ms, p99_ms;
+} twdic_stream_stats;
+TWDIC_API int twdic_server_stream_stats(twdic_server* s, int32_t stream_id, twdic_stream_stats* out);
 TWDIC_API int twdic_server_destroy(twdic_server* s);
 
 /* ---- tracking loop (FFTCCTWorkerThread::processFrameFFTCC /

@@ -104,4 +104,28 @@ def test_full_queue_drops_frames():
         np.testing.assert_array_equal(a[k], b[k])
     st = srv.stats()
     assert st["dropped"] == 1 and st["completed"] == 2
+    ss = srv.stream_stats(sid)
+    assert ss["dropped"] == 1 and ss["completed"] == 2 and ss["p50_ms"] <= ss["p99_ms"]
+    assert ss["average_fps"] == 0  # fewer than 32 completed frames
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_stream_fps_statistics():
+    """The reference's processing-rate statistic per stream: after 32 paced
+    frames its average FPS is set, and it lies within the rates the frame
+    spacing allows."""
+    import time
+    pair, g = synth.small_case()
+    srv = DICServer(queue_depth=4)
+    sid = srv.add_stream(_params(g))
+    srv.set_reference(sid, pair.ref)
+    for _ in range(34):
+        t = srv.submit(sid, pair.tar)
+        assert t is not None
+        srv.poll(sid, t)
+        time.sleep(0.01)  # at most 100 frames per second
+    ss = srv.stream_stats(sid)
+    assert ss["completed"] == 34 and ss["dropped"] == 0
+    assert 10 <= ss["average_fps"] <= 100, ss
     srv.close()

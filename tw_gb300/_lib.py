@@ -44,7 +44,7 @@ EXPORTED = (
     "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_icgn_unroll", "twdic_batch_set_graph",
     "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
-    "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_destroy",
+    "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_stream_stats", "twdic_server_destroy",
     "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
     "twdic_tracker_create", "twdic_tracker_num_pois", "twdic_tracker_process", "twdic_tracker_colormap",
     "twdic_tracker_destroy", "twdic_icgn_set_interpolation", "twdic_frame_set_interpolation",
@@ -89,6 +89,14 @@ class Tuning(ctypes.Structure):
         ("fftcc_use_tc", ctypes.c_int32), ("fftcc_groups", ctypes.c_int32), ("fftcc_pois_per_group", ctypes.c_int32),
         ("fftcc_ms", ctypes.c_float), ("icgn_ms", ctypes.c_float), ("from_cache", ctypes.c_int32),
         ("icgn_chunk", ctypes.c_int32), ("icgn_unroll", ctypes.c_int32),
+    ]
+
+
+class StreamStats(ctypes.Structure):
+    """twdic_stream_stats"""
+    _fields_ = [
+        ("completed", ctypes.c_uint64), ("dropped", ctypes.c_uint64), ("average_fps", ctypes.c_int32),
+        ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
     ]
 
 
@@ -165,6 +173,7 @@ def load():
                         ctypes.POINTER(ctypes.c_double)], _I),
         "twdic_server_resume": ([_VP], _I),
         "twdic_server_stats": ([_VP, ctypes.POINTER(ServerCounters)], _I),
+        "twdic_server_stream_stats": ([_VP, _I, ctypes.POINTER(StreamStats)], _I),
         "twdic_server_destroy": ([_VP], _I),
         "twdic_frame_set_fftcc_tuning": ([_VP, _I, _I, _I], _I),
         "twdic_frame_get_tuning": ([_VP, ctypes.POINTER(Tuning)], _I),

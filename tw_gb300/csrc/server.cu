@@ -71,7 +71,39 @@ struct CamStream {
     float *d_u = nullptr, *d_v = nullptr, *d_z = nullptr, *d_p6 = nullptr;
     int32_t* d_it = nullptr;
     uint8_t* d_fl = nullptr;
+    // per-stream statistics: counters, latencies, and the processing rate of
+    // FFTCCTWorkerThread::updateFPS (TW/TW_Core/fftcctworkerthread.cpp:574-605)
+    uint64_t completed = 0, dropped = 0;
+    std::vector<double> lat_ms;
+    bool has_done = false;
+    Clock::time_point last_done;
+    std::deque<int> fps_q;  // instantaneous rates, at most kFpsWindow
+    int fps_samples = 0, fps_avg = 0;
 };
+
+// PROCESSING_FPS_STAT_QUEUE_LENGTH (TW/TW_Core/Structures.h:26)
+constexpr int kFpsWindow = 32;
+
+// updateFPS: the rate 1000 / elapsed (integer milliseconds between two
+// completed frames of the stream, integer division) joins a queue of at most
+// kFpsWindow values; every kFpsWindow samples, once the queue is full, the
+// average is their integer mean and the sample count restarts.
+void fps_update(CamStream& cs, int elapsed_ms) {
+    if (elapsed_ms > 0) {
+        cs.fps_q.push_back(1000 / elapsed_ms);
+        cs.fps_samples += 1;
+    }
+    if ((int)cs.fps_q.size() > kFpsWindow) cs.fps_q.pop_front();
+    if ((int)cs.fps_q.size() == kFpsWindow && cs.fps_samples == kFpsWindow) {
+        int sum = 0;
+        while (!cs.fps_q.empty()) {
+            sum += cs.fps_q.front();
+            cs.fps_q.pop_front();
+        }
+        cs.fps_avg = sum / kFpsWindow;
+        cs.fps_samples = 0;
+    }
+}
 
 struct Lane {
     cudaStream_t st = nullptr;
@@ -248,8 +280,15 @@ void retire(twdic_server* s, Lane& lane) {
         sl.state = lane.rc == TWDIC_OK ? kDone : kFailed;
         cs.busy = false;
         if (lane.rc == TWDIC_OK) {
+            const double ms = std::chrono::duration<double, std::milli>(sl.t_done - sl.t_submit).count();
             s->completed += 1;
-            s->lat_ms.push_back(std::chrono::duration<double, std::milli>(sl.t_done - sl.t_submit).count());
+            s->lat_ms.push_back(ms);
+            cs.completed += 1;
+            cs.lat_ms.push_back(ms);
+            if (cs.has_done)
+                fps_update(cs, (int)std::chrono::duration_cast<std::chrono::milliseconds>(now - cs.last_done).count());
+            cs.has_done = true;
+            cs.last_done = now;
         }
     }
     lane.work.clear();
@@ -436,6 +475,7 @@ int twdic_submit(twdic_server* s, int32_t stream_id, const uint8_t* tar, int32_t
     s->submitted += 1;
     if (si < 0) {
         s->dropped += 1;
+        cs.dropped += 1;
         return fail_msg(TWDIC_ERR_BUSY, "stream queue full: frame dropped");
     }
     Slot& sl = cs.slots[si];
@@ -523,6 +563,26 @@ int twdic_server_stats(twdic_server* s, twdic_server_counters* out) {
         out->p50_ms = q(0.50);
         out->p99_ms = q(0.99);
         out->max_ms = l.back();
+    }
+    return TWDIC_OK;
+}
+
+int twdic_server_stream_stats(twdic_server* s, int32_t stream_id, twdic_stream_stats* out) {
+    if (!s || !out) return fail_msg(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->streams.find(stream_id);
+    if (it == s->streams.end()) return fail_msg(TWDIC_ERR_INVALID_ARG, "unknown stream id");
+    const CamStream& cs = *it->second;
+    std::memset(out, 0, sizeof(*out));
+    out->completed = cs.completed;
+    out->dropped = cs.dropped;
+    out->average_fps = cs.fps_avg;
+    if (!cs.lat_ms.empty()) {
+        std::vector<double> l = cs.lat_ms;
+        std::sort(l.begin(), l.end());
+        auto q = [&](double f) { return l[std::min(l.size() - 1, (size_t)(f * (l.size() - 1) + 0.5))]; };
+        out->p50_ms = q(0.50);
+        out->p99_ms = q(0.99);
     }
     return TWDIC_OK;
 }

@@ -87,6 +87,13 @@ class DICServer:
         check(self._lib.twdic_server_stats(self._h, ctypes.byref(c)))
         return {k: getattr(c, k) for k, _ in ServerCounters._fields_}
 
+    def stream_stats(self, stream_id: int) -> dict:
+        """One stream's completed and dropped frames, latency percentiles and
+        the reference's average processing FPS (see twdic_server_stream_stats)."""
+        c = _lib.StreamStats()
+        check(self._lib.twdic_server_stream_stats(self._h, stream_id, ctypes.byref(c)))
+        return {k: getattr(c, k) for k, _ in _lib.StreamStats._fields_}
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.twdic_server_destroy(self._h)

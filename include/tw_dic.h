@@ -203,6 +203,13 @@ TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_
  * so the subsets in flight on an SM overlap and are re-read from L1, and the
  * reference gradients come from a per-reference image (4 B per ROI pixel). */
 TWDIC_API int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk);
+/* Initial guesses of a frame handle in batched calls (twdic_batch_process and
+ * the server): mode 0 (default) runs FFT-CC and starts IC-GN from its integer
+ * displacements, as FFTCCTWorkerThread::processFrameFFTCC_ICGN does; mode 1
+ * skips FFT-CC and starts IC-GN from the u, v arrays passed in (in/out, as
+ * cuICGN2D::cuCompute's U, V), e.g. the previous frame's displacements of a
+ * camera stream; ZNCC is then not written. */
+TWDIC_API int twdic_frame_set_guess_mode(twdic_frame* h, int mode);
 /* Unrolling of the IC-GN sample loop (2, 4 or 8; default 8) for the one-POI-per-warp
  * layout with 1024-thread CTAs (other shapes unroll by 4). */
 TWDIC_API int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll);
@@ -361,6 +368,12 @@ typedef struct {
     double p50_ms, p99_ms;
 } twdic_stream_stats;
 TWDIC_API int twdic_server_stream_stats(twdic_server* s, int32_t stream_id, twdic_stream_stats* out);
+/* Last-frame guesses for one camera stream: mode 1 keeps each frame's
+ * displacements on the device and starts the next frame's IC-GN from them,
+ * skipping FFT-CC (ZNCC is not written); the first frame after
+ * twdic_server_set_reference runs FFT-CC.  Mode 0 (default): FFT-CC every
+ * frame, the reference's behaviour. */
+TWDIC_API int twdic_server_set_stream_guess(twdic_server* s, int32_t stream_id, int mode);
 TWDIC_API int twdic_server_destroy(twdic_server* s);
 
 /* ---- tracking loop (FFTCCTWorkerThread::processFrameFFTCC /

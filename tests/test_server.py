@@ -129,3 +129,38 @@ def test_stream_fps_statistics():
     assert ss["completed"] == 34 and ss["dropped"] == 0
     assert 10 <= ss["average_fps"] <= 100, ss
     srv.close()
+
+
+@pytest.mark.gpu
+def test_last_frame_guesses():
+    """Guess mode 1: after the first frame of a reference, IC-GN starts from
+    the stream's last displacements on the device and FFT-CC is skipped. On a
+    drifting camera sequence every frame still meets the parity bar against
+    FFT-CC-seeded IC-GN (the oracle), and a new reference restarts from FFT-CC."""
+    from oracle import oracle as O
+    ref, tars, g = synth.camera_sequence(200, 176, frames=4, seed=41, r=10, grid=9, margin=12)
+    p = _params(g)
+    poi = dic.poi_positions(p)
+    srv = DICServer(queue_depth=2)
+    sid = srv.add_stream(p)
+    srv.set_stream_guess(sid, 1)
+    for rnd in range(2):  # the second round after a fresh reference
+        srv.set_reference(sid, ref)
+        first = None
+        for tar in tars:
+            t = srv.submit(sid, tar)
+            assert t is not None
+            out = srv.poll(sid, t)
+            if first is None:
+                first = out
+            else:  # no FFT-CC ran: the ZNCC array still holds the first frame's
+                np.testing.assert_array_equal(out["zncc"], first["zncc"])
+                assert (out["u"] != first["u"]).any()
+            u_or, v_or, _, _ = O.fftcc(ref, tar, poi, g.subset_r)
+            p6_or, it_or, fl_or = O.icgn(ref, tar, g, poi, u_or, v_or)
+            both = (out["flags"] == 0) & (fl_or == 0)
+            assert both.mean() > 0.9
+            bad = (np.abs(out["u"] - p6_or[:, 0]) > 1e-3) | (np.abs(out["v"] - p6_or[:, 3]) > 1e-3)
+            assert bad[both].sum() <= 0.01 * both.sum() + 1, (rnd, bad[both].sum())
+    assert srv.stream_stats(sid)["completed"] == 2 * len(tars)
+    srv.close()

@@ -40,11 +40,11 @@ EXPORTED = (
     "twdic_icgn_create", "twdic_icgn_reset_ref", "twdic_icgn_compute", "twdic_icgn_destroy",
     "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
-    "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_icgn_unroll", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
+    "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_icgn_unroll", "twdic_frame_set_guess_mode", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
     "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_icgn_unroll", "twdic_batch_set_graph",
     "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
-    "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_stream_stats", "twdic_server_destroy",
+    "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_stream_stats", "twdic_server_set_stream_guess", "twdic_server_destroy",
     "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
     "twdic_tracker_create", "twdic_tracker_num_pois", "twdic_tracker_process", "twdic_tracker_colormap",
     "twdic_tracker_destroy", "twdic_icgn_set_interpolation", "twdic_frame_set_interpolation",
@@ -152,6 +152,7 @@ def load():
         "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
         "twdic_frame_set_icgn_layout": ([_VP, _I], _I),
         "twdic_frame_set_icgn_unroll": ([_VP, _I], _I),
+        "twdic_frame_set_guess_mode": ([_VP, _I], _I),
         "twdic_frame_set_fftcc_twiddles": ([_VP, _I], _I),
         "twdic_icgn_compute_noalloc": ([P, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP], _I),
         "twdic_batch_create": ([ctypes.POINTER(_VP)], _I),
@@ -174,6 +175,7 @@ def load():
         "twdic_server_resume": ([_VP], _I),
         "twdic_server_stats": ([_VP, ctypes.POINTER(ServerCounters)], _I),
         "twdic_server_stream_stats": ([_VP, _I, ctypes.POINTER(StreamStats)], _I),
+        "twdic_server_set_stream_guess": ([_VP, _I, _I], _I),
         "twdic_server_destroy": ([_VP], _I),
         "twdic_frame_set_fftcc_tuning": ([_VP, _I, _I, _I], _I),
         "twdic_frame_get_tuning": ([_VP, ctypes.POINTER(Tuning)], _I),

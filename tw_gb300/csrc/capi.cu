@@ -149,6 +149,9 @@ struct Engine {
     IcgnTune icgn_tune;
     FftccTune fftcc_tune;
     int interp = TWDIC_INTERP_BICUBIC;  // target interpolation of IC-GN (ICGN2DInterpolationFLag)
+    // batched calls: 1 = no FFT-CC, IC-GN starts from the u, v arrays passed in
+    // (the last frame's displacements); 0 = FFT-CC then IC-GN
+    int guess = 0;
 
     DevBuf d_ref, d_tar, d_poi;
     DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work, d_tw;
@@ -719,6 +722,13 @@ int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk) {
     return TWDIC_OK;
 }
 
+int twdic_frame_set_guess_mode(twdic_frame* h, int mode) {
+    if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
+    if (mode != 0 && mode != 1) return fail(TWDIC_ERR_INVALID_ARG, "guess mode must be 0 or 1");
+    h->e.guess = mode;
+    return TWDIC_OK;
+}
+
 int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
     if (unroll != 2 && unroll != 4 && unroll != 8) return fail(TWDIC_ERR_INVALID_ARG, "unroll must be 2, 4 or 8");
@@ -1043,11 +1053,20 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         TW_TRY(e.set_tar(a.tars[i], a.strides ? a.strides[i] : 0, a.mem_in));
         const FrameOut o = frame_out(e, a, i);
         const size_t n = (size_t)e.n;
+        const bool fast = e.prm.path == TWDIC_PATH_FAST;
+        TW_CUDA(cudaMemsetAsync(o.it, 0, 4 * n, b->stream));
+        if (e.guess) {
+            // IC-GN from the displacements in u, v (ZNCC is not recomputed)
+            if (a.mem_out == TWDIC_MEM_HOST) {
+                TW_CUDA(cudaMemcpyAsync(o.u, a.u[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
+                TW_CUDA(cudaMemcpyAsync(o.v, a.v[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
+            }
+            if (fast && e.interp == TWDIC_INTERP_BICUBIC) fast_ic.push_back(i);
+            continue;
+        }
         TW_CUDA(cudaMemsetAsync(o.u, 0, 4 * n, b->stream));
         TW_CUDA(cudaMemsetAsync(o.v, 0, 4 * n, b->stream));
         TW_CUDA(cudaMemsetAsync(o.z, 0, 4 * n, b->stream));
-        TW_CUDA(cudaMemsetAsync(o.it, 0, 4 * n, b->stream));
-        const bool fast = e.prm.path == TWDIC_PATH_FAST;
         if (fast && e.fftcc_tune.use_tc && fftcc_tc_supported(e.g))
             fast_tc.push_back(i);
         else
@@ -1239,7 +1258,8 @@ int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frame
         for (int i = 0; i < count; ++i) {
             const Engine& e = frames[i]->e;
             caches_ok = caches_ok && e.cache_valid;
-            for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)tars[i], (uintptr_t)(strides ? strides[i] : 0),
+            for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)e.guess, (uintptr_t)tars[i],
+                                (uintptr_t)(strides ? strides[i] : 0),
                                 (uintptr_t)u[i], (uintptr_t)v[i], (uintptr_t)(zncc ? zncc[i] : nullptr),
                                 (uintptr_t)(p6 ? p6[i] : nullptr), (uintptr_t)(iters ? iters[i] : nullptr),
                                 (uintptr_t)(flags ? flags[i] : nullptr)})

@@ -66,6 +66,10 @@ struct CamStream {
     std::deque<int> queue;  // slot indices, oldest first
     bool busy = false;      // a frame of this stream is in a batch in flight
     bool has_ref = false;
+    // guesses: 1 = after a completed frame of the current reference, IC-GN starts
+    // from the last displacements (still in d_u, d_v) and FFT-CC is skipped
+    int guess_mode = 0;
+    bool has_guess = false;
     void* d_block = nullptr;
     uint8_t* d_tar = nullptr;
     float *d_u = nullptr, *d_v = nullptr, *d_z = nullptr, *d_p6 = nullptr;
@@ -227,6 +231,7 @@ int launch_batch(twdic_server* s, Lane& lane, std::vector<CamStream*>& picked) {
         cs->busy = true;
         lane.work.emplace_back(cs->id, si);
         frames[i] = cs->frame;
+        if (rc == TWDIC_OK) rc = twdic_frame_set_guess_mode(cs->frame, cs->guess_mode && cs->has_guess ? 1 : 0);
         tars[i] = cs->d_tar;
         u[i] = cs->d_u;
         v[i] = cs->d_v;
@@ -285,6 +290,7 @@ void retire(twdic_server* s, Lane& lane) {
             s->lat_ms.push_back(ms);
             cs.completed += 1;
             cs.lat_ms.push_back(ms);
+            cs.has_guess = true;
             if (cs.has_done)
                 fps_update(cs, (int)std::chrono::duration_cast<std::chrono::milliseconds>(now - cs.last_done).count());
             cs.has_done = true;
@@ -455,7 +461,10 @@ int twdic_server_set_reference(twdic_server* s, int32_t stream_id, const uint8_t
     s->cv_done.wait(lk, [&] { return !it->second->busy; });
     CamStream& cs = *it->second;
     const int rc = twdic_frame_set_reference(cs.frame, img, stride, TWDIC_MEM_HOST);
-    if (rc == TWDIC_OK) cs.has_ref = true;
+    if (rc == TWDIC_OK) {
+        cs.has_ref = true;
+        cs.has_guess = false;  // the next frame starts from FFT-CC again
+    }
     lk.unlock();
     s->cv_sched.notify_all();
     return rc;
@@ -564,6 +573,16 @@ int twdic_server_stats(twdic_server* s, twdic_server_counters* out) {
         out->p99_ms = q(0.99);
         out->max_ms = l.back();
     }
+    return TWDIC_OK;
+}
+
+int twdic_server_set_stream_guess(twdic_server* s, int32_t stream_id, int mode) {
+    if (!s) return fail_msg(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    if (mode != 0 && mode != 1) return fail_msg(TWDIC_ERR_INVALID_ARG, "guess mode must be 0 or 1");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->streams.find(stream_id);
+    if (it == s->streams.end()) return fail_msg(TWDIC_ERR_INVALID_ARG, "unknown stream id");
+    it->second->guess_mode = mode;
     return TWDIC_OK;
 }
 

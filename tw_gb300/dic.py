@@ -286,6 +286,11 @@ class DICFrame:
         consecutive POIs (threads 128 to 1024, a table sampler)."""
         check(self._lib.twdic_frame_set_icgn_layout(self._h, chunk))
 
+    def set_guess_mode(self, mode):
+        """Batched calls: 1 skips FFT-CC and starts IC-GN from the u, v passed
+        in (e.g. the last frame's); 0 (default) runs FFT-CC."""
+        check(self._lib.twdic_frame_set_guess_mode(self._h, mode))
+
     def set_icgn_unroll(self, unroll):
         """Unrolling of the IC-GN sample loop: 2, 4 or 8 (default)."""
         check(self._lib.twdic_frame_set_icgn_unroll(self._h, unroll))

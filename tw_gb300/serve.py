@@ -87,6 +87,12 @@ class DICServer:
         check(self._lib.twdic_server_stats(self._h, ctypes.byref(c)))
         return {k: getattr(c, k) for k, _ in ServerCounters._fields_}
 
+    def set_stream_guess(self, stream_id: int, mode: int):
+        """1: each frame's IC-GN starts from the stream's last displacements
+        (FFT-CC skipped after the first frame of a reference); 0: FFT-CC every
+        frame (default)."""
+        check(self._lib.twdic_server_set_stream_guess(self._h, stream_id, mode))
+
     def stream_stats(self, stream_id: int) -> dict:
         """One stream's completed and dropped frames, latency percentiles and
         the reference's average processing FPS (see twdic_server_stream_stats)."""

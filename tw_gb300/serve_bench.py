@@ -25,7 +25,9 @@ RESOLUTIONS = [(640, 480), (1280, 1024), (2048, 2048)]
 
 
 def run_serving(seconds=4.0, streams_per_res=4, lanes=2, max_batch=32, queue_depth=4, seed=5, data=None,
-                use_graph=True):
+                use_graph=True, guesses=False):
+    """guesses: every stream starts each frame's IC-GN from its last
+    displacements (twdic_server_set_stream_guess) instead of FFT-CC."""
     import numpy as np
     from tw_gb300 import dic, synth
     from tw_gb300.serve import DICServer
@@ -43,6 +45,8 @@ def run_serving(seconds=4.0, streams_per_res=4, lanes=2, max_batch=32, queue_dep
         nx, ny = dic.num_pois(p)
         for _ in range(streams_per_res):
             sid = srv.add_stream(p)
+            if guesses:
+                srv.set_stream_guess(sid, 1)
             srv.set_reference(sid, ref)
             streams.append(dict(sid=sid, res=res, tars=tars, n=nx * ny, fps=float(rng.uniform(30, 120))))
     # warm-up: one frame per stream (reference precompute, first tables)
@@ -101,7 +105,7 @@ def run_serving(seconds=4.0, streams_per_res=4, lanes=2, max_batch=32, queue_dep
                                                                RESOLUTIONS)
                        + "; 31x31 subsets (r = 15), step 8, margin 20; Poisson arrivals, rates U[30, 120] fps",
            "seconds": round(wall, 3), "lanes": lanes, "max_batch": max_batch, "queue_depth": queue_depth,
-           "graph": use_graph, "per_resolution": {}}
+           "graph": use_graph, "initial_guesses": "last frame" if guesses else "FFT-CC", "per_resolution": {}}
     pois = 0
     for res in RESOLUTIONS:
         lat = sorted(l for s, l in results if s["res"] == res)

@@ -183,7 +183,9 @@ TWDIC_API int twdic_frame_destroy(twdic_frame* h);
  * TWDIC_INTERP_BICUBIC, the Hermite bicubic LUT (BicubicCoefficients_s,
  * TW_utils.cpp:604-700; the default), or TWDIC_INTERP_BSPLINE, the bicubic
  * B-spline LUT (BicubicSplineCoefficients_s, TW_utils.cpp:521-602; every ROI
- * pixel has coefficients, image pixels outside the image read as 0). */
+ * pixel has coefficients, image pixels outside the image read as 0).  The fast
+ * path evaluates either from the 16-byte neighbourhood table (the default
+ * sampler) or from the coefficient LUT (sampler 1). */
 #define TWDIC_INTERP_BICUBIC 0
 #define TWDIC_INTERP_BSPLINE 1
 TWDIC_API int twdic_icgn_set_interpolation(twdic_icgn* h, int mode);

@@ -300,11 +300,15 @@ struct Engine {
         return icgn_solve(u, v, p6, iters, flags);
     }
 
-    // Per-target preparation: the bicubic coefficient LUT of the target
-    // (TW_utils.cpp:604-700), when the IC-GN variant reads one.
+    // Per-target preparation: the table the IC-GN variant reads, the bicubic
+    // (TW_utils.cpp:604-700) or B-spline (TW_utils.cpp:521-602) coefficient
+    // LUT of the target or its 4x4 neighbourhood table.
     int prepare_target() {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "IC-GN needs a reference and a target image");
-        if (interp == TWDIC_INTERP_BSPLINE) {
+        if (interp == TWDIC_INTERP_BSPLINE && prm.path == TWDIC_PATH_FAST && solve_tune().sampler == kSampNbhdBs) {
+            TW_TRY(d_lut.ensure(sizeof(uint4) * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_nbhd_table(g, d_tar.as<uint8_t>(), d_lut.as<uint4>(), stream, true));
+        } else if (interp == TWDIC_INTERP_BSPLINE) {
             TW_TRY(d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
             TW_CUDA(launch_bspline_lut(g, d_tar.as<uint8_t>(), d_lut.as<float4>(), stream));
         } else if (prm.path == TWDIC_PATH_PLAIN || icgn_tune.sampler == kSampLut) {
@@ -317,10 +321,12 @@ struct Engine {
         return TWDIC_OK;
     }
 
-    // the fast IC-GN launch shape; the B-spline interpolant is only in a LUT
+    // the fast IC-GN launch shape; B-spline from the neighbourhood table
+    // (kSampNbhdBs) or from its coefficient LUT (the window sampler is
+    // Catmull-Rom only)
     IcgnTune solve_tune() const {
         IcgnTune t = icgn_tune;
-        if (interp == TWDIC_INTERP_BSPLINE) t.sampler = kSampLut;
+        if (interp == TWDIC_INTERP_BSPLINE) t.sampler = t.sampler == kSampNbhd ? kSampNbhdBs : kSampLut;
         return t;
     }
 

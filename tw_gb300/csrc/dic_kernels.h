@@ -14,6 +14,7 @@ enum IcgnSampler {
     kSampWindow = 0,  // staged target window in shared memory, Catmull-Rom
     kSampLut = 1,     // per-frame float bicubic LUT (64 B per ROI pixel), Horner
     kSampNbhd = 2,    // per-frame 4x4 byte neighbourhood table (16 B per ROI pixel), Catmull-Rom
+    kSampNbhdBs = 3,  // the same table over every ROI pixel, the reference's B-spline interpolant
 };
 
 // Launch shape of the fast IC-GN kernel, chosen by the autotuner.
@@ -74,8 +75,10 @@ cudaError_t launch_ref_precompute_plain(const Geom& g, const uint8_t* ref, const
 cudaError_t launch_bicubic_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
 // B-spline coefficient LUT of the target, same layout (kernels_plain.cu)
 cudaError_t launch_bspline_lut(const Geom& g, const uint8_t* tar, float4* lut, cudaStream_t st);
-// 4x4 byte neighbourhoods of every ROI pixel of the target (kernels_icgn_fast.cu)
-cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st);
+// 4x4 byte neighbourhoods of every ROI pixel of the target (kernels_icgn_fast.cu);
+// full: the last ROI row and column too, bytes outside the image zero (the
+// B-spline sampler), otherwise those entries are zero (the bicubic samplers)
+cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st, bool full = false);
 cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi, int n, const float* subR,
                               const float2* sd, const float* chol, const float* refnorm, const uint8_t* rflag,
                               const float4* lut, float* u, float* v, float* p6, int* iters, uint8_t* flags,

@@ -174,22 +174,43 @@ __global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, con
 
 // 4x4 byte neighbourhood of every ROI pixel (i, j) of the target: rows
 // i-1 .. i+2, columns j-1 .. j+2 of the ROI-relative pixel, one 32-bit word
-// per row, lowest byte leftmost.  Zero on the ROI's last row and column, the
-// entries the reference's LUT never writes (TW_MemManager.cpp calloc).  The
-// ROI has one pixel of border on every side (validated on the host), and the
-// neighbourhood of the other last-but-one pixels stays inside the image.
-__global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __restrict__ table) {
+// per row, lowest byte leftmost.  Bicubic (full = 0): zero on the ROI's last
+// row and column, the entries the reference's LUT never writes
+// (TW_MemManager.cpp calloc).  The ROI has one pixel of border on every side
+// (validated on the host), and the neighbourhood of the other last-but-one
+// pixels stays inside the image.  B-spline (full = 1): every ROI pixel, with
+// the bytes outside the image zero, as the reference's B-spline LUT reads
+// them (TW_utils.cpp:521-602).
+__global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __restrict__ table, int full) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.rh || j >= g.rw) return;
     uint4 q = make_uint4(0u, 0u, 0u, 0u);
-    if (i != g.rh - 1 && j != g.rw - 1) {
-        const uint8_t* t = tar + (size_t)(i + g.sy - 1) * g.pitch + (j + g.sx - 1);
+    const int y0 = i + g.sy - 1, x0 = j + g.sx - 1;
+    if (!full && (i == g.rh - 1 || j == g.rw - 1)) {
+        // bicubic: the LUT's unwritten last row and column
+    } else if (y0 >= 0 && x0 >= 0 && y0 + 3 < g.img_h && x0 + 3 < g.img_w) {
+        const uint8_t* t = tar + (size_t)y0 * g.pitch + x0;
         uint32_t w[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const uint8_t* r = t + (size_t)a * g.pitch;
             w[a] = (uint32_t)r[0] | ((uint32_t)r[1] << 8) | ((uint32_t)r[2] << 16) | ((uint32_t)r[3] << 24);
+        }
+        q = make_uint4(w[0], w[1], w[2], w[3]);
+    } else {
+        // B-spline near the image edge: bytes outside the image are zero
+        uint32_t w[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            w[a] = 0u;
+            const int y = y0 + a;
+            if (y < 0 || y >= g.img_h) continue;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int x = x0 + b;
+                if (x >= 0 && x < g.img_w) w[a] |= (uint32_t)tar[(size_t)y * g.pitch + x] << (8 * b);
+            }
         }
         q = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -229,6 +250,42 @@ __device__ __forceinline__ float cr_combine4x4(float2 H01, float2 H23, float t) 
     const float f3 = fmaf(3.f, H01.y - H23.x, H23.y - H01.x);
     const float f0 = 2.f * H01.y;
     return fmaf(fmaf(fmaf(f3, t, f2), t, f1), t, f0);
+}
+
+// The reference's B-spline interpolant (BicubicSplineCoefficients_s,
+// TW_utils.cpp:521-602: the 4x4 neighbourhood prefiltered on both sides by
+// the local interpolation matrix CP, then mapped by the cubic B-spline basis
+// matrix Base) is a tensor product of one 4-tap filter whose weights are
+// cubics in the fraction: the rows of Base CP, powers of t increasing, are
+// (0, 1, 0, 0), (3/56) (-11, -1, 15, -3), (3/56) (19, -39, 25, -5) and
+// (1/7) (-3, 8, -8, 3).  Along one row of four pixels v0..v3 at fraction t
+//   h(t) = v1 + (3/56) t (e1 + t (e2 + (8/3) t e3)),
+//   e1 = -11 v0 - v1 + 15 v2 - 3 v3, e2 = 19 v0 - 39 v1 + 25 v2 - 5 v3,
+//   e3 = -3 v0 + 8 v1 - 8 v2 + 3 v3,
+// the integer coefficients by DP4A and v1 by the byte permute, as for
+// Catmull-Rom; the four row values are combined by the same weights in the
+// other fraction.
+__device__ __forceinline__ float2 bs_row_pair(uint32_t wa, uint32_t wb, float t) {
+    const float2 v1 = __fadd2_rn(make_float2(v1_biased(wa), v1_biased(wb)), make_float2(-12582912.0f, -12582912.0f));
+    const float2 e1 = make_float2((float)dp4a_us(wa, 0xFD0FFFF5u), (float)dp4a_us(wb, 0xFD0FFFF5u));  // (-11, -1, 15, -3)
+    const float2 e2 = make_float2((float)dp4a_us(wa, 0xFB19D913u), (float)dp4a_us(wb, 0xFB19D913u));  // (19, -39, 25, -5)
+    const float2 e3 = make_float2((float)dp4a_us(wa, 0x03F808FDu), (float)dp4a_us(wb, 0x03F808FDu));  // (-3, 8, -8, 3)
+    const float ta = (3.0f / 56.0f) * t, tb = (8.0f / 3.0f) * t;
+    return __ffma2_rn(__ffma2_rn(__ffma2_rn(e3, make_float2(tb, tb), e2), make_float2(t, t), e1), make_float2(ta, ta),
+                      v1);
+}
+// B-spline combination in fraction t of four row values (H01 = (h_0, h_1),
+// H23 = (h_2, h_3)): the interpolated value, with the scalings in the
+// weights ((3/56) e1 and (3/56) e2 together on the packed pipe).
+__device__ __forceinline__ float bs_combine4x4(float2 H01, float2 H23, float t) {
+    constexpr float k = 3.0f / 56.0f;
+    const float2 f12 = __ffma2_rn(
+        make_float2(H23.y, H23.y), make_float2(-3.f * k, -5.f * k),
+        __ffma2_rn(make_float2(H23.x, H23.x), make_float2(15.f * k, 25.f * k),
+                   __ffma2_rn(make_float2(H01.y, H01.y), make_float2(-k, -39.f * k),
+                              __fmul2_rn(make_float2(H01.x, H01.x), make_float2(-11.f * k, 19.f * k)))));
+    const float f3 = fmaf(3.0f / 7.0f, H23.y - H01.x, (8.0f / 7.0f) * (H01.y - H23.x));
+    return fmaf(fmaf(fmaf(f3, t, f12.y), t, f12.x), t, H01.y);
 }
 
 // Per-sample sums of one IC-GN pass on packed FP32: (sum t', sum t'^2),
@@ -334,7 +391,9 @@ __device__ __forceinline__ bool pass_out_of_roi_warp(const Geom& g, const float*
 //   kSampLut: the per-frame bicubic coefficient LUT (four float4 planes,
 //     k_bicubic_lut), evaluated by Horner's rule;
 //   kSampNbhd: the per-frame 4x4 neighbourhood table (16 bytes per ROI
-//     pixel, k_nbhd_table), one 16-byte gather per sample, Catmull-Rom.
+//     pixel, k_nbhd_table), one 16-byte gather per sample, Catmull-Rom;
+//   kSampNbhdBs: the same table over every ROI pixel, the reference's
+//     B-spline interpolant (bs_row_pair, bs_combine4x4).
 // The Catmull-Rom form with central-difference derivatives is algebraically
 // the reference's Hermite bicubic LUT (TW_utils.cpp:604-700).
 template <int THREADS, int SAMPLER, bool MULTI>
@@ -488,6 +547,10 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
                             const uint4 q = nb0[(size_t)iy * g.rw + ix];
                             const float2 h01 = cr_row_pair(q.x, q.y, fx), h23 = cr_row_pair(q.z, q.w, fx);
                             tp = fmaf(0.5f, cr_combine4x4(h01, h23, fy), -c);
+                        } else if (SAMPLER == kSampNbhdBs) {
+                            const uint4 q = nb0[(size_t)iy * g.rw + ix];
+                            const float2 h01 = bs_row_pair(q.x, q.y, fx), h23 = bs_row_pair(q.z, q.w, fx);
+                            tp = bs_combine4x4(h01, h23, fy) - c;
                         } else if (SAMPLER == kSampLut) {
                             const float4* q = lut0 + ((size_t)iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
@@ -734,6 +797,10 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                             const uint4 q = nb0[(unsigned)(iy * g.rw + ix)];  // < 2^31 entries
                             const float2 h01 = cr_row_pair(q.x, q.y, fx), h23 = cr_row_pair(q.z, q.w, fx);
                             tp = fmaf(0.5f, cr_combine4x4(h01, h23, fy), -c);
+                        } else if (SAMPLER == kSampNbhdBs) {
+                            const uint4 q = nb0[(unsigned)(iy * g.rw + ix)];
+                            const float2 h01 = bs_row_pair(q.x, q.y, fx), h23 = bs_row_pair(q.z, q.w, fx);
+                            tp = bs_combine4x4(h01, h23, fy) - c;
                         } else {
                             const float4* q = lut0 + (unsigned)(iy * g.rw + ix);
                             const float4 a0 = q[0], a1 = q[plane], a2 = q[2 * plane], a3 = q[3 * plane];
@@ -872,9 +939,9 @@ cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st) {
+cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st, bool full) {
     dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
-    k_nbhd_table<<<grd, blk, 0, st>>>(g, tar, table);
+    k_nbhd_table<<<grd, blk, 0, st>>>(g, tar, table, full ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -976,6 +1043,7 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
                  : launch_icgn_warp_t<NW, SA, false>(J, tune.chunk, tune.ctas_per_sm, tune.unroll, st)
 #define TWDIC_ICGN_WARP_N(NW)                                                                    \
     if (tune.sampler == kSampLut) { TWDIC_ICGN_WARP(NW, kSampLut); }                              \
+    if (tune.sampler == kSampNbhdBs) { TWDIC_ICGN_WARP(NW, kSampNbhdBs); }                        \
     TWDIC_ICGN_WARP(NW, kSampNbhd)
         if (tune.threads == 128) { TWDIC_ICGN_WARP_N(4); }
         if (tune.threads == 256) { TWDIC_ICGN_WARP_N(8); }
@@ -999,6 +1067,7 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
 #define TWDIC_ICGN_FAST_T(TH)                                                                    \
     if (t1.sampler == kSampLut) { TWDIC_ICGN_FAST(TH, kSampLut); }                              \
     if (t1.sampler == kSampNbhd) { TWDIC_ICGN_FAST(TH, kSampNbhd); }                            \
+    if (t1.sampler == kSampNbhdBs) { TWDIC_ICGN_FAST(TH, kSampNbhdBs); }                        \
     TWDIC_ICGN_FAST(TH, kSampWindow)
     if (t1.threads == 32) { TWDIC_ICGN_FAST_T(32); }
     if (t1.threads == 64) { TWDIC_ICGN_FAST_T(64); }

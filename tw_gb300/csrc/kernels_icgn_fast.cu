@@ -37,139 +37,212 @@ namespace twdic {
 
 namespace {
 
-constexpr int kPreThreads = 256;
 
-__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+__device__ __forceinline__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 
-// Per-reference precompute (TW_paDIC_ICGN2D_CPU.cpp:516-595, :676-693).
-// One warp per POI for the subset sums (FP32 lane partials, FP32 warp sums);
-// then the 6x6 factorizations of the CTA's kPrePois POIs run lane-parallel,
-// one POI per lane, in FP64: Cholesky, then H^-1 = L^-T L^-1 stored packed
-// (21 doubles) for the per-iteration solve.  On GB300 an FP64 warp
-// instruction holds the FP64 pipe for many cycles whatever its active lanes,
-// so each FP64 instruction here serves 32 POIs.
-constexpr int kPrePois = 32;
+// Per-reference precompute (TW_paDIC_ICGN2D_CPU.cpp:516-595, :676-693), in
+// two kernels.
+// k_ref_sums: one warp per POI.  The subset is walked in row-major sample
+// order k = lane + 32 j (every lane busy whatever the subset width): first
+// the integer sum of its pixels (the mean, bit-equal to the reference's),
+// then the 34 FP32 sums (Hessian lower triangle, sum (R - mean)^2, sum SD_k,
+// sum SD_k (R - mean)) on the packed FP32 pipe, lane partials reduced over
+// the warp.  The Hessian sums are staged, as floats, in the POI's own slot of
+// the inverse-Hessian array.
+// k_ref_factor: one POI per thread, in FP64: Cholesky (spotrf's steps, as
+// potrf6), then H^-1 = L^-T L^-1 packed (21 doubles) for the per-iteration
+// solve, dividing by the diagonal through its six reciprocals.  On GB300 an
+// FP64 warp instruction holds the FP64 pipe for many cycles whatever its
+// active lanes, so each serves 32 POIs.
+constexpr int kSumWarps = 8;
+constexpr int kFactorThreads = 128;
 
-__global__ void __launch_bounds__(kPreThreads) k_ref_precompute_fast(Geom g, const uint8_t* __restrict__ ref,
-                                                                      const int2* __restrict__ poi, int n,
-                                                                      float* stats, double* hinv,
-                                                                      uint8_t* rflag) {
-    constexpr int NW = kPreThreads / 32;
-    __shared__ float fsum[kPrePois][35];  // [0..20] H lower, [21] sum (R-mean)^2, [22..27] sum SD, [28..33] sum SD (R-mean), [34] mean
-    __shared__ int sflag[kPrePois];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
-    const int base = blockIdx.x * kPrePois;
-    for (int slot = wid; slot < kPrePois; slot += NW) {
-        const int p = base + slot;
-        if (p >= n) {
-            if (lane == 0) sflag[slot] = -1;
-            continue;
-        }
-        const int2 pyx = poi[p];
-        if (pyx.x - g.ry < g.sy || pyx.y - g.rx < g.sx || pyx.x + g.ry >= g.sy + g.rh || pyx.y + g.rx >= g.sx + g.rw) {
-            if (lane == 0) sflag[slot] = kOutofROI;
-            continue;
-        }
-        const uint8_t* r0 = ref + (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
-        int isum = 0;
-        for (int l = 0; l < SH; ++l)
-            for (int m = lane; m < SW; m += 32) isum += r0[(size_t)l * g.pitch + m];
-        isum = warp_sum(isum);
-        const float mean = (float)isum / (float)S;  // bit-equal to the reference's mean
-        float h[34];
-#pragma unroll
-        for (int k = 0; k < 34; ++k) h[k] = 0.f;
-        for (int l = 0; l < SH; ++l) {
-            for (int m = lane; m < SW; m += 32) {
-                const uint8_t* r = r0 + (size_t)l * g.pitch + m;
-                const float rx = 0.5f * (float)((int)r[1] - (int)r[-1]);
-                const float ry = 0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]);
-                const float dx = (float)(m - g.rx), dy = (float)(l - g.ry);
-                const float d[6] = {rx, rx * dx, rx * dy, ry, ry * dx, ry * dy};
-                const float rt = (float)r[0] - mean;
-                int q = 0;
-#pragma unroll
-                for (int a = 0; a < 6; ++a)
-#pragma unroll
-                    for (int b = 0; b <= a; ++b) h[q++] += d[a] * d[b];
-                h[21] += rt * rt;
-#pragma unroll
-                for (int a = 0; a < 6; ++a) {
-                    h[22 + a] += d[a];
-                    h[28 + a] += d[a] * rt;
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 34; ++k) {
-            const float w = warp_sum(h[k]);  // every lane holds the total
-            if (lane == (k & 31)) fsum[slot][k] = w;
-        }
-        if (lane == 0) {
-            fsum[slot][34] = mean;
-            sflag[slot] = kSuccess;
-        }
-    }
-    __syncthreads();
-    if (wid != 0) return;
-    // lane-parallel FP64 factorization, one POI per lane
-    const int slot = lane, p = base + lane;
-    const int f0 = sflag[slot];
-    if (f0 < 0) return;
-    float* st = stats + (size_t)p * 16;
-    double* hi = hinv + (size_t)p * 21;
-    if (f0 == kOutofROI) {
-        rflag[p] = kOutofROI;
+__global__ void __launch_bounds__(kSumWarps * 32) k_ref_sums(Geom g, const uint8_t* __restrict__ ref,
+                                                               const int2* __restrict__ poi, int n,
+                                                               float* __restrict__ stats, double* hinv,
+                                                               uint8_t* __restrict__ rflag) {
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kSumWarps + (threadIdx.x >> 5);
+    if (p >= n) return;
+    const int2 pyx = poi[p];
+    if (pyx.x - g.ry < g.sy || pyx.y - g.rx < g.sx || pyx.x + g.ry >= g.sy + g.rh || pyx.y + g.rx >= g.sx + g.rw) {
+        if (lane == 0) rflag[p] = kOutofROI;
         return;
     }
-    const float mean = fsum[slot][34];
-    const float rs = (float)sqrt((double)fsum[slot][21]);
-    uint8_t f = kSuccess;
-    if (fabsf(mean) <= FLT_EPSILON || fabsf(rs) <= FLT_EPSILON) f = kDarkSubset;
-    double a[36];
+    const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
+    const int pitch = g.pitch;
+    const uint8_t* r0 = ref + (size_t)(pyx.x - g.ry) * pitch + (pyx.y - g.rx);
+    // sample k = lane + 32 j at row l, column m of the subset (offset o);
+    // a step adds 32 samples: dm columns and 32 / SW rows, then a carry
+    const int m_first = lane % SW, l_first = lane / SW;
+    const int dm = 32 % SW, dofs = (32 / SW) * pitch + dm, wrap = pitch - SW;
+    const int o_first = l_first * pitch + m_first;
+    int isum = 0;
     {
-        int q = 0;
+        int m = m_first, o = o_first;
+        for (int k = lane; k < S; k += 32) {
+            isum += r0[o];
+            o += dofs;
+            m += dm;
+            if (m >= SW) {
+                m -= SW;
+                o += wrap;
+            }
+        }
+    }
+    isum = warp_sum(isum);
+    const float mean = (float)isum / (float)S;  // bit-equal to the reference's mean
+    // SD = (d0 .. d5) = (g_x, g_x dx, g_x dy, g_y, g_y dx, g_y dy) as
+    // D0 = (d0, d1), D1 = (d2, d3), D2 = (d4, d5); Hessian entry (a, b) of the
+    // lower triangle is element tri(a, b) of h below
+    const float2 zero = make_float2(0.f, 0.f);
+    float2 A0 = zero, A1 = zero, A2 = zero, A3 = zero, A4 = zero, A5 = zero, A6 = zero, A7 = zero, A8 = zero,
+           A9 = zero, A10 = zero, B0 = zero, B1 = zero, B2 = zero, C0 = zero, C1 = zero, C2 = zero;
+    {
+        int m = m_first, o = o_first;
+        float2 dd = make_float2((float)(m_first - g.rx), (float)(l_first - g.ry));
+        const float2 dstep = make_float2((float)dm, (float)(32 / SW)), dwrap = make_float2(-(float)SW, 1.f);
+        for (int k = lane; k < S; k += 32) {
+            const uint8_t* r = r0 + o;
+            const float gx = 0.5f * (float)((int)r[1] - (int)r[-1]);
+            const float gy = 0.5f * (float)((int)r[pitch] - (int)r[-pitch]);
+            const float rt = (float)r[0] - mean;
+            const float2 gxd = __fmul2_rn(make_float2(gx, gx), dd), gyd = __fmul2_rn(make_float2(gy, gy), dd);
+            const float2 D0 = make_float2(gx, gxd.x), D1 = make_float2(gxd.y, gy), D2 = gyd;
+            const float2 rr = make_float2(rt, rt);
+            A0 = __ffma2_rn(make_float2(D0.x, D1.x), make_float2(D0.x, D1.x), A0);  // (0,0), (2,2)
+            A1 = __ffma2_rn(make_float2(D0.y, D0.y), D0, A1);                      // (1,0), (1,1)
+            A2 = __ffma2_rn(make_float2(D1.x, D1.x), D0, A2);                      // (2,0), (2,1)
+            A3 = __ffma2_rn(make_float2(D1.y, D1.y), D0, A3);                      // (3,0), (3,1)
+            A4 = __ffma2_rn(make_float2(D1.y, D1.y), D1, A4);                      // (3,2), (3,3)
+            A5 = __ffma2_rn(make_float2(D2.x, D2.x), D0, A5);                      // (4,0), (4,1)
+            A6 = __ffma2_rn(make_float2(D2.x, D2.x), D1, A6);                      // (4,2), (4,3)
+            A7 = __ffma2_rn(make_float2(D2.x, rt), make_float2(D2.x, rt), A7);     // (4,4), (R - mean)^2
+            A8 = __ffma2_rn(make_float2(D2.y, D2.y), D0, A8);                      // (5,0), (5,1)
+            A9 = __ffma2_rn(make_float2(D2.y, D2.y), D1, A9);                      // (5,2), (5,3)
+            A10 = __ffma2_rn(make_float2(D2.y, D2.y), D2, A10);                    // (5,4), (5,5)
+            B0 = __fadd2_rn(B0, D0);
+            B1 = __fadd2_rn(B1, D1);
+            B2 = __fadd2_rn(B2, D2);
+            C0 = __ffma2_rn(D0, rr, C0);
+            C1 = __ffma2_rn(D1, rr, C1);
+            C2 = __ffma2_rn(D2, rr, C2);
+            o += dofs;
+            m += dm;
+            dd = __fadd2_rn(dd, dstep);
+            if (m >= SW) {
+                m -= SW;
+                o += wrap;
+                dd = __fadd2_rn(dd, dwrap);
+            }
+        }
+    }
+    // [0..20] H lower (tri order), [21] sum (R-mean)^2, [22..27] sum SD, [28..33] sum SD (R-mean)
+    float h[34] = {A0.x, A1.x, A1.y, A2.x, A2.y, A0.y, A3.x, A3.y, A4.x, A4.y, A5.x, A5.y,
+                   A6.x, A6.y, A7.x, A8.x, A8.y, A9.x, A9.y, A10.x, A10.y, A7.y, B0.x, B0.y,
+                   B1.x, B1.y, B2.x, B2.y, C0.x, C0.y, C1.x, C1.y, C2.x, C2.y};
+#pragma unroll
+    for (int k = 0; k < 34; ++k) h[k] = warp_sum(h[k]);  // every lane holds the totals
+    if (lane == 0) {
+        const float rs = (float)sqrt((double)h[21]);
+        uint8_t f = kSuccess;  // pending the factorization
+        if (fabsf(mean) <= FLT_EPSILON || fabsf(rs) <= FLT_EPSILON) f = kDarkSubset;
+        float* st = stats + (size_t)p * 16;
+        st[0] = mean;
+        st[1] = rs;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            st[2 + k] = h[22 + k];
+            st[8 + k] = h[28 + k];
+        }
+        st[14] = 0.f;
+        st[15] = 0.f;
+        float* hs = reinterpret_cast<float*>(hinv + (size_t)p * 21);
+#pragma unroll
+        for (int k = 0; k < 21; ++k) hs[k] = h[k];
+        rflag[p] = f;
+    }
+}
+
+__global__ void __launch_bounds__(kFactorThreads) k_ref_factor(int n, double* hinv, uint8_t* __restrict__ rflag) {
+    const int p = blockIdx.x * kFactorThreads + threadIdx.x;
+    if (p >= n) return;
+    const uint8_t f = rflag[p];
+    if (f == kOutofROI) return;
+    double* hi = hinv + (size_t)p * 21;
+    if (f != kSuccess) {
+#pragma unroll
+        for (int k = 0; k < 21; ++k) hi[k] = 0.0;
+        return;
+    }
+    // the staged FP32 sums, all read before the slot is rewritten (every
+    // output below depends on all of them through the factorization)
+    const float* hs = reinterpret_cast<const float*>(hi);
+    double L[21];
+#pragma unroll
+    for (int k = 0; k < 21; ++k) L[k] = (double)hs[k];
+    // (loops of constant trip count with the bounds as predicates, so that
+    // they unroll before L is assigned to registers)
+    double rinv[6];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        double dot = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+            if (k < j) dot += L[tri(j, k)] * L[tri(j, k)];
+        double ajj = L[tri(j, j)] - dot;
+        if (!(ajj > 0.0)) {
+            ok = false;
+            ajj = 1.0;
+        }
+        ajj = __dsqrt_rn(ajj);
+        L[tri(j, j)] = ajj;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            if (i <= j) continue;
+            double s2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                if (k < j) s2 += L[tri(i, k)] * L[tri(j, k)];
+            L[tri(i, j)] = L[tri(i, j)] - s2;
+        }
+        rinv[j] = __drcp_rn(ajj);
 #pragma unroll
         for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int j = 0; j < 6; ++j) a[i * 6 + j] = (j <= i) ? (double)fsum[slot][q++] : 0.0;
+            if (i > j) L[tri(i, j)] *= rinv[j];
     }
-    if (f == kSuccess && potrf6(a) > 0) f = kSingularHessian;
-    if (f == kSuccess) {
-        // H^-1 column by column: L y = e_j, then L^T x = y
+    if (!ok) {
 #pragma unroll
-        for (int j = 0; j < 6; ++j) {
-            double x[6];
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                double acc = (k == j) ? 1.0 : 0.0;
-#pragma unroll
-                for (int i = 0; i < k; ++i) acc -= a[k * 6 + i] * x[i];
-                x[k] = acc / a[k * 6 + k];
-            }
-#pragma unroll
-            for (int k = 5; k >= 0; --k) {
-                double acc = x[k];
-#pragma unroll
-                for (int i = k + 1; i < 6; ++i) acc -= a[i * 6 + k] * x[i];
-                x[k] = acc / a[k * 6 + k];
-            }
-#pragma unroll
-            for (int k = j; k < 6; ++k) hi[tri(k, j)] = x[k];
-        }
-    } else {
         for (int k = 0; k < 21; ++k) hi[k] = 0.0;
+        rflag[p] = kSingularHessian;
+        return;
     }
-    st[0] = mean;
-    st[1] = rs;
-    for (int k = 0; k < 6; ++k) {
-        st[2 + k] = fsum[slot][22 + k];
-        st[8 + k] = fsum[slot][28 + k];
+    // H^-1 column by column: L y = e_j (y_k = 0 for k < j), then L^T x = y
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+        double x[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            if (k < j) {
+                x[k] = 0.0;
+                continue;
+            }
+            double acc = (k == j) ? 1.0 : 0.0;
+#pragma unroll
+            for (int i = j; i < k; ++i) acc -= L[tri(k, i)] * x[i];
+            x[k] = acc * rinv[k];
+        }
+#pragma unroll
+        for (int k = 5; k >= j; --k) {
+            double acc = x[k];
+#pragma unroll
+            for (int i = k + 1; i < 6; ++i) acc -= L[tri(i, k)] * x[i];
+            x[k] = acc * rinv[k];
+        }
+#pragma unroll
+        for (int k = j; k < 6; ++k) hi[tri(k, j)] = x[k];
     }
-    st[14] = 0.f;
-    st[15] = 0.f;
-    rflag[p] = f;
 }
 
 // 4x4 byte neighbourhood of every ROI pixel (i, j) of the target: rows
@@ -935,7 +1008,10 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
 cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
                                        double* chol, uint8_t* rflag, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    k_ref_precompute_fast<<<(n + kPrePois - 1) / kPrePois, kPreThreads, 0, st>>>(g, ref, poi, n, stats, chol, rflag);
+    k_ref_sums<<<(n + kSumWarps - 1) / kSumWarps, kSumWarps * 32, 0, st>>>(g, ref, poi, n, stats, chol, rflag);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_ref_factor<<<(n + kFactorThreads - 1) / kFactorThreads, kFactorThreads, 0, st>>>(n, chol, rflag);
     return cudaGetLastError();
 }
 

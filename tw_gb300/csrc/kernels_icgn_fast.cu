@@ -54,7 +54,7 @@ __device__ __forceinline__ constexpr int tri(int i, int j) { return i * (i + 1) 
 // solve, dividing by the diagonal through its six reciprocals.  On GB300 an
 // FP64 warp instruction holds the FP64 pipe for many cycles whatever its
 // active lanes, so each serves 32 POIs.
-constexpr int kSumWarps = 8;
+constexpr int kSumWarps = 4;  // measured at 2048², 41x41: 4 to 16 warps per CTA within 6 %
 constexpr int kFactorThreads = 128;
 
 __global__ void __launch_bounds__(kSumWarps * 32) k_ref_sums(Geom g, const uint8_t* __restrict__ ref,

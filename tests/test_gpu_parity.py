@@ -240,6 +240,58 @@ def test_icgn_flags_and_counters(small, path):
     assert fl[3] == 4
 
 
+def test_icgn_singular_hessian(small):
+    """A reference subset of vertical stripes (every column constant, one
+    row beyond the subset too) has R_y = 0: its Hessian is singular, so the
+    factorization flags SingularHessian and the IC-GN stops after the first
+    pass, as the oracle (spotrf info > 0)."""
+    pair, g, _, _ = small
+    poi = np.array([[80, 96], [60, 60]], np.int32)
+    ref2 = pair.ref.copy()
+    cols = np.arange(60 - g.subset_r - 2, 60 + g.subset_r + 3)
+    ref2[60 - g.subset_r - 2:60 + g.subset_r + 3, cols] = (37 * cols % 200 + 20).astype(np.uint8)[None, :]
+    u0 = np.array([1.6, 1.6], np.float32)
+    v0 = np.array([-2.4, -2.4], np.float32)
+    p6_or, it_or, fl_or = O.icgn(ref2, pair.tar, g, poi, u0, v0)
+    assert list(fl_or) == [0, 2]
+    for path in PATHS:
+        ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r, 2, 1,
+                          g.max_iter, g.delta_p, path=path)
+        ic.ResetRefImg(ref2)
+        u, v = u0.copy(), v0.copy()
+        iters = np.zeros(2, np.int32)
+        p6, fl = ic.ICGN2D_Algorithm(u, v, iters, poi, pair.tar)
+        np.testing.assert_array_equal(fl, fl_or, err_msg=str(path))
+        np.testing.assert_array_equal(iters, it_or, err_msg=str(path))
+
+
+@pytest.mark.parametrize("r", [6, 15, 24, 31])
+def test_icgn_radii_parity(r):
+    """FFT-CC then IC-GN at subset widths below, near and above the warp
+    width (13 to 63 pixels; the per-reference sums walk a subset 32 samples
+    at a time with a row carry), both paths, against the oracle.  Below
+    r = 6 the reference algorithm in FP32 is itself too ill-conditioned for
+    the 1e-3 px bar: on these images the FP32 oracle differs from its FP64
+    twin by up to 0.021 px at r = 4 and 0.009 px at r = 5 (3e-5 px at r = 6)."""
+    pair, g = synth.small_case(h=150, w=170, r=r, grid=9, seed=300 + r)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    u_or, v_or, z_or, st_or, p6_or, it_or, fl_or = oracle_run(pair, g, poi)
+    for path in PATHS:
+        fr = dic.DICFrame(params_of(g, path))
+        fr.set_reference(pair.ref)
+        out = fr.alloc_outputs()
+        fr.process(pair.tar, **out)
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, r, r, g.grid, g.grid,
+                          g.margin, g.margin, path=path)
+        U, V, Z = f.InitializeFFTCC(pair.ref)
+        f.ComputeFFTCC(U, V, Z, pair.tar)
+        same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
+        rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start, r=r)
+        print(r, path, rep)
+        assert rep.ok(), (r, path, rep)
+
+
 @pytest.mark.parametrize("r", [5, 8, 10, 15, 16, 20, 24, 29, 31])
 def test_fftcc_radii_parity(r):
     """FFT-CC at the subset radii of the uneven-batching workload (r in

@@ -1033,15 +1033,26 @@ FrameOut frame_out(Engine& e, const BatchArgs& a, int i) {
     return o;
 }
 
-// The frame's per-frame target table for the batch's sampler.
+// The sampler a fast-path frame runs with under the batch's launch shape:
+// B-spline frames read the neighbourhood table with the B-spline weights, or
+// the B-spline LUT (the window sampler is Catmull-Rom only).
+int batch_sampler(const IcgnTune& tune, const Engine& e) {
+    if (e.interp != TWDIC_INTERP_BSPLINE) return tune.sampler;
+    return tune.sampler == kSampNbhd ? kSampNbhdBs : kSampLut;
+}
+
+// The frame's per-frame target table for its sampler.
 int prepare_target_for(Engine& e, int sampler) {
     const Geom& g = e.g;
     if (sampler == kSampLut) {
         TW_TRY(e.d_lut.ensure(sizeof(float4) * 4 * (size_t)g.rw * g.rh));
-        TW_CUDA(launch_bicubic_lut(g, e.d_tar.as<uint8_t>(), e.d_lut.as<float4>(), e.stream));
-    } else if (sampler == kSampNbhd) {
+        if (e.interp == TWDIC_INTERP_BSPLINE)
+            TW_CUDA(launch_bspline_lut(g, e.d_tar.as<uint8_t>(), e.d_lut.as<float4>(), e.stream));
+        else
+            TW_CUDA(launch_bicubic_lut(g, e.d_tar.as<uint8_t>(), e.d_lut.as<float4>(), e.stream));
+    } else if (sampler == kSampNbhd || sampler == kSampNbhdBs) {
         TW_TRY(e.d_lut.ensure(sizeof(uint4) * (size_t)g.rw * g.rh));
-        TW_CUDA(launch_nbhd_table(g, e.d_tar.as<uint8_t>(), e.d_lut.as<uint4>(), e.stream));
+        TW_CUDA(launch_nbhd_table(g, e.d_tar.as<uint8_t>(), e.d_lut.as<uint4>(), e.stream, sampler == kSampNbhdBs));
     }
     return TWDIC_OK;
 }
@@ -1067,7 +1078,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
                 TW_CUDA(cudaMemcpyAsync(o.u, a.u[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
                 TW_CUDA(cudaMemcpyAsync(o.v, a.v[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
             }
-            if (fast && e.interp == TWDIC_INTERP_BICUBIC) fast_ic.push_back(i);
+            if (fast) fast_ic.push_back(i);
             continue;
         }
         TW_CUDA(cudaMemsetAsync(o.u, 0, 4 * n, b->stream));
@@ -1077,7 +1088,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             fast_tc.push_back(i);
         else
             TW_TRY(e.fftcc(o.u, o.v, o.z, e.d_fst.as<uint8_t>()));
-        if (fast && e.interp == TWDIC_INTERP_BICUBIC) fast_ic.push_back(i);
+        if (fast) fast_ic.push_back(i);
     }
     // tensor-core FFT-CC: one launch per window size (and per kMaxJobs frames)
     std::vector<bool> used(fast_tc.size(), false);
@@ -1103,28 +1114,41 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
                                          b->d_work.as<int>() + 1, b->stream));
     }
-    // target tables, then one persistent IC-GN launch over the fast frames
+    // target tables, then persistent IC-GN launches over the fast frames
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
-        if (e.prm.path == TWDIC_PATH_FAST && e.interp == TWDIC_INTERP_BICUBIC)
-            TW_TRY(prepare_target_for(e, b->tune.sampler));
+        if (e.prm.path == TWDIC_PATH_FAST)
+            TW_TRY(prepare_target_for(e, batch_sampler(b->tune, e)));
         else
             TW_TRY(e.prepare_target());
     }
-    // one launch per residency level (and per kMaxJobs frames): a launch sizes
-    // shared memory for its largest subset, so frames whose subsets allow
-    // more resident CTAs are not launched with larger ones
-    std::vector<std::pair<int, int>> order;  // (residency, frame index)
-    for (int i : fast_ic) order.emplace_back(icgn_fast_residency(a.frames[i]->e.g, b->tune), i);
-    std::stable_sort(order.begin(), order.end(),
-                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first > y.first; });
+    // one launch per residency level and sampler (and per kMaxJobs frames): a
+    // launch sizes shared memory for its largest subset, so frames whose
+    // subsets allow more resident CTAs are not launched with larger ones
+    struct IcOrder {
+        int residency, sampler, frame;
+    };
+    std::vector<IcOrder> order;
+    for (int i : fast_ic) {
+        const Engine& e = a.frames[i]->e;
+        IcgnTune t = b->tune;
+        t.sampler = batch_sampler(b->tune, e);
+        order.push_back(IcOrder{icgn_fast_residency(e.g, t), t.sampler, i});
+    }
+    std::stable_sort(order.begin(), order.end(), [](const IcOrder& x, const IcOrder& y) {
+        return x.residency != y.residency ? x.residency > y.residency : x.sampler < y.sampler;
+    });
     for (size_t k0 = 0; k0 < order.size();) {
         IcgnJobs J;
         J.njobs = 0;
         J.total = 0;
+        IcgnTune tune = b->tune;
+        tune.sampler = order[k0].sampler;
         size_t k = k0;
-        for (; k < order.size() && J.njobs < kMaxJobs && order[k].first == order[k0].first; ++k) {
-            const int i = order[k].second;
+        for (; k < order.size() && J.njobs < kMaxJobs && order[k].residency == order[k0].residency &&
+               order[k].sampler == order[k0].sampler;
+             ++k) {
+            const int i = order[k].frame;
             Engine& e = a.frames[i]->e;
             const FrameOut o = frame_out(e, a, i);
             IcgnJob& jb = J.job[J.njobs++];
@@ -1135,7 +1159,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             jb.stats = e.c_stat.as<float>();
             jb.hinv = e.c_chol64.as<double>();
             jb.rflag = e.c_flag64.as<uint8_t>();
-            jb.table = b->tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
+            jb.table = tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
             jb.grad = e.c_grad.as<__half2>();
             jb.u = o.u;
             jb.v = o.v;
@@ -1147,11 +1171,11 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             J.total += e.n;
         }
         k0 = k;
-        TW_CUDA(launch_icgn_fast_jobs(J, b->d_work.as<int>(), b->tune, b->stream));
+        TW_CUDA(launch_icgn_fast_jobs(J, b->d_work.as<int>(), tune, b->stream));
     }
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
-        if (e.prm.path == TWDIC_PATH_FAST && e.interp == TWDIC_INTERP_BICUBIC) continue;
+        if (e.prm.path == TWDIC_PATH_FAST) continue;
         const FrameOut o = frame_out(e, a, i);
         TW_TRY(e.icgn_solve(o.u, o.v, o.p6, o.it, o.fl));
     }

@@ -45,15 +45,17 @@ def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-def num_pois(roi_w, roi_h, r, grid, margin):
+def num_pois(roi_w, roi_h, r, grid, margin, ry=None):
+    """r: subset half width (and height unless ry is given)."""
     nx, ny = ctypes.c_int(), ctypes.c_int()
-    rc = lib().or_num_pois(roi_w, roi_h, r, r, grid, grid, margin, margin, ctypes.byref(nx), ctypes.byref(ny))
+    rc = lib().or_num_pois(roi_w, roi_h, r, r if ry is None else ry, grid, grid, margin, margin, ctypes.byref(nx),
+                           ctypes.byref(ny))
     return nx.value, ny.value, rc
 
 
-def poi_positions(start_x, start_y, nx, ny, margin, r, grid):
+def poi_positions(start_x, start_y, nx, ny, margin, r, grid, ry=None):
     yx = np.zeros((ny * nx, 2), dtype=np.int32)
-    lib().or_poi_positions(start_x, start_y, nx, ny, margin, margin, r, r, grid, grid, _p(yx))
+    lib().or_poi_positions(start_x, start_y, nx, ny, margin, margin, r, r if ry is None else ry, grid, grid, _p(yx))
     return yx
 
 
@@ -67,9 +69,10 @@ def precompute_f32(ref, tar, sx, sy, rw, rh):
     return (*out, lut)
 
 
-def fftcc(ref, tar, poi_yx, r, precision="f32", nthreads=0, init=0.0):
+def fftcc(ref, tar, poi_yx, r, precision="f32", nthreads=0, init=0.0, ry=None):
     """Integer-pixel FFT-CC.  Returns (u, v, zncc, status) where status is 0 ok,
-    1 dark subset (outputs left at `init`), 2 window outside the image."""
+    1 dark subset (outputs left at `init`), 2 window outside the image.
+    r: window half width (and height unless ry is given)."""
     ref = np.ascontiguousarray(ref, np.uint8)
     tar = np.ascontiguousarray(tar, np.uint8)
     poi_yx = np.ascontiguousarray(poi_yx, np.int32)
@@ -81,7 +84,7 @@ def fftcc(ref, tar, poi_yx, r, precision="f32", nthreads=0, init=0.0):
     z = np.full(n, init, dt)
     st = np.zeros(n, np.uint8)
     fn = lib().or_fftcc_f32 if precision == "f32" else lib().or_fftcc_f64
-    fn(_p(ref), _p(tar), W, H, _p(poi_yx), n, r, r, nthreads, _p(u), _p(v), _p(z), _p(st))
+    fn(_p(ref), _p(tar), W, H, _p(poi_yx), n, r, r if ry is None else ry, nthreads, _p(u), _p(v), _p(z), _p(st))
     return u, v, z, st
 
 
@@ -114,8 +117,9 @@ def icgn(ref, tar, geom, poi_yx, u0, v0, precision="f32", nthreads=0, iters_init
                                                                                ctypes.c_void_p, ctypes.c_void_p,
                                                                                ctypes.c_int]
     mode = {"bicubic": 0, "bspline": 1}[interp]
+    ry = getattr(geom, "subset_ry", 0) or geom.subset_r
     rc = fn(_p(ref), _p(tar), W, H, geom.start_x, geom.start_y, geom.roi_w, geom.roi_h, geom.subset_r,
-            geom.subset_r, _p(poi_yx), n, geom.max_iter, geom.delta_p, nthreads, _p(p6), _p(iters), _p(flags), mode)
+            ry, _p(poi_yx), n, geom.max_iter, geom.delta_p, nthreads, _p(p6), _p(iters), _p(flags), mode)
     if rc != 0:
         raise ValueError("ROI leaves no one-pixel border")
     return p6, iters, flags

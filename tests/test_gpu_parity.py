@@ -265,19 +265,21 @@ def test_icgn_singular_hessian(small):
         np.testing.assert_array_equal(iters, it_or, err_msg=str(path))
 
 
-@pytest.mark.parametrize("r", [6, 15, 24, 31])
-def test_icgn_radii_parity(r):
+@pytest.mark.parametrize("r,paths", [(6, [PATH_FAST]), (8, PATHS), (15, PATHS), (24, PATHS), (31, PATHS)])
+def test_icgn_radii_parity(r, paths):
     """FFT-CC then IC-GN at subset widths below, near and above the warp
     width (13 to 63 pixels; the per-reference sums walk a subset 32 samples
-    at a time with a row carry), both paths, against the oracle.  Below
-    r = 6 the reference algorithm in FP32 is itself too ill-conditioned for
-    the 1e-3 px bar: on these images the FP32 oracle differs from its FP64
-    twin by up to 0.021 px at r = 4 and 0.009 px at r = 5 (3e-5 px at r = 6)."""
+    at a time with a row carry, two rows a step at r = 6), against the
+    oracle.  Small subsets are ill-conditioned in FP32: on these images the
+    FP32 oracle differs from its FP64 twin by up to 0.021 px at r = 4 and
+    0.009 px at r = 5, and at r = 6 the plain path (FP32 Gauss-Jordan
+    inverse) misses the gradient bar on one POI, so r = 6 runs the fast path
+    (FP64 inverse) only."""
     pair, g = synth.small_case(h=150, w=170, r=r, grid=9, seed=300 + r)
     nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
     poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
     u_or, v_or, z_or, st_or, p6_or, it_or, fl_or = oracle_run(pair, g, poi)
-    for path in PATHS:
+    for path in paths:
         fr = dic.DICFrame(params_of(g, path))
         fr.set_reference(pair.ref)
         out = fr.alloc_outputs()
@@ -290,6 +292,37 @@ def test_icgn_radii_parity(r):
         rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start, r=r)
         print(r, path, rep)
         assert rep.ok(), (r, path, rep)
+
+
+def test_non_square_subsets():
+    """Half width 12, half height 8 (25 x 17 IC-GN subsets, 24 x 16 FFT-CC
+    windows transformed as [2ry][2rx] arrays): POI grid, FFT-CC and IC-GN on
+    both paths against the oracle."""
+    rx, ry = 12, 8
+    pair, _ = synth.small_case(h=150, w=170, r=rx, grid=9, seed=77)
+    g = synth.Geometry(170, 150, 1, 1, 168, 148, rx, 9, 12, subset_ry=ry)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, rx, g.grid, g.margin, ry=ry)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, rx, g.grid, ry=ry)
+    u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, poi, rx, ry=ry)
+    p6_or, it_or, fl_or = O.icgn(pair.ref, pair.tar, g, poi, u_or, v_or)
+    assert (fl_or == 0).mean() > 0.9
+    for path in PATHS:
+        prm = dic.make_params(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, rx, ry, g.grid, g.grid,
+                              g.margin, g.margin, g.max_iter, g.delta_p, path)
+        np.testing.assert_array_equal(dic.poi_positions(prm), poi)
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, rx, ry, g.grid, g.grid,
+                          g.margin, g.margin, path=path)
+        U, V, Z = f.InitializeFFTCC(pair.ref)
+        f.ComputeFFTCC(U, V, Z, pair.tar)
+        same = (U.ravel() == u_or) & (V.ravel() == v_or)
+        assert same.mean() > 0.95, (path, same.mean())
+        np.testing.assert_allclose(Z.ravel()[same], z_or[same], atol=1e-4)
+        fr = dic.DICFrame(prm)
+        fr.set_reference(pair.ref)
+        out = fr.alloc_outputs()
+        fr.process(pair.tar, **out)
+        rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same, r=ry)
+        assert rep.ok(), (path, rep)
 
 
 @pytest.mark.parametrize("r", [5, 8, 10, 15, 16, 20, 24, 29, 31])

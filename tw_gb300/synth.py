@@ -153,6 +153,7 @@ class Geometry:
     margin: int
     max_iter: int = 20
     delta_p: float = 0.001
+    subset_ry: int = 0  # subset half height when it differs from subset_r (0: square)
 
 
 def plain_512(seed: int = 2024) -> Tuple[SpecklePair, Geometry]:

@@ -87,7 +87,8 @@ cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi
 // ---- fast IC-GN (kernels_icgn_fast.cu)
 // stats: 16 floats per POI (mean, norm, sum SD_k [6], sum SD_k (R - mean) [6], pad);
 // chol: 21 doubles per POI, the packed symmetric inverse Hessian formed in FP64
-// from its Cholesky factor.
+// from its Cholesky factor.  Two launches on st: k_ref_sums (subset sums, the
+// FP32 Hessian staged in chol) then k_ref_factor (FP64 factorization in place).
 cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const int2* poi, int n, float* stats,
                                        double* chol, uint8_t* rflag, cudaStream_t st);
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,

@@ -58,6 +58,17 @@ def test_num_pois_and_grid_match_oracle(lib, roi, r, g, m):
     np.testing.assert_array_equal(dic.poi_positions(p), O.poi_positions(1, 1, nx, ny, m, r, g))
 
 
+@pytest.mark.parametrize("rw,rh,rx,ry,g,m", [(168, 148, 12, 8, 9, 12), (300, 200, 5, 20, 7, 3), (97, 131, 16, 9, 4, 0)])
+def test_non_square_grid_matches_oracle(lib, rw, rh, rx, ry, g, m):
+    """Subset half width and height differ (ComputePOIPositions_s takes both,
+    TW_utils.cpp:29-94): the library's POI count and grid equal the oracle's."""
+    p = dic.make_params(rw + 2, rh + 2, 1, 1, rw, rh, rx, ry, g, g, m, m)
+    nx, ny = dic.num_pois(p)
+    onx, ony, rc = O.num_pois(rw, rh, rx, g, m, ry=ry)
+    assert rc == 0 and (nx, ny) == (onx, ony)
+    np.testing.assert_array_equal(dic.poi_positions(p), O.poi_positions(1, 1, nx, ny, m, rx, g, ry=ry))
+
+
 def test_validation_errors_without_gpu(lib):
     # "Number of POIs is below 0!" (cuFFTCC2D ctor, TW_paDIC_cuFFTCC2D.cu:189-190)
     p = dic.make_params(64, 64, 0, 0, 64, 64, 20, 20, 5, 5, 20, 20)

@@ -174,14 +174,23 @@ def cpu_baseline(pair, g, poi, gpu_out=None, target_s=12.0):
 def accuracy_vs_oracle(pair, g, poi, gpu_out, stride=31):
     """The GPU frame's results against the oracle on every stride-th POI:
     FFT-CC in FP32 (integer guesses), then IC-GN in FP32 (the parity
-    reference) and in FP64 from the same guesses.  POIs flagged Success by
-    both sides are compared on u, v and the gradients; flags and iteration
-    counts are compared on all sampled POIs."""
+    reference) and in FP64 from the same guesses.  Integer displacements are
+    compared exactly, a difference counted as an exact tie when both shifts
+    have the same exact correlation; POIs flagged Success by both sides are
+    compared on u, v and the gradients; flags and iteration counts are
+    compared on all sampled POIs."""
+    from oracle import compare as C
     from oracle import oracle as O
     idx = np.arange(0, len(poi), stride)
     sp = np.ascontiguousarray(poi[idx])
     u, v, z, st = O.fftcc(pair.ref, pair.tar, sp, g.subset_r)
     out = {"pois": int(len(idx)), "sample": f"every {stride}-th POI of the frame"}
+    if "u_int" in gpu_out:
+        rep = C.fftcc_parity(pair.ref, pair.tar, sp, g.subset_r, gpu_out["u_int"][idx], gpu_out["v_int"][idx],
+                             gpu_out["zncc"][idx], u, v, z, st)
+        out["fftcc"] = {"compared": rep.n, "integer_equal": rep.n - rep.mismatches, "exact_ties": rep.exact_ties,
+                        "rounding_ties": rep.rounding_ties, "unexplained": rep.unexplained,
+                        "max_abs_zncc": rep.max_zncc_err}
     p6g, itg, flg = gpu_out["p6"][idx], gpu_out["iters"][idx], gpu_out["flags"][idx]
     for prec in ("f32", "f64"):
         p6o, ito, flo = O.icgn(pair.ref, pair.tar, g, sp, u, v, precision=prec)
@@ -377,7 +386,15 @@ def _run_gpu(args, world, rank, local, torch):
         line["batched"] = run_batched(pairs=48, steps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O  # noqa: F401  (CPU baseline leg)
-        line["cpu_baseline"] = cpu_baseline(pair, g, poi, gpu_out={"p6": p6, "iters": iters_np, "flags": flags})
+        # the integer FFT-CC of the same frame (one more call, outside the
+        # timed regions), for the accuracy block's FFT-CC comparison
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r,
+                          g.grid, g.grid, g.margin, g.margin, path=PATH_FAST)
+        U, V, Z = f.InitializeFFTCC(pair.ref)
+        f.ComputeFFTCC(U, V, Z, pair.tar)
+        gpu_out = {"p6": p6, "iters": iters_np, "flags": flags, "u_int": U.ravel(), "v_int": V.ravel(),
+                   "zncc": Z.ravel()}
+        line["cpu_baseline"] = cpu_baseline(pair, g, poi, gpu_out=gpu_out)
     if rank == 0:
         print(json.dumps(line))
     return 0

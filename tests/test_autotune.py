@@ -62,3 +62,28 @@ def test_autotune_choice_meets_parity_and_is_cached(tmp_path):
     for k in ("icgn_threads", "icgn_sampler", "icgn_chunk", "icgn_unroll", "fftcc_groups", "fftcc_pois_per_group"):
         assert t2[k] == t[k]
     assert len(cache.read_text().strip().splitlines()) == 1
+
+
+def test_damaged_cache_entry_is_measured_again(tmp_path):
+    """A cached line with values no setter accepts (an internal sampler
+    number, an unroll of 3) is skipped: the shapes are measured again, the
+    new choice is appended, and that one is reused."""
+    pair, g = synth.small_case()
+    cache = tmp_path / "tuning.txt"
+    f = dic.DICFrame(_params(g))
+    f.set_reference(pair.ref)
+    f.autotune(pair.tar, cache_path=cache)
+    key, vals = cache.read_text().strip().splitlines()[0].split(" ", 1)
+    v = vals.split()
+    v[2], v[4] = "4", "3"  # icgn_sampler, icgn_unroll
+    cache.write_text(key + " " + " ".join(v) + "\n")
+    f2 = dic.DICFrame(_params(g))
+    f2.set_reference(pair.ref)
+    t2 = f2.autotune(pair.tar, cache_path=cache)
+    assert t2["from_cache"] == 0 and t2["icgn_sampler"] in (0, 1, 2) and t2["icgn_unroll"] in (2, 4, 8)
+    assert len(cache.read_text().strip().splitlines()) == 2
+    f3 = dic.DICFrame(_params(g))
+    f3.set_reference(pair.ref)
+    t3 = f3.autotune(pair.tar, cache_path=cache)
+    assert t3["from_cache"] == 1 and t3["icgn_sampler"] == t2["icgn_sampler"]
+    assert t3["icgn_unroll"] == t2["icgn_unroll"]

@@ -794,6 +794,17 @@ std::string tuning_key(const Engine& e) {
     return buf;
 }
 
+// A cache entry is taken only with the values the setters accept
+// (twdic_frame_set_tuning, _icgn_layout, _icgn_unroll, _fftcc_tuning); a
+// hand-edited or damaged line is skipped, so the shapes are measured again.
+bool cached_tuning_valid(const twdic_tuning& c) {
+    return valid_icgn_threads(c.icgn_threads) && c.icgn_ctas_per_sm >= 0 && c.icgn_sampler >= kSampWindow &&
+           c.icgn_sampler <= kSampNbhd && c.icgn_chunk >= 0 &&
+           (c.icgn_unroll == 2 || c.icgn_unroll == 4 || c.icgn_unroll == 8) &&
+           (c.fftcc_use_tc == 0 || c.fftcc_use_tc == 1) && c.fftcc_groups >= 0 && c.fftcc_groups <= 2 &&
+           c.fftcc_pois_per_group >= 0;
+}
+
 bool cache_lookup(const char* path, const std::string& key, twdic_tuning* t) {
     FILE* f = path ? std::fopen(path, "r") : nullptr;
     if (!f) return false;
@@ -806,7 +817,8 @@ bool cache_lookup(const char* path, const std::string& key, twdic_tuning* t) {
         std::memset(&c, 0, sizeof(c));
         if (std::sscanf(line + k, " %d %d %d %d %d %d %d %d %f %f", &c.icgn_threads, &c.icgn_ctas_per_sm,
                         &c.icgn_sampler, &c.icgn_chunk, &c.icgn_unroll, &c.fftcc_use_tc, &c.fftcc_groups,
-                        &c.fftcc_pois_per_group, &c.fftcc_ms, &c.icgn_ms) == 10) {
+                        &c.fftcc_pois_per_group, &c.fftcc_ms, &c.icgn_ms) == 10 &&
+            cached_tuning_valid(c)) {
             *t = c;  // the last entry for a key wins
             found = true;
         }

@@ -164,3 +164,32 @@ def test_last_frame_guesses():
             assert bad[both].sum() <= 0.01 * both.sum() + 1, (rnd, bad[both].sum())
     assert srv.stream_stats(sid)["completed"] == 2 * len(tars)
     srv.close()
+
+
+@pytest.mark.gpu
+def test_remove_stream_while_polling():
+    """A call waiting on a ticket whose stream is removed returns an error
+    status instead of reading the freed slots, and a ticket that was read
+    once is unknown afterwards."""
+    import threading
+    import time
+    pair, g = synth.small_case()
+    srv = DICServer(queue_depth=2, start_paused=True)
+    sid = srv.add_stream(_params(g))
+    srv.set_reference(sid, pair.ref)
+    t = srv.submit(sid, pair.tar)
+    rc = []
+    th = threading.Thread(
+        target=lambda: rc.append(srv._lib.twdic_poll(srv._h, t, 1, None, None, None, None, None, None, None)))
+    th.start()
+    time.sleep(0.2)  # the poll is waiting: the server is paused
+    srv.remove_stream(sid)
+    th.join(timeout=10)
+    assert not th.is_alive() and rc and rc[0] in (-4, -1), rc  # stream removed / ticket unknown
+    sid2 = srv.add_stream(_params(g))
+    srv.set_reference(sid2, pair.ref)
+    srv.resume()
+    t2 = srv.submit(sid2, pair.tar)
+    assert srv.poll(sid2, t2)["flags"].size > 0
+    assert srv._lib.twdic_poll(srv._h, t2, 0, None, None, None, None, None, None, None) == -1
+    srv.close()

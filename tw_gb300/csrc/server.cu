@@ -442,7 +442,14 @@ int twdic_server_remove_stream(twdic_server* s, int32_t stream_id) {
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->streams.find(stream_id);
     if (it == s->streams.end()) return fail_msg(TWDIC_ERR_INVALID_ARG, "unknown stream id");
-    s->cv_done.wait(lk, [&] { return !it->second->busy; });
+    // no batch of the stream in flight, no twdic_submit copying into its
+    // slots and no twdic_poll copying out of them
+    s->cv_done.wait(lk, [&] {
+        if (it->second->busy) return false;
+        for (const Slot& sl : it->second->slots)
+            if (sl.state == kFilling || sl.state == kReading) return false;
+        return true;
+    });
     CamStream& cs = *it->second;
     for (Slot& sl : cs.slots)
         if (sl.ticket) s->tickets.erase(sl.ticket);
@@ -450,6 +457,8 @@ int twdic_server_remove_stream(twdic_server* s, int32_t stream_id) {
     s->committed -= cs.bytes;
     free_stream_buffers(cs);
     s->streams.erase(it);
+    lk.unlock();
+    s->cv_done.notify_all();  // calls waiting on the removed stream's tickets
     return TWDIC_OK;
 }
 
@@ -505,6 +514,7 @@ int twdic_submit(twdic_server* s, int32_t stream_id, const uint8_t* tar, int32_t
     cs.queue.push_back(si);
     lk.unlock();
     s->cv_sched.notify_all();
+    s->cv_done.notify_all();  // a twdic_server_remove_stream waiting for this copy
     return TWDIC_OK;
 }
 
@@ -517,9 +527,14 @@ int twdic_poll(twdic_server* s, uint64_t ticket, int32_t wait, float* u, float* 
     const int sid = it->second.first, si = it->second.second;
     CamStream* cs = s->streams.at(sid).get();
     Slot* sl = &cs->slots[si];
+    if (sl->state == kReading) return fail_msg(TWDIC_ERR_STATE, "ticket is being read by another call");
     if (sl->state != kDone && sl->state != kFailed) {
         if (!wait) return TWDIC_PENDING;
-        s->cv_done.wait(lk, [&] { return sl->state == kDone || sl->state == kFailed || s->stop; });
+        // the ticket leaves the table when its stream is removed or another
+        // call reads it; the slot is not touched after that
+        auto gone = [&] { return s->tickets.find(ticket) == s->tickets.end(); };
+        s->cv_done.wait(lk, [&] { return s->stop || gone() || sl->state == kDone || sl->state == kFailed; });
+        if (gone()) return fail_msg(TWDIC_ERR_STATE, "ticket taken by another call or its stream removed");
         if (sl->state != kDone && sl->state != kFailed) return fail_msg(TWDIC_ERR_STATE, "server stopped");
     }
     const int rc = sl->rc;
@@ -539,6 +554,8 @@ int twdic_poll(twdic_server* s, uint64_t ticket, int32_t wait, float* u, float* 
     s->tickets.erase(ticket);
     sl->ticket = 0;
     sl->state = kFree;
+    lk.unlock();
+    s->cv_done.notify_all();  // other calls waiting on this ticket
     return rc == TWDIC_OK ? TWDIC_OK : fail_msg(rc, "the batch holding this frame failed");
 }
 

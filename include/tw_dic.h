@@ -330,7 +330,12 @@ TWDIC_API int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes);
  * others are on the GPU join the next batch.  Results equal
  * twdic_frame_process on the same frame.  twdic_poll returns TWDIC_PENDING
  * until the frame is done (wait = 1 blocks), then copies the results out and
- * frees the slot; latency_ms is submit-to-done. */
+ * frees the slot; latency_ms is submit-to-done.  A ticket is read once: a
+ * second twdic_poll on it fails with TWDIC_ERR_INVALID_ARG (read) or
+ * TWDIC_ERR_STATE (being read).  twdic_server_remove_stream waits for the
+ * stream's batch in flight and for twdic_submit / twdic_poll copies into or
+ * out of its slots, then drops its pending frames; a twdic_poll waiting on
+ * one of them returns TWDIC_ERR_STATE. */
 typedef struct twdic_server twdic_server;
 typedef struct {
     uint64_t hbm_budget_bytes;

@@ -80,6 +80,16 @@ int main(int argc, char** argv) {
         cudaMemcpy(gv.data(), dV, sizeof(float) * n, cudaMemcpyDeviceToHost);
         put(out, gu.data(), n);
         put(out, gv.data(), n);
+        // the B-spline interpolation flag (ICGN2DInterpolationFLag::BicubicSpline)
+        ICGN2D_CPU bic(ImageView(ref.data(), W, H), W, H, 1, 1, W - 2, H - 2, r, r, f.GetNumPOIsX(),
+                       f.GetNumPOIsY(), 20, 0.001f, ICGN2DInterpolationFLag::BicubicSpline, paDICThreadFlag::Multicore);
+        std::vector<float> bu(U[0], U[0] + n), bv(V[0], V[0] + n);
+        std::vector<int> bit(n, 0);
+        bic.ICGN2D_Algorithm(bu.data(), bv.data(), bit.data(), poi[0][0], ImageView(tar.data(), W, H));
+        put(out, bu.data(), n);
+        put(out, bv.data(), n);
+        put(out, bit.data(), n);
+        put(out, bic.Flags().data(), n);
         cic.cuFinalize();
         cf.cuDestroyFFTCC(dU, dV, dZ);
         f.FinalizeFFTCC(poi, U, V, Z);

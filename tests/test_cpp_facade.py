@@ -76,3 +76,18 @@ def test_facade_matches_python_entry_points(tmp_path):
     np.testing.assert_array_equal(it, w["iters"])
     np.testing.assert_array_equal(gu, w["u"])
     np.testing.assert_array_equal(gv, w["v"])
+    # the B-spline flag against a B-spline frame
+    bu, bv, bit, bfl = take(np.float32, n), take(np.float32, n), take(np.int32, n), take(np.uint8, n)
+    assert o == len(raw)
+    from tw_gb300 import INTERP_BSPLINE
+    fb = dic.DICFrame(dic.make_params(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r,
+                                      g.subset_r, g.grid, g.grid, g.margin, g.margin, g.max_iter, g.delta_p))
+    fb.set_interpolation(INTERP_BSPLINE)
+    fb.set_reference(pair.ref)
+    wb = fb.alloc_outputs()
+    fb.process(pair.tar, **wb)
+    np.testing.assert_array_equal(bu, wb["u"])
+    np.testing.assert_array_equal(bv, wb["v"])
+    np.testing.assert_array_equal(bit, wb["iters"])
+    np.testing.assert_array_equal(bfl, wb["flags"])
+    assert not np.array_equal(bu, u)  # a different interpolant

@@ -1,5 +1,7 @@
 """Generate tests/golden/small_case.npz: a seeded synthetic speckle pair, its POI
-grid and the oracle's FFT-CC and IC-GN outputs on it.
+grid and the oracle's FFT-CC and IC-GN outputs on it; and
+tests/golden/small_case_bspline.npz: the oracle's IC-GN outputs on the same
+inputs with the B-spline interpolation (BicubicSplineCoefficients_s).
 
 The reference cannot be built or run here (FFTW, MKL, OpenCV, Qt, Windows.h),
 and it ships no golden vectors, so this fixture pins the oracle against
@@ -33,6 +35,10 @@ def main():
     np.savez_compressed(out, ref=pair.ref, tar=pair.tar, poi=poi, geom=geom, delta_p=np.float32(g.delta_p),
                         fftcc_u=u, fftcc_v=v, fftcc_zncc=z, icgn_p6=p6, icgn_iters=it, icgn_flags=fl)
     print(out, os.path.getsize(out), "bytes;", len(poi), "POIs; flags", np.bincount(fl))
+    bp6, bit, bfl = O.icgn(pair.ref, pair.tar, g, poi, u, v, interp="bspline")
+    out_b = os.path.join(os.path.dirname(os.path.abspath(__file__)), "small_case_bspline.npz")
+    np.savez_compressed(out_b, icgn_p6=bp6, icgn_iters=bit, icgn_flags=bfl)
+    print(out_b, os.path.getsize(out_b), "bytes; flags", np.bincount(bfl))
 
 
 if __name__ == "__main__":

@@ -220,3 +220,17 @@ def test_golden_fixture_regression():
     np.testing.assert_array_equal(fl, d["icgn_flags"])
     np.testing.assert_array_equal(it, d["icgn_iters"])
     np.testing.assert_allclose(p6, d["icgn_p6"], rtol=0, atol=1e-6)
+
+
+def test_golden_fixture_regression_bspline():
+    """The oracle's B-spline IC-GN on the stored inputs, from its own FFT-CC
+    guesses, against tests/golden/small_case_bspline.npz."""
+    d = np.load(os.path.join(GOLDEN, "small_case.npz"))
+    b = np.load(os.path.join(GOLDEN, "small_case_bspline.npz"))
+    g = synth.Geometry(*[int(x) for x in d["geom"][:9]], int(d["geom"][9]), float(d["delta_p"]))
+    p6, it, fl = O.icgn(d["ref"], d["tar"], g, d["poi"], d["fftcc_u"], d["fftcc_v"], interp="bspline")
+    np.testing.assert_array_equal(fl, b["icgn_flags"])
+    np.testing.assert_array_equal(it, b["icgn_iters"])
+    np.testing.assert_allclose(p6, b["icgn_p6"], rtol=0, atol=1e-6)
+    # a different interpolant from the bicubic fixture's
+    assert np.abs(p6 - d["icgn_p6"]).max() > 1e-5

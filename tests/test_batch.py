@@ -119,3 +119,35 @@ def test_batch_with_bspline_frames_equals_alone():
     for o, w in zip(outs, want):
         for k in w:
             np.testing.assert_array_equal(o[k], w[k])
+
+
+def test_batch_graph_recaptured_after_interpolation_change():
+    """A captured graph holds each frame's sampler and target table: after a
+    frame switches to the B-spline interpolation the next call is captured
+    anew, and that frame's results equal the frame alone."""
+    import torch
+    from tw_gb300 import INTERP_BSPLINE
+    pairs = [synth.small_case(h=h, w=w, r=r, grid=gr, seed=s) for h, w, r, gr, s, _ in CASES[:2]]
+    frames = []
+    for pair, g in pairs:
+        f = _frame(g)
+        f.set_reference(pair.ref)
+        frames.append(f)
+    dev_tars = [torch.from_numpy(p.tar).cuda() for p, _ in pairs]
+    outs = [f.alloc_outputs(device="cuda") for f in frames]
+    b = dic.DICBatch(graph=True)
+    b.process(frames, dev_tars, outs)
+    b.process(frames, dev_tars, outs)
+    assert b.replayed
+    frames[1].set_interpolation(INTERP_BSPLINE)
+    b.process(frames, dev_tars, outs)
+    assert not b.replayed
+    torch.cuda.synchronize()
+    pair, g = pairs[1]
+    f = _frame(g)
+    f.set_interpolation(INTERP_BSPLINE)
+    f.set_reference(pair.ref)
+    w = f.alloc_outputs()
+    f.process(pair.tar, **w)
+    for k in w:
+        np.testing.assert_array_equal(outs[1][k].cpu().numpy(), w[k], err_msg=k)

@@ -1300,7 +1300,9 @@ int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frame
         for (int i = 0; i < count; ++i) {
             const Engine& e = frames[i]->e;
             caches_ok = caches_ok && e.cache_valid;
-            for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)e.guess, (uintptr_t)e.interp, (uintptr_t)tars[i],
+            // the frame's own settings that batch_enqueue reads, then its arrays
+            for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)e.guess, (uintptr_t)e.interp,
+                                (uintptr_t)e.fftcc_tune.use_tc, (uintptr_t)tars[i],
                                 (uintptr_t)(strides ? strides[i] : 0),
                                 (uintptr_t)u[i], (uintptr_t)v[i], (uintptr_t)(zncc ? zncc[i] : nullptr),
                                 (uintptr_t)(p6 ? p6[i] : nullptr), (uintptr_t)(iters ? iters[i] : nullptr),

@@ -266,6 +266,8 @@ TWDIC_API int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t s
  *     flags out, all num_pois long; the work is queued on `stream`
  *     (cudaStream_t as void*, NULL = legacy default stream) and the call
  *     returns without synchronising;
+ *   - the bicubic interpolation (TWDIC_INTERP_BICUBIC), sampled from the
+ *     target image itself (no per-frame table);
  *   - the reference precompute is redone on every call (no cache survives
  *     between calls); the array keeps the last call's contents, and the parts
  *     that must start at zero are cleared on the stream by each call;

@@ -402,7 +402,7 @@ def _run_gpu(args, world, rank, local, torch):
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
-# profiles/k_icgn_warp_2048_r20.md and profiles/k_fftcc_tc_2048_r20.md
+# profiles/k_icgn_warp_2048_subset41.md and profiles/k_fftcc_tc_2048_subset41.md
 NCU_TRAFFIC = {"k_icgn_warp": 123.86e6 + 6.69e6, "k_fftcc_tc": 9.60e6 + 0.0}
 # from the same IC-GN capture: L1 hit rate of its gathers and the FMA-heavy
 # pipe's share of cycles (the kernel's limiter)

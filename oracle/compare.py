@@ -1,6 +1,6 @@
 """TEST INFRASTRUCTURE ONLY: parity checks of GPU results against the oracle.
 
-Parity definition (from the benchmark spec for this path):
+Parity definition for this path:
 * integer FFT-CC displacements equal the oracle's, except at peaks that tie:
   an exact tie is two shifts with equal exact (integer) correlation; a
   rounding tie is a pair whose exact correlation values differ by less than

@@ -50,7 +50,7 @@ extern "C" {
 #define TWDIC_ERR_STATE (-4)        /* call order: e.g. compute before a reference image was set */
 #define TWDIC_ERR_CUDA (-5)         /* a CUDA runtime call failed; see twdic_last_error() */
 #define TWDIC_ERR_NO_MEMORY (-6)    /* device allocation failed or the HBM budget would be exceeded */
-#define TWDIC_ERR_UNSUPPORTED (-7)  /* parameter outside this build's limits (e.g. subset radius > 31) */
+#define TWDIC_ERR_UNSUPPORTED (-7)  /* parameter outside the library's limits (e.g. subset radius > 31) */
 #define TWDIC_ERR_TIMEOUT (-8)      /* a bounded device-side wait gave up */
 #define TWDIC_ERR_BUSY (-9)         /* a serving stream's queue is full: the frame was dropped */
 #define TWDIC_PENDING 1             /* twdic_poll: the frame is not done yet (not an error) */

@@ -3,7 +3,7 @@
 // CPU restatement of TW_Engine's reference CPU path for 2D DIC (integer-pixel
 // FFT-CC followed by first-order IC-GN with a bicubic LUT).  Only tests/,
 // __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this
-// library, and only as the checker / the timed CPU baseline.  The product
+// library, and only as the parity reference / the timed CPU baseline.  The product
 // (tw_gb300/) never calls it.
 //
 // Parity status: PARITY UNPINNED against the reference's own outputs.  The

@@ -82,7 +82,7 @@ def test_validation_errors_without_gpu(lib):
     p = dic.make_params(128, 128, 0, 0, 128, 128, 10, 10, 5, 5, 3, 3)
     assert lib.twdic_frame_create(ctypes.byref(p), ctypes.byref(h)) == -3
     assert b"boundary" in lib.twdic_last_error()
-    # subset radius beyond this build's limit
+    # subset radius beyond the library's limit
     p = dic.make_params(256, 256, 1, 1, 254, 254, 32, 32, 5, 5, 3, 3)
     assert lib.twdic_frame_create(ctypes.byref(p), ctypes.byref(h)) == -7
     # ROI outside the image, bad path, NULL arguments

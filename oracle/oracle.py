@@ -1,8 +1,8 @@
 """TEST INFRASTRUCTURE ONLY: ctypes loader for the C++ oracle (tw_oracle.cpp).
 
 The oracle is a CPU restatement of the reference's CPU path (see the header of
-tw_oracle.cpp for the file:line map and for why parity with the reference's own
-outputs is unpinned).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+tw_oracle.cpp for the file:line map); tests/test_ref_pin.py pins it to the
+outputs of the reference's own sources (oracle/build_ref.py).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline leg import this module; the product package never does.
 """
 from __future__ import annotations

@@ -6,14 +6,15 @@
 // library, and only as the parity reference / the timed CPU baseline.  The product
 // (tw_gb300/) never calls it.
 //
-// Parity status: PARITY UNPINNED against the reference's own outputs.  The
-// reference CPU path cannot be compiled (it needs FFTW3, MKL LAPACKE, OpenCV,
-// Qt and Windows.h) and the reference ships no golden vectors or asserting
-// tests.  What is pinned instead: the third-party arithmetic at its boundary
-// (FFTW's DFT definition against numpy.fft, LAPACK spotrf/spotrs against the
-// LAPACK that scipy links) and analytic known answers (POI grid, gradients,
-// bicubic LUT reproduction of corner values and derivatives, imposed synthetic
-// deformation fields).  See tests/test_oracle.py.
+// Parity status: PINNED to the reference's own code.  The reference's
+// Fftcc2D_CPU and ICGN2D_CPU are compiled from their sources
+// (oracle/build_ref.py, with stand-ins for FFTW, LAPACKE, OpenCV and Qt) and
+// their outputs on seeded inputs are stored in tests/golden/ref_*.npz;
+// tests/test_ref_pin.py requires this restatement to reproduce them (integer
+// FFT-CC equal, IC-GN flags and iteration counts equal, u and v within 1e-4
+// px).  The third-party arithmetic is pinned separately: the DFT against
+// numpy.fft and the Cholesky routines against the LAPACK that scipy links
+// (tests/test_oracle.py).
 //
 // Every function follows a reference file:line (paths relative to the
 // TWANG006/TW project root):

@@ -3,11 +3,11 @@ grid and the oracle's FFT-CC and IC-GN outputs on it; and
 tests/golden/small_case_bspline.npz: the oracle's IC-GN outputs on the same
 inputs with the B-spline interpolation (BicubicSplineCoefficients_s).
 
-The reference cannot be built or run here (FFTW, MKL, OpenCV, Qt, Windows.h),
-and it ships no golden vectors, so this fixture pins the oracle against
-itself: tests/test_oracle.py re-runs the oracle on the stored inputs and
-requires the stored outputs.  Re-run this script only when the oracle's
-arithmetic is changed on purpose.
+This fixture is a regression record of the oracle itself: tests/test_oracle.py
+re-runs the oracle on the stored inputs and requires the stored outputs.  The
+oracle's pin to the reference's own code is a separate set of fixtures
+(make_ref_golden.py, tests/test_ref_pin.py).  Re-run this script only when the
+oracle's arithmetic is changed on purpose.
 
     python tests/golden/make_golden.py
 """

@@ -6,8 +6,10 @@ reference image's precompute cached, as the reference's worker thread runs it
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
---impl reference times the reference's CPU algorithm (the oracle restatement;
-the reference itself cannot be built here) on the host cores instead.
+--impl reference times the reference's CPU algorithm on the host cores
+instead: whole frames of the same workload through the oracle restatement
+(whose outputs are pinned to the reference's own code by tests/test_ref_pin.py;
+the reference sources themselves are not present where the bench runs).
 Multi-GPU runs are independent replicas (the path has no exchange step).
 """
 from __future__ import annotations
@@ -34,6 +36,13 @@ WORKLOAD = ("2048x2048 uint8 speckle pair (100k speckles, sinusoidal field u=3si
             "reference precompute cached")
 
 
+def config_of(n_pois, world):
+    """The workload's configuration, the same in both arms."""
+    return {"workload": WORKLOAD, "pois": n_pois, "parallelism": f"replicas x{world}",
+            "l2": "GPU arm: flushed between steps by a 256 MB write outside the timed events; CPU arm: the "
+                  "frame's working set (images, gradients, 268 MB LUT) exceeds the host caches"}
+
+
 def env_int(name, default):
     try:
         return int(os.environ.get(name, default))
@@ -43,7 +52,8 @@ def env_int(name, default):
 
 # --------------------------------------------------------------- clocks ----
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling every 20 ms; only the samples
+    taken between mark_start() and mark_stop() (the timed region) count."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -52,21 +62,34 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (host time, csv line)
+        self.t0 = self.t1 = None
 
-    def start(self):
+    def start(self, wait_s=5.0):
+        """Start sampling and wait (at most wait_s) for the first sample."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
             self.proc = None
+            return
+        t_end = time.perf_counter() + wait_s
+        while not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.01)
 
     def _read(self):
         for ln in self.proc.stdout:
-            self.lines.append(ln.strip())
+            self.lines.append((time.perf_counter(), ln.strip()))
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_stop(self):
+        self.t1 = time.perf_counter()
+        time.sleep(0.05)  # the sample taken at the region's end
 
     def stop(self):
         if not self.proc:
@@ -79,7 +102,11 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0 = self.t0 if self.t0 is not None else -1e30
+        t1 = (self.t1 + 0.025) if self.t1 is not None else 1e30
+        for ts, ln in self.lines:
+            if ts < t0 or ts > t1:
+                continue
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -92,7 +119,7 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "interval_ms": 20}
 
 
 # ---------------------------------------------------------- distributed ----
@@ -204,50 +231,61 @@ def accuracy_vs_oracle(pair, g, poi, gpu_out, stride=31):
     return out
 
 
+def cpu_frame(pair, g, poi, nthreads=0):
+    """One whole frame on the host cores, as the reference's CPU path runs it:
+    FFT-CC of every POI (Fftcc2D_CPU::Algorithm_FFTCC), then IC-GN of every
+    POI including the per-call whole-ROI gradient and LUT precompute
+    (ICGN2D_CPU::ICGN2D_Algorithm).  Returns seconds."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    u, v, z, st = O.fftcc(pair.ref, pair.tar, poi, g.subset_r, nthreads=nthreads)
+    O.icgn(pair.ref, pair.tar, g, poi, u, v, nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
 def run_reference(args, world, rank):
+    """Whole frames of the workload on the host cores, timed one per step
+    (warm-up steps are bounded samples of 2000 POIs)."""
     if rank != 0:
         return 0
     pair, g = workload()
-    from tw_gb300 import synth  # noqa: F401
     from oracle import oracle as O
     nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
     poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
-    rate, dt, thr = cpu_rate(pair, g, poi, 1000)
-    per_step = int(min(len(poi), max(1000, rate * 3.0)))  # about 3 s of CPU work per step
+    P = len(poi)
     for _ in range(args.warmup):
-        cpu_rate(pair, g, poi, 500)
-    rates, spent = [], []
-    for _ in range(args.steps):
-        r, dt, thr = cpu_rate(pair, g, poi, per_step)
-        rates.append(r)
-        spent.append(dt)
-    value = len(rates) / sum(1.0 / r for r in rates)  # frames at the harmonic-mean rate
-    lat = sorted(1000.0 * len(poi) / r for r in rates)  # full-frame latency, extrapolated
-    times = [1000.0 * len(poi) / r / 1000.0 for r in rates]
+        cpu_frame(pair, g, poi[:2000])
+    t_wall0 = time.perf_counter()
+    secs = [cpu_frame(pair, g, poi) for _ in range(args.steps)]
+    t_wall = time.perf_counter() - t_wall0
+    value = P * len(secs) / sum(secs)
+    lat = [1000.0 * x for x in secs]
     line = {"metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1000.0 * sum(times) / len(times), 3),
+            "warmup": args.warmup, "ms_per_step": round(sum(lat) / len(lat), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD, "step": f"bounded sample of {per_step} POIs per step"},
-            "frame_latency_ms": {"p50": round(lat[len(lat) // 2], 1), "p99": round(lat[-1], 1),
-                                 "note": "full-frame latency extrapolated from the sample"},
-            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": thr, "kind": "port",
-                             "sample": f"{per_step} POIs per step (+ whole-ROI precompute), extrapolated to "
-                                       f"{len(poi)} POIs; {sum(spent):.1f} s of CPU work over {args.steps} steps"},
+            "impl": "reference", "config": config_of(P, 1),
+            "frame_latency_ms": {"p50": round(pct(lat, 50), 1), "p99": round(pct(lat, 99), 1)},
+            "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                             "sample": f"whole frames of {P} POIs (FFT-CC + IC-GN with the per-call whole-ROI "
+                                       f"gradient/LUT precompute), one per step; {sum(secs):.1f} s over "
+                                       f"{args.steps} steps; OpenMP over POIs"},
             "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "gpu_launches": 0}
+            "gpu_launches": 0,
+            "wall_s_timed_region": round(t_wall, 3)}
     print(json.dumps(line))
     return 0
 
 
 # ------------------------------------------------------------- GPU legs ----
-def time_frames(fr, tar_dev, outs, steps, warmup, flush, torch):
+def time_frames(fr, tar_dev, outs, steps, warmup, flush, torch, clocks=None):
     """Device-timed frames with device-resident inputs; L2 flushed between
     frames outside the timed events."""
     for i in range(warmup):
         flush.fill_(i)
         fr.process(tar_dev, **outs)
     torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.mark_start()
     stream = torch.cuda.current_stream()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     phases = []
@@ -258,6 +296,8 @@ def time_frames(fr, tar_dev, outs, steps, warmup, flush, torch):
         evs[i][1].record(stream)
         phases.append(fr.phase_times())
     torch.cuda.synchronize()
+    if clocks is not None:
+        clocks.mark_stop()
     ms = [a.elapsed_time(b) for a, b in evs]
     return ms, phases
 
@@ -313,7 +353,7 @@ def _run_gpu(args, world, rank, local, torch):
     clocks = ClockSampler(local)
     clocks.start()
     t_wall0 = time.perf_counter()
-    ms, phases = time_frames(fr, tar_dev, outs, args.steps, args.warmup, flush, torch)
+    ms, phases = time_frames(fr, tar_dev, outs, args.steps, args.warmup, flush, torch, clocks)
     t_wall = time.perf_counter() - t_wall0
     torch.cuda.synchronize()
     dist_barrier(world)
@@ -339,17 +379,6 @@ def _run_gpu(args, world, rank, local, torch):
     acc = C.truth_error(pair, poi, p6, flags)
     kbar = float(iters[flags == 0].mean())
 
-    # plain FP32 GPU path, same workload, same timing rules
-    frp = dic.DICFrame(params_of(g, PATH_PLAIN))
-    frp.set_stream(torch.cuda.current_stream())
-    frp.set_reference(ref_dev)
-    outs_p = frp.alloc_outputs(device="cuda")
-    psteps = max(3, min(args.steps, 10))
-    ms_p, phases_p = time_frames(frp, tar_dev, outs_p, psteps, min(args.warmup, 3), flush, torch)
-    plain_value = P * psteps / (sum(ms_p) / 1000.0)
-    del frp, outs_p
-    torch.cuda.empty_cache()
-
     # roofline of the dominant phase
     ph = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
     roof = roofline(g, P, ph, kbar)
@@ -358,15 +387,10 @@ def _run_gpu(args, world, rank, local, torch):
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (IC-GN), fp16 tensor core / fp32 (FFT-CC), "
                                                             "fp64 (6x6 solve)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "path": "fast", "pois": P, "l2": "flushed between steps (256 MB write, "
-                       "outside the timed events)", "parallelism": f"replicas x{world}"},
+            "config": config_of(P, world),
+            "path": "fast (tensor-core FFT-CC, one-POI-per-warp IC-GN on the neighbourhood table)",
             "frame_latency_ms": {"p50": round(pct(ms, 50), 4), "p99": round(pct(ms, 99), 4)},
             "phases_ms": {k: round(v, 4) for k, v in ph.items()},
-            "plain_fp32": {"value": round(plain_value, 1), "ms_per_step": round(sum(ms_p) / psteps, 4),
-                           "p50_ms": round(pct(ms_p, 50), 4), "p99_ms": round(pct(ms_p, 99), 4),
-                           "phases_ms": {k: round(statistics.mean(p[k] for p in phases_p), 4)
-                                         for k in phases_p[0]}},
-            "speedup_vs_plain_fp32": round(value / (plain_value * world), 3),
             "accuracy": {"vs_imposed_field": acc, "mean_iterations": round(kbar, 3),
                          "success_fraction": float((flags == 0).mean())},
             "roofline": roof,
@@ -377,6 +401,27 @@ def _run_gpu(args, world, rank, local, torch):
             "gpu_launches": 3 * args.steps,
             "clocks": clk,
             "wall_s_timed_region": round(t_wall, 3)}
+    if not args.no_plain:
+        # plain FP32 GPU path, same workload, same timing rules
+        frp = dic.DICFrame(params_of(g, PATH_PLAIN))
+        frp.set_stream(torch.cuda.current_stream())
+        frp.set_reference(ref_dev)
+        outs_p = frp.alloc_outputs(device="cuda")
+        psteps = max(3, min(args.steps, 10))
+        ms_p, phases_p = time_frames(frp, tar_dev, outs_p, psteps, min(args.warmup, 3), flush, torch)
+        plain_value = P * psteps / (sum(ms_p) / 1000.0)
+        php = {k: statistics.mean(p[k] for p in phases_p) for k in phases_p[0]}
+        del frp, outs_p
+        torch.cuda.empty_cache()
+        line["plain_fp32"] = {"value": round(plain_value, 1), "ms_per_step": round(sum(ms_p) / psteps, 4),
+                              "p50_ms": round(pct(ms_p, 50), 4), "p99_ms": round(pct(ms_p, 99), 4),
+                              "phases_ms": {k: round(v, 4) for k, v in php.items()}}
+        line["speedup_vs_plain_fp32"] = round(value / (plain_value * world), 3)
+        # the same ratio per phase: FFT-CC (tensor-core DFT GEMMs against a
+        # direct FP32 DFT), target table (neighbourhood table against the
+        # float LUT), IC-GN
+        line["speedup_vs_plain_fp32_by_phase"] = {k: round(php[k] / ph[k], 3) for k in ("fftcc", "prepare", "icgn")
+                                                  if ph.get(k, 0) > 0}
     if rank == 0 and not args.no_serving:
         # serving (12 camera streams, Poisson arrivals) and batched uneven
         # pairs, each on its own synthetic data generated before its run
@@ -410,21 +455,40 @@ NCU_ICGN_L1_HIT = 0.891
 NCU_ICGN_FMAHEAVY = 0.680
 
 
+def fp32_peak(peaks):
+    """FP32 SIMT peak: SMs x 128 FP32 lanes x 2 flops (FMA) x the measured
+    maximum SM clock.  Derived, not measured: MEASURED_PEAKS.json has no FP32
+    figure.  Returns (flops/s, description)."""
+    sms = 152
+    try:
+        import torch
+        if torch.cuda.is_available():
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    return sms * 128 * 2 * sm_mhz * 1e6, f"derived: {sms} SMs x 128 FP32 lanes x 2 flops x {sm_mhz:.0f} MHz"
+
+
 def roofline(g, P, ph, kbar):
     """Roofline of the dominant kernel, the fast IC-GN (k_icgn_warp), timed by
     the per-phase CUDA events of the frame.
 
-    HBM view (the one reported as `frac`): algorithmic bytes per launch are
-    the compulsory ones -- the target's 4x4 neighbourhood table read once
-    (16 B per ROI pixel), the per-reference gradient image (4 B per ROI
-    pixel), the target image once, and per POI the reference cache entry
-    (statistics 64 B, FP64 inverse Hessian 168 B, flag 1 B), the POI (8 B),
-    u/v in (8 B) and out (8 B), p6 (24 B), iteration count (4 B) and flag
-    (1 B).  The kernel is not HBM bound: its per-sample gathers (k*S*20 B per
-    POI, k = mean iterations) are served by L1 (89 % hits) and L2, and it is
-    limited by the SM's FP32 / integer pipes (FMA-heavy pipe busy 68 % of
-    cycles); the gather and FP32 views are reported beside it, with the
-    tensor-core view of the FFT-CC kernel (48 N^3 flops per POI)."""
+    Binding view (bound / achieved / peak / frac): FP32.  The kernel is
+    limited by the SM's FP32 and integer pipes (ncu: FMA-heavy pipe busy 68 %
+    of cycles, 79 % issue) with its gathers served by L1 (89 % hits); the
+    credited work is k*S*64 flops per POI (k = mean iterations, S = subset
+    pixels; 64 flops per sample and iteration: warp 8, bicubic Horner 30,
+    mean/norm 6, residual 4, right-hand side 12, address 4), against the
+    derived FP32 peak.
+
+    Secondary views: HBM (the compulsory bytes per launch: the target's 4x4
+    neighbourhood table read once, 16 B per ROI pixel; the per-reference
+    gradient image, 4 B per ROI pixel; the target image; per POI the
+    reference cache entry -- statistics 64 B, FP64 inverse Hessian 168 B, flag
+    1 B -- the POI 8 B, u/v in 8 B and out 8 B, p6 24 B, iteration count 4 B
+    and flag 1 B); gathers (k*S*20 B per POI through L1/L2); and the tensor
+    view of the FFT-CC kernel (48 N^3 flops per POI)."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -433,32 +497,35 @@ def roofline(g, P, ph, kbar):
     hbm = peaks.get("hbm_gbs", 6800.0)
     tc = peaks.get("bf16_tflops", 1900.0)
     src = "measured" if peaks else "fallback"
+    fp32, fp32_src = fp32_peak(peaks)
     S = (2 * g.subset_r + 1) ** 2
     N = 2 * g.subset_r
     t_icgn = ph["icgn"] / 1000.0
     t_fftcc = ph["fftcc"] / 1000.0
     per_poi = 64 + 168 + 1 + 8 + 8 + 8 + 24 + 4 + 1
     bytes_icgn = P * per_poi + (16 + 4) * g.roi_w * g.roi_h + g.img_w * g.img_h
-    achieved = bytes_icgn / t_icgn / 1e9
+    flops_icgn = kbar * S * 64 * P
+    achieved = flops_icgn / t_icgn / 1e12
     gather = kbar * S * 20 * P
     flops_fftcc = 48 * N ** 3 * P
     fft_tflops = flops_fftcc / t_fftcc / 1e12
-    return {"kernel": "k_icgn_warp (IC-GN)", "bound": "hbm", "achieved": round(achieved, 2), "peak": hbm,
-            "unit": "GB/s", "frac": round(achieved / hbm, 5), "traffic": NCU_TRAFFIC["k_icgn_warp"],
-            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)",
-            "algorithmic_bytes_per_launch": int(bytes_icgn), "kernel_ms": round(ph["icgn"], 4),
+    return {"kernel": "k_icgn_warp (IC-GN)", "bound": "fp32", "achieved": round(achieved, 3),
+            "peak": round(fp32 / 1e12, 2), "unit": "TFLOP/s", "frac": round(achieved * 1e12 / fp32, 4),
+            "traffic": NCU_TRAFFIC["k_icgn_warp"], "peak_source": fp32_src,
+            "flops_per_launch": int(flops_icgn), "kernel_ms": round(ph["icgn"], 4),
+            "ncu": {"fmaheavy_pipe_busy": NCU_ICGN_FMAHEAVY, "l1_hit_rate": NCU_ICGN_L1_HIT},
+            "hbm_view": {"algorithmic_bytes_per_launch": int(bytes_icgn),
+                         "achieved_gbs": round(bytes_icgn / t_icgn / 1e9, 2), "peak_gbs": hbm,
+                         "frac": round(bytes_icgn / t_icgn / 1e9 / hbm, 5), "traffic": NCU_TRAFFIC["k_icgn_warp"],
+                         "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)"},
             "gather_view": {"gather_bytes_per_launch": int(gather), "achieved_gbs": round(gather / t_icgn / 1e9, 1),
                             "l1_hit_rate_ncu": NCU_ICGN_L1_HIT},
-            "fp32_view": {"flops_per_launch": int(kbar * S * 64 * P),
-                          "achieved_tflops": round(kbar * S * 64 * P / t_icgn / 1e12, 2),
-                          "fmaheavy_pipe_busy_ncu": NCU_ICGN_FMAHEAVY},
             "fftcc_tensor_view": {"kernel": "k_fftcc_tc", "flops_per_launch": int(flops_fftcc),
                                   "achieved_tflops": round(fft_tflops, 2), "peak_tflops": tc,
                                   "frac": round(fft_tflops / tc, 4), "kernel_ms": round(ph["fftcc"], 4),
-                                  "traffic": NCU_TRAFFIC["k_fftcc_tc"]},
-            "frame_roofline": frame_roofline(g, P, ph, kbar, peaks, bytes_icgn),
-            "note": "frac is against HBM; the IC-GN kernel is bound by the SM's FP32/integer pipes "
-                    "(gathers served by L1), see gather_view and fp32_view"}
+                                  "traffic": NCU_TRAFFIC["k_fftcc_tc"],
+                                  "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)"},
+            "frame_roofline": frame_roofline(g, P, ph, kbar, peaks, bytes_icgn)}
 
 
 def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
@@ -473,16 +540,8 @@ def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
     clock."""
     N = 2 * g.subset_r
     S = (2 * g.subset_r + 1) ** 2
-    sms = 152
-    try:
-        import torch
-        if torch.cuda.is_available():
-            sms = torch.cuda.get_device_properties(0).multi_processor_count
-    except Exception:
-        pass
-    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     peak_tc = peaks.get("bf16_tflops", 1900.0) * 1e12
-    peak_fp32 = sms * 128 * 2 * sm_mhz * 1e6
+    peak_fp32, fp32_src = fp32_peak(peaks)
     peak_hbm = peaks.get("hbm_gbs", 6800.0) * 1e9
     t_tc = P * 48 * N ** 3 / peak_tc
     t_fp32 = P * kbar * S * 64 / peak_fp32
@@ -496,7 +555,7 @@ def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
                          "hbm_compulsory": round(t_hbm * 1e3, 4)},
             "peaks": {"tensor_tflops": peak_tc / 1e12, "fp32_tflops": round(peak_fp32 / 1e12, 1),
                       "hbm_gbs": peak_hbm / 1e9,
-                      "fp32_source": f"{sms} SMs x 128 lanes x 2 flops x {sm_mhz:.0f} MHz (derived, not measured)"}}
+                      "fp32_source": fp32_src}}
 
 
 def main(argv=None):
@@ -507,6 +566,7 @@ def main(argv=None):
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving and batched legs")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparator leg")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

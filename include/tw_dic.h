@@ -140,7 +140,9 @@ typedef struct twdic_icgn twdic_icgn;
 TWDIC_API int twdic_icgn_create(const twdic_params* p, int32_t num_x, int32_t num_y, twdic_icgn** out);
 /* ResetRefImg / cuInitialize (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:770-795;
  * TW_paDIC_ICGN2D_CPU.cpp:66-70).  The per-reference precompute runs on the
- * next compute call whose POIs differ from the cached ones. */
+ * next compute call, and again on any later call whose POI contents differ
+ * from the previous call's (host or device POIs alike: a device POI array is
+ * read afresh on every call, so it may be rewritten in place between calls). */
 TWDIC_API int twdic_icgn_reset_ref(twdic_icgn* h, const uint8_t* img, int32_t stride, int mem);
 /* cuCompute (TW/TW_Engine/TW_paDIC_cuICGN2D.cu:811-968) with the CPU path's
  * semantics ICGN2D_Algorithm (TW_paDIC_ICGN2D_CPU.cpp:77-132, :481-925).
@@ -274,9 +276,14 @@ TWDIC_API int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t s
  *   - every call shares the one array: calls whose GPU work overlaps (other
  *     streams, other host threads) race and corrupt each other's results --
  *     serialise them;
+ *   - the parameters are checked as twdic_icgn_create checks them; the
+ *     path must be TWDIC_PATH_FAST (TWDIC_ERR_UNSUPPORTED otherwise);
  *   - the first call on a device resolves the array's device address
  *     (cudaGetSymbolAddress, which may load the library's module on that
- *     device); make that first call before any stream capture. */
+ *     device); make that first call before any stream capture.  The address
+ *     is resolved again when another context is current on the device;
+ *     cudaDeviceReset between calls is not supported (the new primary
+ *     context may not be told apart from the old one). */
 #define TWDIC_NOALLOC_MAX_POIS 196608
 TWDIC_API int twdic_icgn_compute_noalloc(const twdic_params* p, const uint8_t* d_ref, const uint8_t* d_tar,
                                          const int32_t* d_poi_yx, int32_t num_pois, float* d_u, float* d_v,

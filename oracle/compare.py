@@ -42,15 +42,16 @@ class FftccReport:
         return self.unexplained == 0 and self.max_zncc_err <= ZNCC_TOL
 
 
-def fftcc_parity(ref, tar, poi, r, u, v, z, u_or, v_or, z_or, st_or, tie_rtol=1e-5) -> FftccReport:
+def fftcc_parity(ref, tar, poi, r, u, v, z, u_or, v_or, z_or, st_or, tie_rtol=1e-5, ry=None) -> FftccReport:
+    """r: window half width (and height unless ry is given)."""
     ok = st_or == 0
     mis = ok & ((u != u_or) | (v != v_or))
     exact = rounding = unexplained = 0
-    n2 = 2 * r
+    ry = r if ry is None else ry
     for i in np.nonzero(mis)[0]:
-        c = O.exact_surface(ref, tar, poi[i, 0], poi[i, 1], r)
-        a = c[int(v[i]) % n2, int(u[i]) % n2]
-        b = c[int(v_or[i]) % n2, int(u_or[i]) % n2]
+        c = O.exact_surface(ref, tar, poi[i, 0], poi[i, 1], r, ry=ry)
+        a = c[int(v[i]) % (2 * ry), int(u[i]) % (2 * r)]
+        b = c[int(v_or[i]) % (2 * ry), int(u_or[i]) % (2 * r)]
         span = float(c.max() - c.min()) or 1.0
         if a == b:
             exact += 1

@@ -88,12 +88,28 @@ def fftcc(ref, tar, poi_yx, r, precision="f32", nthreads=0, init=0.0, ry=None):
     return u, v, z, st
 
 
-def exact_surface(ref, tar, py, px, r):
+def exact_surface(ref, tar, py, px, r, ry=None):
+    """Exact integer circular correlation sum f(x) g(x + k) of the [2ry][2rx]
+    windows at (py, px), indexed [ky][kx]."""
     H, W = ref.shape
-    c = np.zeros((2 * r, 2 * r), np.int64)
+    ry = r if ry is None else ry
+    c = np.zeros((2 * ry, 2 * r), np.int64)
     lib().or_fftcc_exact_surface(_p(np.ascontiguousarray(ref)), _p(np.ascontiguousarray(tar)), W, int(py), int(px),
-                                 int(r), int(r), _p(c))
+                                 int(r), int(ry), _p(c))
     return c
+
+
+def candidate_lower_bound(ref, tar, py, px, r, window=0.008):
+    """Number of shifts whose exact ZNCC lies within `window` of the exact
+    peak.  With the tensor-core FFT-CC's surface error below 1e-3, every such
+    shift is among its candidates (those within 0.01 of the approximate
+    peak), so this is a lower bound on that candidate count."""
+    c = exact_surface(ref, tar, py, px, r).astype(np.float64)
+    f = ref[py - r:py + r, px - r:px + r].astype(np.float64)
+    g = tar[py - r:py + r, px - r:px + r].astype(np.float64)
+    n2 = (2 * r) ** 2
+    z = (c - n2 * f.mean() * g.mean()) / np.sqrt(((f - f.mean()) ** 2).sum() * ((g - g.mean()) ** 2).sum())
+    return int((z >= z.max() - window).sum())
 
 
 def icgn(ref, tar, geom, poi_yx, u0, v0, precision="f32", nthreads=0, iters_init=0, interp="bicubic"):

@@ -1,17 +1,22 @@
 """GPU parity of the C-ABI paths against the oracle (the FP32 restatement of
 the reference CPU path), at sizes the oracle finishes in seconds, plus
 size-independent properties at the full 2048x2048 workload."""
+import glob
+import os
+
 import numpy as np
 import pytest
 
 from oracle import compare as C
 from oracle import oracle as O
-from tw_gb300 import PATH_FAST, PATH_PLAIN, SAMPLER_LUT, SAMPLER_NBHD, SAMPLER_WINDOW, synth
+from tw_gb300 import (INTERP_BICUBIC, INTERP_BSPLINE, PATH_FAST, PATH_PLAIN, SAMPLER_LUT, SAMPLER_NBHD,
+                      SAMPLER_WINDOW, synth)
 from tw_gb300 import dic
 
 pytestmark = pytest.mark.gpu
 
 PATHS = [PATH_PLAIN, PATH_FAST]
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def params_of(g, path):
@@ -71,11 +76,13 @@ def test_frame_parity(request, case, path):
                       g.grid, g.margin, g.margin, path=path)
     U, V, Z = f.InitializeFFTCC(pair.ref)
     f.ComputeFFTCC(U, V, Z, pair.tar)
+    rep_f = C.fftcc_parity(pair.ref, pair.tar, poi, g.subset_r, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or,
+                           st_or)
+    assert rep_f.ok(), rep_f
     same_start = (U.ravel() == u_or) & (V.ravel() == v_or)
-    assert same_start.mean() > 0.99
     rep = C.icgn_parity(out["p6"], out["iters"], out["flags"], p6_or, it_or, fl_or, mask=same_start,
                         r=g.subset_r)
-    print(case, path, rep)
+    print(case, path, rep_f, rep)
     assert rep.ok(), rep
     np.testing.assert_array_equal(out["u"], out["p6"][:, 0])
     np.testing.assert_array_equal(out["v"], out["p6"][:, 3])
@@ -320,9 +327,10 @@ def test_non_square_subsets():
                           g.margin, g.margin, path=path)
         U, V, Z = f.InitializeFFTCC(pair.ref)
         f.ComputeFFTCC(U, V, Z, pair.tar)
+        rep_f = C.fftcc_parity(pair.ref, pair.tar, poi, rx, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or, st_or,
+                               ry=ry)
+        assert rep_f.ok(), (path, rep_f)
         same = (U.ravel() == u_or) & (V.ravel() == v_or)
-        assert same.mean() > 0.95, (path, same.mean())
-        np.testing.assert_allclose(Z.ravel()[same], z_or[same], atol=1e-4)
         fr = dic.DICFrame(prm)
         fr.set_reference(pair.ref)
         out = fr.alloc_outputs()
@@ -406,11 +414,20 @@ def test_full_size_properties():
     assert d[:, [0, 3]].max() < 1e-3
     err = C.truth_error(pair, poi, a["p6"], a["flags"])
     assert err["rms"] < 0.02, err
-    # oracle on a sample of POIs (its FFT-CC guesses), through the IC-GN API
+    # oracle on a sample of POIs: the integer FFT-CC of the whole frame on
+    # both paths, then IC-GN from the oracle's guesses through the IC-GN API
     rng = np.random.default_rng(0)
     idx = np.sort(rng.choice(len(poi), 3000, replace=False))
     sp = poi[idx]
     u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, sp, g.subset_r)
+    for path in PATHS:
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, g.subset_r, g.subset_r, g.grid,
+                          g.grid, g.margin, g.margin, path=path)
+        U, V, Z = f.InitializeFFTCC(pair.ref)
+        f.ComputeFFTCC(U, V, Z, pair.tar)
+        rep_f = C.fftcc_parity(pair.ref, pair.tar, sp, g.subset_r, U.ravel()[idx], V.ravel()[idx], Z.ravel()[idx],
+                               u_or, v_or, z_or, st_or)
+        assert rep_f.ok(), (path, rep_f)
     p6_or, it_or, fl_or = O.icgn(pair.ref, pair.tar, g, sp, u_or, v_or)
     for path in PATHS:
         ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r,
@@ -421,3 +438,110 @@ def test_full_size_properties():
         p6, fl = ic.ICGN2D_Algorithm(u, v, iters, sp, pair.tar)
         rep = C.icgn_parity(p6, iters, fl, p6_or, it_or, fl_or, r=g.subset_r)
         assert rep.ok(), (path, rep)
+
+
+@pytest.mark.parametrize("y_amp,min_cand", [(1.5, 129), (8.0, 17)])
+def test_fftcc_broad_surface_parity(y_amp, min_cand):
+    """Low-texture stripes give a broad, periodic correlation surface: every
+    POI has more candidate shifts (within 0.01 ZNCC of the approximate peak)
+    than one exact-evaluation pass of a group batch holds at y_amp 1.5
+    (about 200 per POI), and more than 16 at y_amp 8.  Every candidate is
+    evaluated exactly, in a fixed slot order, so the integer result equals
+    the oracle's and repeats bit for bit."""
+    ref, tar = synth.stripe_pair(y_amp=y_amp)
+    r, grid, margin = 20, 9, 12
+    g = synth.Geometry(170, 150, 1, 1, 168, 148, r, grid, margin)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, r, grid, margin)
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, margin, r, grid)
+    counts = np.array([O.candidate_lower_bound(ref, tar, py, px, r) for py, px in poi])
+    assert counts.min() >= min_cand, counts.min()
+    u_or, v_or, z_or, st_or = O.fftcc(ref, tar, poi, r)
+    for path in PATHS:
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, r, r, grid, grid, margin, margin,
+                          path=path)
+        runs = []
+        for _ in range(2):
+            U, V, Z = f.InitializeFFTCC(ref)
+            st = np.zeros(f.GetNumPOIs(), np.uint8)
+            f.ComputeFFTCC(U, V, Z, tar, status=st)
+            runs.append((U.copy(), V.copy(), Z.copy()))
+            assert (st == st_or).all()
+        rep = C.fftcc_parity(ref, tar, poi, r, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or, st_or)
+        print(y_amp, path, rep)
+        assert rep.ok(), (y_amp, path, rep)
+        for a, b in zip(runs[0], runs[1]):
+            np.testing.assert_array_equal(a, b)
+
+
+REF_CASES = sorted(os.path.basename(p)[4:-4] for p in glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
+
+
+@pytest.mark.parametrize("path", PATHS)
+@pytest.mark.parametrize("case", REF_CASES)
+def test_gpu_matches_reference_fixture(case, path):
+    """The CUDA path against the outputs of the reference's own CPU code
+    (tests/golden/ref_<case>.npz, made from the reference sources): integer
+    FFT-CC equal but for counted ties, ZNCC within 3e-5; IC-GN from the
+    stored guesses with the reference's flags, its iteration counts but for
+    convergence-threshold ties (at most 1 % + 1), u and v within 1e-3 px."""
+    d = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
+    gm = [int(x) for x in d["geom"]]
+    g = synth.Geometry(gm[0], gm[1], gm[2], gm[3], gm[4], gm[5], gm[6], gm[8], gm[9], gm[10],
+                       float(d["delta_p"]), subset_ry=gm[7])
+    ref, tar, poi = d["ref"], d["tar"], d["poi"]
+    rx, ry = g.subset_r, g.subset_ry
+    if "fftcc_u" in d:
+        f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, rx, ry, g.grid, g.grid,
+                          g.margin, g.margin, path=path)
+        np.testing.assert_array_equal(f.POIPositions(), poi)
+        U, V, Z = f.InitializeFFTCC(ref)
+        st = np.zeros(f.GetNumPOIs(), np.uint8)
+        f.ComputeFFTCC(U, V, Z, tar, status=st)
+        rep = C.fftcc_parity(ref, tar, poi, rx, U.ravel(), V.ravel(), Z.ravel(), d["fftcc_u"], d["fftcc_v"],
+                             d["fftcc_zncc"], st, ry=ry)
+        assert rep.ok(), (case, path, rep)
+    for interp in ("bicubic", "bspline"):
+        if f"{interp}_u" not in d:
+            continue
+        n = len(poi)
+        ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, rx, ry, n, 1, g.max_iter,
+                          g.delta_p, path=path,
+                          Iflag=INTERP_BSPLINE if interp == "bspline" else INTERP_BICUBIC)
+        ic.ResetRefImg(ref)
+        u, v = d["guess_u"].copy(), d["guess_v"].copy()
+        iters = np.zeros(n, np.int32)
+        p6, fl = ic.ICGN2D_Algorithm(u, v, iters, poi, tar)
+        np.testing.assert_array_equal(fl, d[f"{interp}_flags"], err_msg=f"{case} {interp} {path}")
+        ties = int((iters != d[f"{interp}_iters"]).sum())
+        assert ties <= int(0.01 * n) + 1, (case, interp, path, ties)
+        du = float(np.abs(u - d[f"{interp}_u"]).max())
+        dv = float(np.abs(v - d[f"{interp}_v"]).max())
+        print(case, interp, path, "ties", ties, "du", du, "dv", dv)
+        assert du <= C.UV_TOL and dv <= C.UV_TOL, (case, interp, path, du, dv)
+
+
+def test_device_pois_rewritten_in_place(small):
+    """A device POI array rewritten in place between two calls (same
+    address, new contents) is read afresh: the second call's results follow
+    the new POIs (here the same POIs in reverse order, so a stale reference
+    cache would pair every POI with another POI's Hessian)."""
+    import torch
+    pair, g, poi, (u_or, v_or, z_or, st_or, p6_or, it_or, fl_or) = small
+    n = len(poi)
+    ic = dic.cuICGN2D(g.img_w, g.img_h, g.start_x, g.start_y, g.roi_w, g.roi_h, g.subset_r, g.subset_r, n, 1,
+                      g.max_iter, g.delta_p, path=PATH_FAST)
+    ic.cuInitialize(torch.from_numpy(pair.ref).cuda())
+    d_tar = torch.from_numpy(pair.tar).cuda()
+    d_poi = torch.from_numpy(poi).cuda()
+    for order in (np.arange(n), np.arange(n)[::-1].copy()):
+        d_poi.copy_(torch.from_numpy(poi[order]))
+        du = torch.from_numpy(u_or[order]).cuda()
+        dv = torch.from_numpy(v_or[order]).cuda()
+        p6 = torch.zeros((n, 6), dtype=torch.float32, device="cuda")
+        it = torch.zeros(n, dtype=torch.int32, device="cuda")
+        fl = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        ic.cuCompute(d_tar, d_poi, du, dv, p6, it, fl)
+        torch.cuda.synchronize()
+        rep = C.icgn_parity(p6.cpu().numpy(), it.cpu().numpy(), fl.cpu().numpy(), p6_or[order], it_or[order],
+                            fl_or[order], r=g.subset_r)
+        assert rep.ok(), rep

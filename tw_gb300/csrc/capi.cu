@@ -157,7 +157,6 @@ struct Engine {
     DevBuf d_u, d_v, d_zncc, d_fst, d_p6, d_iters, d_flags, d_err, d_work, d_tw;
     // per-reference cache
     bool cache_valid = false;
-    const void* cache_poi_key = nullptr;
     std::vector<int32_t> cache_poi_host;
     DevBuf c_subR, c_sd, c_chol, c_norm, c_flag;  // plain
     DevBuf c_stat, c_chol64, c_flag64, c_grad;    // fast
@@ -369,6 +368,9 @@ int check_mem(int mem) {
 
 // Error message setter for entry points defined in other translation units.
 void set_error_message(const char* msg) { g_last_error = msg; }
+int validate_params(const twdic_params* p, bool need_grid, bool need_border) {
+    return validate(p, need_grid, need_border);
+}
 
 }  // namespace twdic
 
@@ -504,19 +506,28 @@ int twdic_icgn_compute(twdic_icgn* h, const uint8_t* tar, int32_t stride, const 
     Engine& e = h->e;
     const size_t n = (size_t)e.n;
     TW_TRY(e.set_tar(tar, stride, mem_in));
-    // POIs: the per-reference cache is keyed on their contents (host) or on
-    // the array's address (device).
+    // POIs: the per-reference cache is keyed on their contents.  Host POIs
+    // are compared with a host copy; device POIs are copied into the handle's
+    // array on every call by a kernel that reports whether any pair changed
+    // (the caller may rewrite the same buffer, or an allocator may hand its
+    // address to new POIs).
     if (mem_in == TWDIC_MEM_HOST) {
         if (e.cache_poi_host.size() != 2 * n || std::memcmp(e.cache_poi_host.data(), poi_yx, 8 * n) != 0) {
             e.cache_poi_host.assign(poi_yx, poi_yx + 2 * n);
             TW_TRY(copy_in(e.d_poi.p, poi_yx, 8 * n, mem_in, e.stream));
             e.cache_valid = false;
         }
-    } else if (e.cache_poi_key != poi_yx) {
-        TW_TRY(copy_in(e.d_poi.p, poi_yx, 8 * n, mem_in, e.stream));
-        e.cache_poi_key = poi_yx;
-        e.cache_poi_host.clear();
-        e.cache_valid = false;
+    } else {
+        int* changed_d = e.d_work.as<int>() + 2;
+        int changed = 0;
+        TW_CUDA(cudaMemsetAsync(changed_d, 0, sizeof(int), e.stream));
+        TW_CUDA(launch_poi_refresh(poi_yx, e.d_poi.as<int2>(), (int)n, changed_d, e.stream));
+        TW_CUDA(cudaMemcpyAsync(&changed, changed_d, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+        TW_CUDA(cudaStreamSynchronize(e.stream));
+        if (changed) {
+            e.cache_poi_host.clear();
+            e.cache_valid = false;
+        }
     }
     float *du = u, *dv = v, *dp6 = p6 ? p6 : e.d_p6.as<float>();
     int* dit = iters;

@@ -128,6 +128,9 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
 bool fftcc_tc_supported(const Geom& g);
 
 // ---- tracking loop (kernels_track.cu)
+// Copy n device (y, x) pairs into dst; *changed |= 1 when any pair differed
+// (the caller zeroes it first)
+cudaError_t launch_poi_refresh(const int32_t* src, int2* dst, int n, int* changed, cudaStream_t st);
 cudaError_t launch_track_update(int2* poi, const float* u, const float* v, float* acc_u, float* acc_v, int n,
                                 int lo_y, int hi_y, int lo_x, int hi_x, cudaStream_t st);
 cudaError_t launch_colormap(uint32_t* tex_u, uint32_t* tex_v, const int2* poi, const float* u, const float* v,

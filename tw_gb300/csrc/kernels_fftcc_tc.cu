@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <climits>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -43,7 +44,7 @@ namespace twdic {
 namespace {
 
 constexpr int kThreads = 128;
-constexpr int kMaxCand = 16;      // exact re-evaluations per POI
+constexpr int kCandChunk = 128;   // exact re-evaluations per pass (all POIs of a group batch)
 constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
 constexpr int kMaxGroups = 4;     // 128-thread groups per CTA (upper bound)
 // Candidate window of the approximate correlation surface, in ZNCC units.
@@ -98,10 +99,10 @@ struct TcJobs {
     TcJob job[kMaxJobs];
 };
 
+// Candidates of one pass: (POI << 16 | shift index) and exact sums.
 struct PeakScratch {
-    int cand[kMaxPB][kMaxCand];
-    float candV[kMaxPB][kMaxCand];  // approximate surface value of each candidate
-    int candS[kMaxPB][kMaxCand];
+    int cand[kCandChunk];
+    int candS[kCandChunk];
 };
 
 __host__ __device__ __forceinline__ int kmaj(int r, int k, int K) {  // LBO 128 B, SBO 16*K B
@@ -210,26 +211,6 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 }
 __device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast<__half*>(p) = __float2half_rn(v); }
 
-// Optional phase timing (compiled only with -DTWDIC_TC_TRACE): thread 0 of
-// every group adds the clock64() cycles of each phase of each batch; with
-// -DTWDIC_TC_TRACE_ERR as well, slot 14 records the largest error of the
-// approximate surface at any candidate.
-#ifdef TWDIC_TC_TRACE
-__device__ unsigned long long g_tc_trace[16];
-#define TC_MARK(i)                                                           \
-    do {                                                                     \
-        if (t == 0) {                                                        \
-            const long long now_ = clock64();                                \
-            atomicAdd(&g_tc_trace[i], (unsigned long long)(now_ - tmark_));  \
-            tmark_ = now_;                                                   \
-        }                                                                    \
-    } while (0)
-#else
-#define TC_MARK(i) \
-    do {           \
-    } while (0)
-#endif
-
 // ----------------------------------------------------------------- kernel --
 // blockDim = 128 * s.groups (up to four).  Each 128-thread group runs its
 // own batches (own operand region, TMEM columns, mbarriers and named barrier)
@@ -248,9 +229,10 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     __shared__ int wsum[kMaxGroups][2 * kMaxPB][2];
     __shared__ float sscale[kMaxGroups][kMaxPB];
     __shared__ int sdark[kMaxGroups][kMaxPB];
-    __shared__ int ncand[kMaxGroups][kMaxPB];
+    __shared__ int cbase[kMaxGroups][kMaxPB];      // first candidate slot of each POI
+    __shared__ int cend[kMaxGroups][kMaxPB];       // one past its last
+    __shared__ int wtot[kMaxGroups][4];            // candidates per warp
     __shared__ uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
-    __shared__ int smaxi[kMaxGroups][kMaxPB];       // its first index
     __shared__ int2 spoi[kMaxGroups][kMaxPB];
     __shared__ int wbase[kMaxGroups][2 * kMaxPB];  // byte offset of each window's (0, 0) in wwin
     __shared__ int wrs[kMaxGroups];                // row stride of the windows in wwin
@@ -306,9 +288,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
     uint32_t phase = 0, tphase = 0;
-#ifdef TWDIC_TC_TRACE
-    long long tmark_ = clock64();
-#endif
 
     // batches: the first of every group by position, then the next free one
     // from a launch-wide counter (taken by thread 0 at the start of a batch,
@@ -332,8 +311,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         if (t < PB) {
             spoi[grp][t] = (b0 + t < n_job) ? poi[b0 + t] : make_int2(-1, -1);
             smaxv[grp][t] = 0u;
-            smaxi[grp][t] = 0x7fffffff;
-            ncand[grp][t] = 1;
         }
         group_sync(bar_id);
 
@@ -383,7 +360,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         bool ok = mbar_wait(tbar, tphase);
         tphase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
-        TC_MARK(0);
 
         // ---- phase L2: windows -> A1 (rows (window, x), K = y), exact FP16;
         // integer sums per window by segmented warp reductions
@@ -420,7 +396,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         fence_async_smem();
         group_sync(bar_id);
-        TC_MARK(1);
 
         // ---- stage 1: D1[(w,x)][(part,ky)] = A1 * B1
         if (t == 0) {
@@ -451,7 +426,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
-        TC_MARK(2);
 
         // ---- epilogue 1: Y -> A2 (rows (p, ky, w); K = (part, x) with split
         // twiddles, K = (x, part) interleaved with single ones, so that a row's
@@ -515,7 +489,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         tc_fence_before();
         fence_async_smem();
         group_sync(bar_id);
-        TC_MARK(3);
 
         // ---- stage 2: F = Y * W (rows (p,ky,w); columns Re kx | Im kx)
         if (t == 0) {
@@ -553,7 +526,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
-        TC_MARK(4);
 
         // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
         {
@@ -621,7 +593,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         tc_fence_before();
         fence_async_smem();
         group_sync(bar_id);
-        TC_MARK(5);
 
         // ---- stage 3: conj(Z) = conj(C) * W (rows (p,ky); columns Re x | Im x)
         if (t == 0) {
@@ -658,7 +629,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
-        TC_MARK(6);
 
         // ---- epilogue 3: Z -> A4 (rows (p, x), K = (ky, part) interleaved:
         // k = 2 ky + part, so a POI row's Re and Im of one ky are one 32-bit
@@ -704,7 +674,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         tc_fence_before();
         fence_async_smem();
         group_sync(bar_id);
-        TC_MARK(7);
 
         // ---- stage 4: c[(p,x)][y] = A4 * B4
         if (t == 0) {
@@ -722,7 +691,6 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
         tc_fence_after();
-        TC_MARK(8);
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
         // (scratch in the shared operand region, which stage 4 has finished
@@ -730,12 +698,11 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         const bool rowv = t < PB * N;
         const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
         const bool live = rowv && !sdark[grp][p4];
-        if (t < kMaxPB * kMaxCand) (&ps->candS[0][0])[t] = 0;
-        // approximate peak per POI: row maxima (first on ties), then the
-        // largest value and, among rows holding it, the smallest index, each
-        // by a segmented warp reduction and one shared atomic per warp segment
+        if (t < kCandChunk) ps->candS[t] = 0;
+        // approximate peak value per POI: each thread's maximum over the
+        // surface rows y of its column x4, then a segmented warp reduction and
+        // one shared atomic per warp segment
         float bv = -3.4e38f;
-        int bi = 0x7fffffff;
 #pragma unroll
         for (int y0 = 0; y0 < NP; y0 += 8) {
             if (y0 >= N) break;  // padding columns
@@ -744,103 +711,126 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-                if (live && y0 + j < N && cv[j] > bv) { bv = cv[j]; bi = (y0 + j) * N + x4; }
+                if (live && y0 + j < N && cv[j] > bv) bv = cv[j];
         }
         const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
         const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
         if (live && lane == __ffs(seg) - 1) atomicMax(&smaxv[grp][p4], ov);
         group_sync(bar_id);
-        const uint32_t pv = live ? smaxv[grp][p4] : 0u;
-        const uint32_t mi = __reduce_min_sync(seg, (live && f32_ord(bv) == pv) ? (uint32_t)bi : 0xffffffffu);
-        if (live && lane == __ffs(seg) - 1 && mi != 0xffffffffu) atomicMin(&smaxi[grp][p4], (int)mi);
-        group_sync(bar_id);
-        TC_MARK(15);
         // candidates: every shift within kCandZncc (ZNCC units; the surface is
-        // N^2 ZNCC) of the approximate peak; slot 0 holds the approximate argmax
+        // N^2 ZNCC) of the approximate peak, the peak itself included, as one
+        // bit per surface row y of this thread's column; a warp with no such
+        // column skips the second read
+        uint64_t cmask = 0;
         {
-            const float th = f32_unord(pv) - kCandZncc * (float)n2;
-            const int first = live ? smaxi[grp][p4] : -1;
-            if (live && x4 == 0) {
-                ps->cand[p4][0] = first;
-                ps->candV[p4][0] = f32_unord(pv);
-            }
-            // a row holds a candidate only if its maximum reaches the
-            // threshold: warps with no such row skip the second read
+            const float th = live ? f32_unord(smaxv[grp][p4]) - kCandZncc * (float)n2 : 3.4e38f;
             if (__any_sync(kFull, live && bv >= th)) {
 #pragma unroll
-            for (int y0 = 0; y0 < NP; y0 += 8) {
-                if (y0 >= N) break;  // padding columns
-                float cv[8];
-                tmem_ld8(tm_warp + y0, cv);
-                tmem_ld_wait();
+                for (int y0 = 0; y0 < NP; y0 += 8) {
+                    if (y0 >= N) break;  // padding columns
+                    float cv[8];
+                    tmem_ld8(tm_warp + y0, cv);
+                    tmem_ld_wait();
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    if (live && y0 + j < N && cv[j] >= th) {
-                        const int idx = (y0 + j) * N + x4;
-                        if (idx != first) {
-                            const int slot = atomicAdd(&ncand[grp][p4], 1);
-                            if (slot < kMaxCand) {
-                                ps->cand[p4][slot] = idx;
-                                ps->candV[p4][slot] = cv[j];
-                            }
-                        }
-                    }
+                    for (int j = 0; j < 8; ++j)
+                        if (live && y0 + j < N && cv[j] >= th) cmask |= 1ull << (y0 + j);
                 }
-            }
             }
         }
         tc_fence_before();
+        // candidate slots in a fixed order (thread, then row) by a group-wide
+        // exclusive scan of the per-thread counts; a POI's threads are
+        // consecutive, so POI p owns the slots [cbase[p], cend[p])
+        const int cnt = __popcll(cmask);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int up = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += up;
+        }
+        if (lane == 31) wtot[grp][warp] = incl;
         group_sync(bar_id);
-        TC_MARK(9);
-        // exact integer correlation of every candidate, read from the staged
-        // windows: tasks (POI, candidate, row) over the group's threads, four
-        // products per DP4A, one shared atomic per task.  Lanes walk the words
-        // of their row in a lane-rotated order, which spreads rows that share
-        // shared-memory banks over different words.
-        {
-            const int NW4 = s.NW4;
-            const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
-            int total = 0;
-            for (int p = 0; p < PB; ++p) total += sdark[grp][p] ? 0 : min(ncand[grp][p], kMaxCand) * N;
-            const int rot = lane % NW4;
-            for (int task = t; task < total; task += 128) {
-                int p = 0, rem = task;
-                for (;;) {
-                    const int cnt = sdark[grp][p] ? 0 : min(ncand[grp][p], kMaxCand) * N;
-                    if (rem < cnt) break;
-                    rem -= cnt;
-                    ++p;
+        int wpre = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const int tw = wtot[grp][w];
+            wpre += (w < warp) ? tw : 0;
+            total += tw;
+        }
+        const int excl = wpre + incl - cnt;
+        if (rowv && x4 == 0) cbase[grp][p4] = excl;
+        if (rowv && x4 == N - 1) cend[grp][p4] = excl + cnt;
+        // exact integer correlation of every candidate, kCandChunk slots at a
+        // time (any number of candidates: a broad or periodic surface only
+        // takes more chunks), read from the staged windows: tasks (slot, row)
+        // over the group's threads, four products per DP4A, one shared atomic
+        // per task.  Lanes walk the words of their row in a lane-rotated
+        // order, which spreads rows that share shared-memory banks over
+        // different words.  Thread t < PB keeps POI t's best candidate: the
+        // largest exact sum, the smallest index among equal sums (the
+        // reference's first maximum), whatever the chunking.
+        int best_s = INT_MIN, best_i = 0;
+        for (int lo = 0; lo < total; lo += kCandChunk) {
+            if (lo > 0) {
+                group_sync(bar_id);  // the previous chunk's sums have been read
+                if (t < kCandChunk) ps->candS[t] = 0;
+            }
+            if (cnt > 0 && excl < lo + kCandChunk && excl + cnt > lo) {
+                uint64_t m = cmask;
+                for (int k = excl; m != 0; ++k) {
+                    const int y = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    if (k >= lo && k < lo + kCandChunk) ps->cand[k - lo] = (p4 << 16) | (y * N + x4);
                 }
-                const int c = rem / N, y = rem - c * N;
-                const int idx = ps->cand[p][c];
-                const int ky = idx / N, kx = idx - ky * N;
-                int yy = y + ky;
-                if (yy >= N) yy -= N;
+            }
+            group_sync(bar_id);
+            const int nc = min(total - lo, kCandChunk);
+            {
+                const int NW4 = s.NW4;
+                const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
+                const int rot = lane % NW4;
                 const int rs = wrs[grp];
-                const uint8_t* fb = wwin + wbase[grp][2 * p] + y * rs;
-                const uint8_t* gb = wwin + wbase[grp][2 * p + 1] + yy * rs;
-                const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
-                unsigned acc = 0;
-                int j = rot;
+                for (int task = t; task < nc * N; task += 128) {
+                    const int c = task / N, y = task - c * N;
+                    const int code = ps->cand[c];
+                    const int p = code >> 16, idx = code & 0xffff;
+                    const int ky = idx / N, kx = idx - ky * N;
+                    int yy = y + ky;
+                    if (yy >= N) yy -= N;
+                    const uint8_t* fb = wwin + wbase[grp][2 * p] + y * rs;
+                    const uint8_t* gb = wwin + wbase[grp][2 * p + 1] + yy * rs;
+                    const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
+                    unsigned acc = 0;
+                    int j = rot;
 #pragma unroll 2
-                for (int jj = 0; jj < NW4; ++jj) {
-                    uint32_t fw = ld_unaligned_p(fb + 4 * j);
-                    if (j == NW4 - 1) fw &= tail;
-                    int a = kx + 4 * j;  // g bytes (x + kx) mod N for x = 4j .. 4j+3
-                    if (a >= N) a -= N;
-                    uint32_t gw = ld_unaligned_p(gb + a);
-                    if (a + 4 > N) {
-                        const int nlo = N - a;
-                        gw = (gw & (0xffffffffu >> (8 * (4 - nlo)))) | (g0 << (8 * nlo));
+                    for (int jj = 0; jj < NW4; ++jj) {
+                        uint32_t fw = ld_unaligned_p(fb + 4 * j);
+                        if (j == NW4 - 1) fw &= tail;
+                        int a = kx + 4 * j;  // g bytes (x + kx) mod N for x = 4j .. 4j+3
+                        if (a >= N) a -= N;
+                        uint32_t gw = ld_unaligned_p(gb + a);
+                        if (a + 4 > N) {
+                            const int nlo = N - a;
+                            gw = (gw & (0xffffffffu >> (8 * (4 - nlo)))) | (g0 << (8 * nlo));
+                        }
+                        acc = __dp4a(fw, gw, acc);
+                        if (++j == NW4) j = 0;
                     }
-                    acc = __dp4a(fw, gw, acc);
-                    if (++j == NW4) j = 0;
+                    atomicAdd(&ps->candS[c], (int)acc);
                 }
-                atomicAdd(&ps->candS[p][c], (int)acc);
+            }
+            group_sync(bar_id);
+            if (t < PB && !sdark[grp][t]) {
+                const int a = max(cbase[grp][t], lo), b = min(cend[grp][t], lo + kCandChunk);
+                for (int k = a; k < b; ++k) {
+                    const int sc = ps->candS[k - lo], id = ps->cand[k - lo] & 0xffff;
+                    if (sc > best_s || (sc == best_s && id < best_i)) {
+                        best_s = sc;
+                        best_i = id;
+                    }
+                }
             }
         }
-        group_sync(bar_id);
-        TC_MARK(11);
         if (t < PB && b0 + t < n_job) {
             const int gp = b0 + t;
             float* u = jb.u;
@@ -850,17 +840,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             if (sdark[grp][t]) {
                 status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
             } else {
-                const int nc = min(ncand[grp][t], kMaxCand);
-#ifdef TWDIC_TC_TRACE
-                atomicAdd(&g_tc_trace[12], (unsigned long long)ncand[grp][t]);
-                if (ncand[grp][t] > kMaxCand) atomicAdd(&g_tc_trace[13], 1ull);
-#endif
-                int best = ps->cand[t][0], bs = ps->candS[t][0];
-                for (int c = 1; c < nc; ++c) {
-                    const int sc = ps->candS[t][c], id = ps->cand[t][c];
-                    if (sc > bs || (sc == bs && id < best)) { bs = sc; best = id; }
-                }
-                int iu = best % N, iv = best / N;
+                int iu = best_i % N, iv = best_i / N;
                 if (iu > g.rx) iu -= N;
                 if (iv > g.ry) iv -= N;
                 const long long sf = wsum[grp][2 * t][0], sg = wsum[grp][2 * t + 1][0];
@@ -869,27 +849,15 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 // exact integer numerator and norms; the quotient in FP32
                 // (relative error below 5e-7: GB300's FP64 divide and square
                 // root are slow)
-                const long long cnum = (long long)n2 * bs - sf * sg;
+                const long long cnum = (long long)n2 * best_s - sf * sg;
                 u[gp] = (float)iu;
                 v[gp] = (float)iv;
                 zncc[gp] = (float)cnum * rsqrtf((float)numf) * rsqrtf((float)numg);
-#ifdef TWDIC_TC_TRACE_ERR
-                // largest error of the approximate surface at the candidates,
-                // ZNCC units x 1e6 (a separate switch: its FP64 work would
-                // distort the phase timing)
-                for (int c = 0; c < nc; ++c) {
-                    const double zk = (double)((long long)n2 * ps->candS[t][c] - sf * sg) /
-                                      sqrt((double)numf * (double)numg);
-                    const double e = fabs((double)ps->candV[t][c] / n2 - zk);
-                    atomicMax(&g_tc_trace[14], (unsigned long long)(e * 1e6));
-                }
-#endif
                 status[gp] = 0;
             }
         }
         if (t == 0) snext[grp] = nxt;
         group_sync(bar_id);
-        TC_MARK(10);
     }
 
     // ---- teardown
@@ -1180,13 +1148,3 @@ cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* ta
 }
 
 }  // namespace twdic
-
-#ifdef TWDIC_TC_TRACE
-// Trace builds only: copy out and clear the per-phase cycle counters.
-extern "C" __attribute__((visibility("default"))) int twdic_tc_trace_read(unsigned long long* out16) {
-    cudaDeviceSynchronize();
-    if (cudaMemcpyFromSymbol(out16, twdic::g_tc_trace, sizeof(unsigned long long) * 16) != cudaSuccess) return -1;
-    unsigned long long z[16] = {};
-    return cudaMemcpyToSymbol(twdic::g_tc_trace, z, sizeof(z)) == cudaSuccess ? 0 : -1;
-}
-#endif

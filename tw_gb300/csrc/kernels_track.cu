@@ -2,6 +2,8 @@
 // displacement colour map of TW_Core's FFT-CC worker thread
 // (TW/TW_Core/fftcctworkerthread.cpp:228-330, :408-438; kernels at
 // TW/TW_Core/cuda_utils.cu:109-240).
+#include <algorithm>
+
 #include "dic_common.cuh"
 #include "dic_kernels.h"
 
@@ -83,6 +85,23 @@ __global__ void k_colormap(uint32_t* __restrict__ tex_u, uint32_t* __restrict__ 
     }
 }
 
+// Device POIs of the IC-GN handle: copied into the handle's array, read as
+// 32-bit words (the caller's array need only be 4-byte aligned); *changed is
+// set when any pair differs from the array's previous contents, for which
+// the per-reference precompute was made.
+__global__ void k_poi_refresh(const int32_t* __restrict__ src, int2* __restrict__ dst, int n, int* changed) {
+    int diff = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += blockDim.x * gridDim.x) {
+        const int2 a = make_int2(src[2 * i], src[2 * i + 1]);
+        const int2 b = dst[i];
+        if (a.x != b.x || a.y != b.y) {
+            dst[i] = a;
+            diff = 1;
+        }
+    }
+    if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+
 }  // namespace
 
 cudaError_t launch_track_update(int2* poi, const float* u, const float* v, float* acc_u, float* acc_v, int n,
@@ -100,6 +119,13 @@ cudaError_t launch_colormap(uint32_t* tex_u, uint32_t* tex_v, const int2* poi, c
     const int grid = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
     k_colormap<<<grid, 256, 0, st>>>(tex_u, tex_v, poi, u, v, acc_u, acc_v, n, g.sx, g.sy, g.rw, g.rh, min_u, max_u,
                                      min_v, max_v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_poi_refresh(const int32_t* src, int2* dst, int n, int* changed, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int grid = std::min((n + 255) / 256, 1024);
+    k_poi_refresh<<<grid, 256, 0, st>>>(src, dst, n, changed);
     return cudaGetLastError();
 }
 

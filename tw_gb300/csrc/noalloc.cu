@@ -22,7 +22,8 @@
 
 namespace twdic {
 
-void set_error_message(const char* msg);  // capi.cu
+void set_error_message(const char* msg);                                      // capi.cu
+int validate_params(const twdic_params* p, bool need_grid, bool need_border);  // capi.cu
 
 namespace {
 
@@ -43,22 +44,45 @@ static __device__ __align__(256) unsigned char g_icgn_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the context the address was resolved in
 
 int fail_msg(int code, const char* msg) {
     set_error_message(msg);
     return code;
 }
 
-// Device address of the scratch array on the current device.  The first call
-// per device resolves it with cudaGetSymbolAddress (which may load the
-// module on that device); later calls reuse the cached address.
+// cuCtxGetCurrent, resolved once through the runtime (no link-time
+// dependency on libcuda)
+typedef int (*ctx_get_current_t)(void**);
+ctx_get_current_t ctx_get_current() {
+    static ctx_get_current_t fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<ctx_get_current_t>(f);
+    }();
+    return fn;
+}
+
+// Device address of the scratch array in the current context.  The first
+// call on a device (and the first after another context is made current on
+// it) resolves it with cudaGetSymbolAddress, which may load the library's
+// module there; later calls reuse it.
 int scratch_address(void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail_msg(TWDIC_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail_msg(TWDIC_ERR_UNSUPPORTED, "device ordinal out of range");
+    auto current_ctx = [] {
+        void* c = nullptr;
+        if (auto fn = ctx_get_current()) fn(&c);
+        return c;
+    };
+    void* ctx = current_ctx();
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_icgn_scratch);
         if (e != cudaSuccess || !p) {
@@ -67,6 +91,7 @@ int scratch_address(void** out) {
             return fail_msg(TWDIC_ERR_CUDA, buf);
         }
         g_scratch_ptr[dev] = p;
+        g_scratch_ctx[dev] = current_ctx();  // the runtime has made its context current by now
     }
     *out = g_scratch_ptr[dev];
     return TWDIC_OK;
@@ -80,26 +105,22 @@ extern "C" TWDIC_API int twdic_icgn_compute_noalloc(const twdic_params* p, const
                                                     int32_t num_pois, float* d_u, float* d_v, float* d_p6,
                                                     int32_t* d_iters, uint8_t* d_flags, void* stream) {
     using namespace twdic;
-    if (!p || !d_ref || !d_tar || !d_poi_yx || !d_u || !d_v || !d_p6 || !d_iters || !d_flags)
+    if (!d_ref || !d_tar || !d_poi_yx || !d_u || !d_v || !d_p6 || !d_iters || !d_flags)
         return fail_msg(TWDIC_ERR_INVALID_ARG, "NULL argument (every buffer is required)");
+    // the parameter checks of the handle entry points (twdic_icgn_create)
+    int rc = validate_params(p, false, true);
+    if (rc != TWDIC_OK) return rc;
+    if (p->path != TWDIC_PATH_FAST)
+        return fail_msg(TWDIC_ERR_UNSUPPORTED, "twdic_icgn_compute_noalloc runs the fast path only (path = 1)");
     if (num_pois <= 0) return fail_msg(TWDIC_ERR_NO_POI, "Number of POIs is below 0!");
     if (num_pois > TWDIC_NOALLOC_MAX_POIS)
         return fail_msg(TWDIC_ERR_UNSUPPORTED,
                         "twdic_icgn_compute_noalloc: num_pois exceeds TWDIC_NOALLOC_MAX_POIS (196608)");
     if (reinterpret_cast<uintptr_t>(d_poi_yx) % 8 != 0)
         return fail_msg(TWDIC_ERR_INVALID_ARG, "POI array must be 8-byte aligned");
-    if (p->img_width <= 0 || p->img_height <= 0 || p->roi_width <= 0 || p->roi_height <= 0)
-        return fail_msg(TWDIC_ERR_INVALID_ARG, "image and ROI sizes must be positive");
-    if (p->subset_x < 1 || p->subset_y < 1) return fail_msg(TWDIC_ERR_INVALID_ARG, "subset half size must be >= 1");
-    if (p->subset_x > 31 || p->subset_y > 31) return fail_msg(TWDIC_ERR_UNSUPPORTED, "subset half size exceeds 31");
-    if (p->max_iterations < 1 || !(p->delta_p >= 0.f))
-        return fail_msg(TWDIC_ERR_INVALID_ARG, "max_iterations must be >= 1 and delta_p >= 0");
-    if (p->start_x < 1 || p->start_y < 1 || p->start_x + p->roi_width + 1 > p->img_width ||
-        p->start_y + p->roi_height + 1 > p->img_height)
-        return fail_msg(TWDIC_ERR_BORDER, "Not enough boundary pixels for gradients!");
 
     void* scratch = nullptr;
-    int rc = scratch_address(&scratch);
+    rc = scratch_address(&scratch);
     if (rc != TWDIC_OK) return rc;
     unsigned char* base = static_cast<unsigned char*>(scratch);
     float* stats = reinterpret_cast<float*>(base + kStatsOff);

@@ -179,6 +179,28 @@ def small_case(h: int = 160, w: int = 192, r: int = 10, grid: int = 7, seed: int
     return pair, Geometry(w, h, 1, 1, w - 2, h - 2, r, grid, 12)
 
 
+def stripe_pair(h: int = 150, w: int = 170, period: int = 8, y_amp: float = 1.5, shift=(3, 2), seed: int = 5,
+                noise_sigma: float = 2.0) -> Tuple[np.ndarray, np.ndarray]:
+    """A low-texture pair with a broad, periodic correlation surface:
+    vertical stripes of `period` px (amplitude 50 around 128) with a weak
+    vertical texture of amplitude `y_amp`, the target shifted by an integer
+    `shift` (dx, dy), noise sigma `noise_sigma`.  In a window whose width is a
+    multiple of the period nearly every vertical shift at every period
+    multiple correlates within 0.01 ZNCC of the peak (about 200 shifts per
+    40 x 40 window at y_amp 1.5, 40 to 80 at y_amp 8)."""
+    rng = np.random.default_rng(seed)
+    H, W = h + 40, w + 40
+    x = np.arange(W)[None, :]
+    y = np.arange(H)[:, None]
+    base = 128 + 50.0 * np.sin(2 * np.pi * x / period) + y_amp * np.sin(2 * np.pi * y / 37.0) * np.cos(
+        2 * np.pi * x / 53.0)
+    base = np.broadcast_to(base, (H, W))
+    dx, dy = shift
+    ref = base[20:20 + h, 20:20 + w] + rng.normal(0, noise_sigma, (h, w))
+    tar = base[20 - dy:20 - dy + h, 20 - dx:20 - dx + w] + rng.normal(0, noise_sigma, (h, w))
+    return (np.clip(np.rint(ref), 0, 255).astype(np.uint8), np.clip(np.rint(tar), 0, 255).astype(np.uint8))
+
+
 def camera_sequence(w: int, h: int, frames: int = 3, seed: int = 31, r: int = 15, grid: int = 8,
                     margin: int = 20):
     """A simulated camera: one reference and `frames` targets under a linear

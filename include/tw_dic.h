@@ -179,6 +179,29 @@ TWDIC_API int twdic_frame_set_stream(twdic_frame* h, void* stream);
  * t[4] result download, t[5] per-reference precompute (0 when cached). */
 TWDIC_API int twdic_frame_phase_times(const twdic_frame* h, float* t6);
 TWDIC_API int twdic_frame_destroy(twdic_frame* h);
+/* The interpolation and gradient tables of the frame's current images, for
+ * inspection, copied to host memory (dst: host floats).  The reference keeps
+ * these as members of its IC-GN classes (ICGN2D_CPU::m_fRx, m_fRy,
+ * m_fInterpolation, TW/TW_Engine/TW_paDIC_ICGN2D_CPU.h:113-125; cuICGN2D's
+ * device buffers in GPUHandle_ICGN, TW/TW_Engine/TW_paDIC.h:40-70).
+ *   TWDIC_TABLE_BICUBIC_LUT    roi_h x roi_w x 4 x 4: the target's bicubic LUT
+ *       (BicubicCoefficients_s, TW/TW_Engine/TW_utils.cpp:604-700), [y][x][k][n]
+ *       the coefficient of fy^k fx^n, last ROI row and column zero
+ *   TWDIC_TABLE_BSPLINE_LUT    the same for the B-spline LUT
+ *       (BicubicSplineCoefficients_s, TW_utils.cpp:521-602)
+ *   TWDIC_TABLE_REF_GRADIENT   roi_h x roi_w x 2: (R_x, R_y) of the reference
+ *       over the ROI, central differences (GradientXY_2Images_s,
+ *       TW_utils.cpp:232-305), as the fast path keeps them (half precision,
+ *       exact: halves of integers below 128)
+ *   TWDIC_TABLE_SUBSET_GRADIENT num_pois x S x 2 (S = subset pixels, row
+ *       major): (R_x, R_y) of every POI's subset as the plain path's
+ *       per-reference cache keeps them (plain path handles only)
+ * The LUTs need a target (a processed frame), the gradients a reference. */
+#define TWDIC_TABLE_BICUBIC_LUT 0
+#define TWDIC_TABLE_BSPLINE_LUT 1
+#define TWDIC_TABLE_REF_GRADIENT 2
+#define TWDIC_TABLE_SUBSET_GRADIENT 3
+TWDIC_API int twdic_frame_table(twdic_frame* h, int which, float* dst);
 
 /* IC-GN target interpolation, ICGN2DInterpolationFLag (TW/TW_Engine/TW_paDIC.h:89-93),
  * the Iflag of the ICGN2D_CPU / cuICGN2D constructors (TW_paDIC_ICGN2D_CPU.h:23-44):

@@ -545,3 +545,37 @@ def test_device_pois_rewritten_in_place(small):
         rep = C.icgn_parity(p6.cpu().numpy(), it.cpu().numpy(), fl.cpu().numpy(), p6_or[order], it_or[order],
                             fl_or[order], r=g.subset_r)
         assert rep.ok(), rep
+
+
+@pytest.mark.parametrize("case", ["small", "plain512"])
+def test_tables_equal_the_oracle(request, case):
+    """The per-pixel tables element by element against the oracle: the
+    bicubic LUT of the target (k_bicubic_lut) bit for bit, including the
+    zero last ROI row and column (TW_utils.cpp:604-700); the reference
+    gradients of the fast path (k_ref_grad) and of every subset in the plain
+    path's per-reference cache (k_ref_precompute_plain) exactly
+    (TW_utils.cpp:232-305); the B-spline LUT (k_bspline_lut) within FP32
+    rounding of its products (TW_utils.cpp:521-602)."""
+    pair, g, poi, _ = request.getfixturevalue(case)
+    rx_o, ry_o, tx_o, ty_o, txy_o, lut_o = O.precompute_f32(pair.ref, pair.tar, g.start_x, g.start_y, g.roi_w,
+                                                            g.roi_h)
+    fr = dic.DICFrame(params_of(g, PATH_PLAIN))
+    fr.set_reference(pair.ref)
+    fr.process(pair.tar, **fr.alloc_outputs())
+    lut = fr.table("bicubic_lut")
+    np.testing.assert_array_equal(lut, lut_o)
+    assert (lut[-1] == 0).all() and (lut[:, -1] == 0).all() and np.abs(lut[:-1, :-1]).max() > 0
+    grad = fr.table("ref_gradient")
+    np.testing.assert_array_equal(grad[..., 0], rx_o)
+    np.testing.assert_array_equal(grad[..., 1], ry_o)
+    sub = fr.table("subset_gradient")
+    r = g.subset_r
+    off = np.arange(-r, r + 1)
+    yy = poi[:, 0, None, None] + off[None, :, None] - g.start_y
+    xx = poi[:, 1, None, None] + off[None, None, :] - g.start_x
+    np.testing.assert_array_equal(sub[..., 0], rx_o[yy, xx].reshape(len(poi), -1))
+    np.testing.assert_array_equal(sub[..., 1], ry_o[yy, xx].reshape(len(poi), -1))
+    bs = fr.table("bspline_lut").reshape(g.roi_h, g.roi_w, 16)
+    bs_o = O.bspline_lut(pair.tar, g.start_x, g.start_y, g.roi_w, g.roi_h)
+    print(case, "B-spline LUT: exact", float((bs == bs_o).mean()), "max diff", float(np.abs(bs - bs_o).max()))
+    np.testing.assert_allclose(bs, bs_o, rtol=1e-6, atol=1e-4)

@@ -40,6 +40,7 @@ EXPORTED = (
     "twdic_icgn_create", "twdic_icgn_reset_ref", "twdic_icgn_compute", "twdic_icgn_destroy",
     "twdic_frame_create", "twdic_frame_num_pois", "twdic_frame_poi_positions", "twdic_frame_set_reference",
     "twdic_frame_process", "twdic_frame_set_stream", "twdic_frame_phase_times", "twdic_frame_destroy",
+    "twdic_frame_table",
     "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_icgn_unroll", "twdic_frame_set_guess_mode", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
     "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_icgn_unroll", "twdic_batch_set_graph",
     "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
@@ -148,6 +149,7 @@ def load():
         "twdic_frame_process": ([_VP, _VP, ctypes.c_int32, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I], _I),
         "twdic_frame_set_stream": ([_VP, _VP], _I),
         "twdic_frame_phase_times": ([_VP, _VP], _I),
+        "twdic_frame_table": ([_VP, _I, _VP], _I),
         "twdic_frame_destroy": ([_VP], _I),
         "twdic_frame_set_tuning": ([_VP, _I, _I, _I, _I], _I),
         "twdic_frame_set_icgn_layout": ([_VP, _I], _I),

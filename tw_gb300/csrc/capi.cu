@@ -638,6 +638,64 @@ int twdic_frame_process(twdic_frame* h, const uint8_t* tar, int32_t stride, int 
     if (!dev) return e.check_err();
     return TWDIC_OK;
 }
+int twdic_frame_table(twdic_frame* h, int which, float* dst) {
+    if (!h || !dst) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    Engine& e = h->e;
+    const Geom& g = e.g;
+    const size_t px = (size_t)g.rw * g.rh;
+    if (which == TWDIC_TABLE_BICUBIC_LUT || which == TWDIC_TABLE_BSPLINE_LUT) {
+        if (!e.have_tar) return fail(TWDIC_ERR_STATE, "the LUT needs a target image (process a frame first)");
+        DevBuf lut;
+        TW_TRY(lut.ensure(sizeof(float4) * 4 * px));
+        if (which == TWDIC_TABLE_BICUBIC_LUT)
+            TW_CUDA(launch_bicubic_lut(g, e.d_tar.as<uint8_t>(), lut.as<float4>(), e.stream));
+        else
+            TW_CUDA(launch_bspline_lut(g, e.d_tar.as<uint8_t>(), lut.as<float4>(), e.stream));
+        std::vector<float4> hb(4 * px);
+        TW_CUDA(cudaMemcpyAsync(hb.data(), lut.p, sizeof(float4) * 4 * px, cudaMemcpyDeviceToHost, e.stream));
+        TW_CUDA(cudaStreamSynchronize(e.stream));
+        // device layout: plane k of float4 (n = 0..3) per ROI pixel
+        for (size_t o = 0; o < px; ++o)
+            for (int k = 0; k < 4; ++k) {
+                const float4 c = hb[k * px + o];
+                float* d = dst + o * 16 + k * 4;
+                d[0] = c.x; d[1] = c.y; d[2] = c.z; d[3] = c.w;
+            }
+        return TWDIC_OK;
+    }
+    if (which == TWDIC_TABLE_REF_GRADIENT) {
+        if (!e.have_ref) return fail(TWDIC_ERR_STATE, "the gradients need a reference image");
+        DevBuf grad;
+        TW_TRY(grad.ensure(sizeof(__half2) * px));
+        TW_CUDA(launch_ref_grad(g, e.d_ref.as<uint8_t>(), grad.as<__half2>(), e.stream));
+        std::vector<__half2> hb(px);
+        TW_CUDA(cudaMemcpyAsync(hb.data(), grad.p, sizeof(__half2) * px, cudaMemcpyDeviceToHost, e.stream));
+        TW_CUDA(cudaStreamSynchronize(e.stream));
+        for (size_t o = 0; o < px; ++o) {
+            dst[2 * o] = __low2float(hb[o]);
+            dst[2 * o + 1] = __high2float(hb[o]);
+        }
+        return TWDIC_OK;
+    }
+    if (which == TWDIC_TABLE_SUBSET_GRADIENT) {
+        if (e.prm.path != TWDIC_PATH_PLAIN) return fail(TWDIC_ERR_STATE, "per-subset gradients: plain path only");
+        if (!e.have_ref) return fail(TWDIC_ERR_STATE, "the gradients need a reference image");
+        TW_TRY(e.ensure_cache(nullptr));
+        const size_t S = (size_t)(2 * g.rx + 1) * (2 * g.ry + 1), n = (size_t)e.n;
+        std::vector<float2> hb(3 * S * n);
+        TW_CUDA(cudaMemcpyAsync(hb.data(), e.c_sd.p, sizeof(float2) * 3 * S * n, cudaMemcpyDeviceToHost,
+                                e.stream));
+        TW_CUDA(cudaStreamSynchronize(e.stream));
+        // steepest-descent planes per POI: (R_x, R_x dx), (R_x dy, R_y), (R_y dx, R_y dy)
+        for (size_t p = 0; p < n; ++p)
+            for (size_t k = 0; k < S; ++k) {
+                dst[(p * S + k) * 2] = hb[p * 3 * S + k].x;
+                dst[(p * S + k) * 2 + 1] = hb[p * 3 * S + S + k].y;
+            }
+        return TWDIC_OK;
+    }
+    return fail(TWDIC_ERR_INVALID_ARG, "unknown table %d", which);
+}
 int twdic_frame_phase_times(const twdic_frame* hc, float* t6) {
     if (!hc || !t6) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
     auto* h = const_cast<twdic_frame*>(hc);

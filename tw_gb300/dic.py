@@ -337,6 +337,19 @@ class DICFrame:
                     iters=torch.zeros(n, dtype=torch.int32, device=device),
                     flags=torch.zeros(n, dtype=torch.uint8, device=device))
 
+    def table(self, which):
+        """Host copy of one of the frame's tables (twdic_frame_table):
+        "bicubic_lut" / "bspline_lut" [roi_h, roi_w, 4, 4], "ref_gradient"
+        [roi_h, roi_w, 2], "subset_gradient" [num_pois, S, 2]."""
+        p = self.params
+        rw, rh = p.roi_width, p.roi_height
+        S = (2 * p.subset_x + 1) * (2 * p.subset_y + 1)
+        code, shape = {"bicubic_lut": (0, (rh, rw, 4, 4)), "bspline_lut": (1, (rh, rw, 4, 4)),
+                       "ref_gradient": (2, (rh, rw, 2)), "subset_gradient": (3, (self.n, S, 2))}[which]
+        out = np.zeros(shape, np.float32)
+        check(self._lib.twdic_frame_table(self._h, code, _ptr(out)))
+        return out
+
     def phase_times(self):
         t = np.zeros(6, np.float32)
         check(self._lib.twdic_frame_phase_times(self._h, _ptr(t)))

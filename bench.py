@@ -426,8 +426,14 @@ def _run_gpu(args, world, rank, local, torch):
         # serving (12 camera streams, Poisson arrivals) and batched uneven
         # pairs, each on its own synthetic data generated before its run
         from tw_gb300.batch_bench import run_batched
-        from tw_gb300.serve_bench import run_serving
-        line["serving"] = run_serving(seconds=4.0)
+        from tw_gb300.serve_bench import make_streams, run_serving
+        sdata = make_streams()
+        line["serving"] = run_serving(seconds=4.0, data=sdata)
+        # the same streams at twice the arrival rates (the GPU near saturation:
+        # frames queue, batches form, lanes overlap) and at four times (overload:
+        # the queues fill and frames are dropped)
+        line["serving_saturation"] = run_serving(seconds=4.0, data=sdata, load=2.0)
+        line["serving_overload"] = run_serving(seconds=4.0, data=sdata, load=4.0)
         line["batched"] = run_batched(pairs=48, steps=3)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O  # noqa: F401  (CPU baseline leg)

@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define TWDIC_ABI_VERSION 1
+#define TWDIC_ABI_VERSION 2
 
 /* status codes */
 #define TWDIC_OK 0
@@ -356,10 +356,14 @@ TWDIC_API int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes);
  * hbm_budget_bytes (0 = 90 % of the free memory at creation).  twdic_submit
  * copies a target into one of the stream's queue_depth pinned slots, or drops
  * it with TWDIC_ERR_BUSY when all are taken (the reference's bounded frame
- * queue).  A scheduler thread batches the oldest pending frame of every idle
- * stream (up to max_batch) into one twdic_batch launch on a free lane (CUDA
- * stream, up to `lanes` batches in flight), so frames that arrive while
- * others are on the GPU join the next batch.  Results equal
+ * queue).  A scheduler thread batches the next pending frame of idle streams
+ * (up to max_batch) into one twdic_batch launch on a free lane (CUDA stream,
+ * up to `lanes` batches in flight), so frames that arrive while others are on
+ * the GPU join the next batch.  By default (mix_sizes = 0) the frames are
+ * taken in order of expected finish (submit time plus an estimate of the
+ * frame's device time from its POI count) and a batch holds only frames
+ * within a factor of two of its first frame's POI count; with mix_sizes = 1,
+ * oldest first and any sizes.  Results equal
  * twdic_frame_process on the same frame.  twdic_poll returns TWDIC_PENDING
  * until the frame is done (wait = 1 blocks), then copies the results out and
  * frees the slot; latency_ms is submit-to-done.  A ticket is read once: a
@@ -378,12 +382,20 @@ typedef struct {
     int32_t start_paused; /* 1: hold frames until twdic_server_resume */
     int32_t icgn_threads; /* fast IC-GN launch shape (0 = default) */
     int32_t icgn_sampler; /* fast IC-GN target sampler when icgn_threads > 0 */
+    int32_t mix_sizes;    /* 0 (default): a batch holds the oldest pending frame and the frames whose
+                             POI count is within a factor of two of it; 1: frames of any size */
 } twdic_server_config;
 typedef struct {
     uint64_t submitted, completed, dropped, batches, batched_frames, graph_replays;
     uint64_t committed_bytes, budget_bytes;
     int32_t streams;
     double p50_ms, p99_ms, max_ms; /* submit-to-done latency over completed frames */
+    uint64_t max_batch_formed;     /* frames in the largest batch launched */
+    int32_t peak_lanes_in_flight;  /* most batches launched and not yet retired at one time */
+    int32_t peak_device_batches;   /* most batches running on the device at one time */
+    double device_busy_ms;         /* device time with a batch running (union of the batches'
+                                      intervals, timed by CUDA events on their lanes) */
+    double device_overlap_ms;      /* device time with two or more batches running */
 } twdic_server_counters;
 TWDIC_API int twdic_server_create(const twdic_server_config* cfg, twdic_server** out);
 TWDIC_API int twdic_server_add_stream(twdic_server* s, const twdic_params* p, int32_t* stream_id);

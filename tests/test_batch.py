@@ -57,7 +57,9 @@ def test_batch_equals_frames_alone():
 
 
 def test_batch_more_frames_than_one_launch_holds():
-    cases = [(64, 72 + 4 * (i % 5), 5, 6, 100 + i, PATH_FAST) for i in range(35)]
+    """130 frames: more than the 128 one IC-GN (and one FFT-CC) launch takes,
+    with two window sizes, so the batch runs two launches of each."""
+    cases = [(64, 72 + 4 * (i % 5), 5 + (i % 2), 6, 100 + i, PATH_FAST) for i in range(130)]
     frames, tars, want = _alone(cases)
     b = dic.DICBatch()
     outs = [f.alloc_outputs() for f in frames]

@@ -36,7 +36,7 @@ def test_header_declares_what_the_binding_binds():
 def test_library_exports_every_declared_symbol(lib):
     for s in header_symbols():
         assert hasattr(lib, s), s
-    assert lib.twdic_abi_version() == 1
+    assert lib.twdic_abi_version() == 2
 
 
 def test_params_struct_matches_header(lib):

@@ -15,14 +15,15 @@ def _params(g, path=PATH_FAST):
 
 def test_frame_device_bytes_formula():
     """Host-only estimate used for admission: images padded to 16-byte rows,
-    per-POI buffers and the fast path's cache, gradient image and
+    per-POI buffers, the small buffers (error flag, work counter, twiddles,
+    TMA descriptors) and the fast path's cache, gradient image and
     neighbourhood table, each rounded up to 2 MiB."""
     _, g = synth.small_case(h=160, w=197, r=10, grid=7)
     p = _params(g)
     n = dic.num_pois(p)[0] * dic.num_pois(p)[1]
     r = lambda b: -(-b // (2 << 20)) * (2 << 20)  # noqa: E731
     pitch = (197 + 15) // 16 * 16
-    want = (2 * r(pitch * 160) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 3 * r(1024)
+    want = (2 * r(pitch * 160) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 4 * r(1024)
             + r(64 * n) + r(168 * n) + r(n) + r(4 * g.roi_w * g.roi_h) + r(16 * g.roi_w * g.roi_h))
     assert frame_device_bytes(p) == want
     big = _params(synth.Geometry(2048, 2048, 1, 1, 2046, 2046, 20, 5, 20))
@@ -42,7 +43,9 @@ CASES = [(160, 192, 10, 7, 21), (130, 257, 10, 5, 22), (200, 150, 16, 9, 23)]
 def test_results_same_alone_and_in_the_mix():
     pairs = [synth.small_case(h=h, w=w, r=r, grid=gr, seed=s) for h, w, r, gr, s in CASES]
     pairs2 = [synth.small_case(h=h, w=w, r=r, grid=gr, seed=s, u0=-0.7, v0=1.3) for h, w, r, gr, s in CASES]
-    srv = DICServer(max_batch=8, queue_depth=4, lanes=2)
+    # frames of any size share a batch here; the server starts paused so that
+    # the first frames of all streams are pending together
+    srv = DICServer(max_batch=8, queue_depth=4, lanes=2, start_paused=True, mix_sizes=True)
     sids = []
     for pair, g in pairs:
         sid = srv.add_stream(_params(g))
@@ -56,10 +59,13 @@ def test_results_same_alone_and_in_the_mix():
             t = srv.submit(sid, tar)
             assert t is not None
             tickets.append((sid, t, rnd))
+    srv.resume()
     got = {(sid, rnd): srv.poll(sid, t) for sid, t, rnd in tickets}
     st = srv.stats()
     assert st["completed"] == len(tickets) and st["dropped"] == 0
     assert st["batches"] >= 1 and st["batched_frames"] == len(tickets)
+    # the first batch took the pending frame of every stream
+    assert st["max_batch_formed"] == len(pairs), st
     assert st["p99_ms"] >= st["p50_ms"] > 0
     for sid, (pair, g), (pair2, _) in zip(sids, pairs, pairs2):
         f = dic.DICFrame(_params(g))
@@ -71,6 +77,40 @@ def test_results_same_alone_and_in_the_mix():
             assert (w["flags"] == 0).mean() > 0.9
             for k in w:
                 np.testing.assert_array_equal(o[k], w[k], err_msg=f"stream {sid} frame {rnd} {k}")
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_batches_form_and_run_on_two_lanes():
+    """Four streams of one size, two frames each, queued while the server is
+    paused: on resume the scheduler fills both lanes with a batch of two
+    frames each (continuous batching over lanes); the device intervals of
+    the batches, timed by events on their lanes, are reported; every result
+    equals the frame processed alone."""
+    pair, g = synth.small_case()
+    pair2, _ = synth.small_case(u0=-0.7, v0=1.3)
+    srv = DICServer(max_batch=2, queue_depth=4, lanes=2, start_paused=True)
+    sids = []
+    for _ in range(4):
+        sid = srv.add_stream(_params(g))
+        srv.set_reference(sid, pair.ref)
+        sids.append(sid)
+    tickets = [(sid, srv.submit(sid, tar), k) for k, tar in enumerate((pair.tar, pair2.tar)) for sid in sids]
+    srv.resume()
+    got = {(sid, k): srv.poll(sid, t) for sid, t, k in tickets}
+    st = srv.stats()
+    print(st)
+    assert st["completed"] == 8 and st["batches"] == 4
+    assert st["max_batch_formed"] == 2 and st["peak_lanes_in_flight"] == 2, st
+    assert st["device_busy_ms"] > 0 and st["peak_device_batches"] >= 1
+    f = dic.DICFrame(_params(g))
+    f.set_reference(pair.ref)
+    for k, tar in enumerate((pair.tar, pair2.tar)):
+        w = f.alloc_outputs()
+        f.process(tar, **w)
+        for sid in sids:
+            for key in w:
+                np.testing.assert_array_equal(got[(sid, k)][key], w[key], err_msg=f"stream {sid} frame {k} {key}")
     srv.close()
 
 

@@ -79,7 +79,7 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [
         ("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int32), ("queue_depth", ctypes.c_int32),
         ("lanes", ctypes.c_int32), ("use_graph", ctypes.c_int32), ("start_paused", ctypes.c_int32),
-        ("icgn_threads", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32),
+        ("icgn_threads", ctypes.c_int32), ("icgn_sampler", ctypes.c_int32), ("mix_sizes", ctypes.c_int32),
     ]
 
 
@@ -108,6 +108,9 @@ class ServerCounters(ctypes.Structure):
         ("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64), ("graph_replays", ctypes.c_uint64),
         ("committed_bytes", ctypes.c_uint64), ("budget_bytes", ctypes.c_uint64), ("streams", ctypes.c_int32),
         ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+        ("max_batch_formed", ctypes.c_uint64), ("peak_lanes_in_flight", ctypes.c_int32),
+        ("peak_device_batches", ctypes.c_int32), ("device_busy_ms", ctypes.c_double),
+        ("device_overlap_ms", ctypes.c_double),
     ]
 
 

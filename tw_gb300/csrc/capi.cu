@@ -161,12 +161,19 @@ struct Engine {
     DevBuf c_subR, c_sd, c_chol, c_norm, c_flag;  // plain
     DevBuf c_stat, c_chol64, c_flag64, c_grad;    // fast
     DevBuf d_lut;
+    // TMA descriptors of d_ref / d_tar for the tensor-core FFT-CC: a pinned
+    // host copy and the device copy the kernels read, re-encoded when the
+    // launch shape changes
+    DevBuf d_tcmaps;
+    void* h_tcmaps = nullptr;
+    TcMapInfo tcmaps{0, 0, 0};
     cudaEvent_t ev[7] = {};
     cudaEvent_t ev_sync = nullptr;  // orders this handle's stream with a batch stream
     float last_times[6] = {0, 0, 0, 0, 0, 0};
     bool times_pending = false;
 
     ~Engine() {
+        if (h_tcmaps) cudaFreeHost(h_tcmaps);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (ev_sync) cudaEventDestroy(ev_sync);
@@ -201,6 +208,8 @@ struct Engine {
         TW_TRY(d_flags.ensure((size_t)n));
         TW_TRY(d_err.ensure(sizeof(unsigned)));
         TW_TRY(d_work.ensure(sizeof(int) * 4));
+        TW_TRY(d_tcmaps.ensure(kTcMapsBytes));
+        TW_CUDA(cudaMallocHost(&h_tcmaps, kTcMapsBytes));
         TW_CUDA(cudaMemsetAsync(d_err.p, 0, sizeof(unsigned), stream));
         // DFT twiddles exp(-2 pi i k / N) of the two window sizes, rounded once
         // from double (the FP32 SIMT FFT-CC kernel reads them)
@@ -253,12 +262,27 @@ struct Engine {
         return TWDIC_OK;
     }
 
+    // TMA descriptors of the images for a tensor-core FFT-CC launch of this
+    // shape: encoded and copied on this handle's stream when the shape
+    // changed (after the previous copy has read the host descriptors).
+    int ensure_tc_maps(const FftccTune& tune) {
+        const uint64_t key = fftcc_tc_maps_key(g, tune);
+        if (key != 0 && key == tcmaps.key) return TWDIC_OK;
+        if (tcmaps.key != 0) TW_CUDA(cudaStreamSynchronize(stream));
+        tcmaps.key = 0;
+        if (!fftcc_tc_encode_maps(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), tune, h_tcmaps, &tcmaps))
+            return fail(TWDIC_ERR_UNSUPPORTED, "tensor-core FFT-CC: tensor maps could not be encoded");
+        TW_CUDA(cudaMemcpyAsync(d_tcmaps.p, h_tcmaps, kTcMapsBytes, cudaMemcpyHostToDevice, stream));
+        return TWDIC_OK;
+    }
+
     // FFT-CC of all POIs into device arrays.
     int fftcc(float* u, float* v, float* z, uint8_t* st) {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "FFT-CC needs a reference and a target image");
         const int2* poi = d_poi.as<int2>();
         if (prm.path == TWDIC_PATH_FAST && fftcc_tune.use_tc && fftcc_tc_supported(g)) {
-            TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, u, v, z, st,
+            TW_TRY(ensure_tc_maps(fftcc_tune));
+            TW_CUDA(launch_fftcc_tc(g, d_tcmaps.p, tcmaps.key, tcmaps.uw, tcmaps.utoff, poi, n, u, v, z, st,
                                     d_err.as<unsigned>(), d_work.as<int>() + 1, fftcc_tune, stream));
         } else {
             TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, d_tw.as<float2>(), u, v, z,
@@ -743,7 +767,7 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
     t += 2 * r(img);                                        // reference, target
     t += r(8 * n);                                          // POIs
     t += 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n);  // u, v, zncc, status, p6, iters, flags
-    t += 3 * r(1024);                                       // error flag, work counter, twiddles
+    t += 4 * r(1024);                                       // error flag, work counter, twiddles, TMA descriptors
     if (p->path == TWDIC_PATH_PLAIN) {
         const uint64_t S = (uint64_t)(2 * p->subset_x + 1) * (2 * p->subset_y + 1);
         t += r(4 * n * S) + r(24 * n * S) + r(144 * n) + r(4 * n) + r(n);
@@ -1056,10 +1080,10 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
 }  // extern "C"
 
 // ------------------------------------------------------------- batches ----
-// Several frame handles' targets in one set of launches: fast-path frames of
-// one window size share one tensor-core FFT-CC launch and all fast-path
-// frames share one persistent IC-GN launch (kMaxJobs per launch).  No
-// reference counterpart (the reference runs one frame per call).
+// Several frame handles' targets in one set of launches: the fast-path frames
+// share one tensor-core FFT-CC launch (all window sizes) and one persistent
+// IC-GN launch per sampler (kMaxJobs frames per launch).  No reference
+// counterpart (the reference runs one frame per call).
 struct twdic_batch {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
@@ -1144,6 +1168,11 @@ int prepare_target_for(Engine& e, int sampler) {
 int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
     const int count = a.count;
     std::vector<int> fast_tc, fast_ic;
+    // per frame: its target into the handle, guesses in (host outputs), and
+    // its part of the preparation launch (neighbourhood table; outputs that
+    // start at zero: the counters always, u, v, zncc unless IC-GN starts from
+    // the given displacements)
+    std::vector<PrepJob> prep;
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
         e.stream = b->stream;
@@ -1152,56 +1181,80 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         const FrameOut o = frame_out(e, a, i);
         const size_t n = (size_t)e.n;
         const bool fast = e.prm.path == TWDIC_PATH_FAST;
-        TW_CUDA(cudaMemsetAsync(o.it, 0, 4 * n, b->stream));
+        PrepJob pj{};
+        pj.g = e.g;
+        pj.tar = e.d_tar.as<uint8_t>();
+        pj.n = e.n;
+        pj.zero_i = o.it;
+        if (fast) {
+            const int sampler = batch_sampler(b->tune, e);
+            if (sampler == kSampNbhd || sampler == kSampNbhdBs) {
+                TW_TRY(e.d_lut.ensure(sizeof(uint4) * (size_t)e.g.rw * e.g.rh));
+                pj.table = e.d_lut.as<uint4>();
+                pj.full = sampler == kSampNbhdBs ? 1 : 0;
+            }
+        }
         if (e.guess) {
             // IC-GN from the displacements in u, v (ZNCC is not recomputed)
             if (a.mem_out == TWDIC_MEM_HOST) {
                 TW_CUDA(cudaMemcpyAsync(o.u, a.u[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
                 TW_CUDA(cudaMemcpyAsync(o.v, a.v[i], 4 * n, cudaMemcpyHostToDevice, b->stream));
             }
-            if (fast) fast_ic.push_back(i);
-            continue;
+        } else {
+            pj.zero_f[0] = o.u;
+            pj.zero_f[1] = o.v;
+            pj.zero_f[2] = o.z;
+            if (fast && e.fftcc_tune.use_tc && fftcc_tc_supported(e.g)) fast_tc.push_back(i);
         }
-        TW_CUDA(cudaMemsetAsync(o.u, 0, 4 * n, b->stream));
-        TW_CUDA(cudaMemsetAsync(o.v, 0, 4 * n, b->stream));
-        TW_CUDA(cudaMemsetAsync(o.z, 0, 4 * n, b->stream));
-        if (fast && e.fftcc_tune.use_tc && fftcc_tc_supported(e.g))
-            fast_tc.push_back(i);
-        else
-            TW_TRY(e.fftcc(o.u, o.v, o.z, e.d_fst.as<uint8_t>()));
         if (fast) fast_ic.push_back(i);
+        prep.push_back(pj);
     }
-    // tensor-core FFT-CC: one launch per window size (and per kMaxJobs frames)
-    std::vector<bool> used(fast_tc.size(), false);
-    for (size_t k = 0; k < fast_tc.size(); ++k) {
-        if (used[k]) continue;
-        const int rx = a.frames[fast_tc[k]]->e.g.rx;
+    for (size_t k0 = 0; k0 < prep.size(); k0 += kMaxPrepJobs) {
+        PrepJobs P;
+        for (size_t k = k0; k < prep.size() && k < k0 + kMaxPrepJobs; ++k) {
+            PrepJob& pj = P.job[P.njobs++];
+            pj = prep[k];
+            pj.px_begin = P.px_total;
+            pj.z_begin = P.z_total;
+            if (pj.table) P.px_total += (long long)pj.g.rw * pj.g.rh;
+            P.z_total += pj.n;
+        }
+        TW_CUDA(launch_batch_prepare(P, b->stream));
+    }
+    // FFT-CC of the frames off the tensor-core path, one call each
+    for (int i = 0; i < count; ++i) {
+        Engine& e = a.frames[i]->e;
+        if (e.guess || std::find(fast_tc.begin(), fast_tc.end(), i) != fast_tc.end()) continue;
+        const FrameOut o = frame_out(e, a, i);
+        TW_TRY(e.fftcc(o.u, o.v, o.z, e.d_fst.as<uint8_t>()));
+    }
+    // tensor-core FFT-CC: one launch over every window size (the launch takes
+    // the frames in segments of one window size), per kMaxTcJobsPerLaunch frames
+    {
         std::vector<FftccJob> jobs;
-        for (size_t m = k; m < fast_tc.size(); ++m) {
-            if (used[m] || a.frames[fast_tc[m]]->e.g.rx != rx) continue;
+        for (size_t m = 0; m < fast_tc.size(); ++m) {
             const int i = fast_tc[m];
             Engine& e = a.frames[i]->e;
+            TW_TRY(e.ensure_tc_maps(b->fftcc_tune));
             const FrameOut o = frame_out(e, a, i);
-            jobs.push_back(FftccJob{e.g, e.d_ref.as<uint8_t>(), e.d_tar.as<uint8_t>(), e.d_poi.as<int2>(), e.n, o.u,
-                                    o.v, o.z, e.d_fst.as<uint8_t>()});
-            used[m] = true;
-            if ((int)jobs.size() == kMaxJobs) {
+            jobs.push_back(FftccJob{e.g, e.d_tcmaps.p, e.tcmaps.key, e.tcmaps.uw, e.tcmaps.utoff,
+                                    e.d_poi.as<int2>(), e.n, o.u, o.v, o.z, e.d_fst.as<uint8_t>()});
+            if ((int)jobs.size() == kMaxTcJobsPerLaunch || m + 1 == fast_tc.size()) {
                 TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
                                              b->d_work.as<int>() + 1, b->stream));
                 jobs.clear();
             }
         }
-        if (!jobs.empty())
-            TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
-                                         b->d_work.as<int>() + 1, b->stream));
     }
-    // target tables, then persistent IC-GN launches over the fast frames
+    // float LUTs (the LUT samplers and the plain path), one launch per frame
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
-        if (e.prm.path == TWDIC_PATH_FAST)
-            TW_TRY(prepare_target_for(e, batch_sampler(b->tune, e)));
-        else
+        if (e.prm.path == TWDIC_PATH_FAST) {
+            const int sampler = batch_sampler(b->tune, e);
+            if (sampler == kSampLut) TW_TRY(prepare_target_for(e, sampler));
+        } else {
             TW_TRY(e.prepare_target());
+        }
     }
     // one launch per residency level and sampler (and per kMaxJobs frames): a
     // launch sizes shared memory for its largest subset, so frames whose
@@ -1273,7 +1326,7 @@ int twdic_batch_create(twdic_batch** out) {
     TW_CUDA(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
     b->stream = b->own_stream;
     TW_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
-    TW_TRY(b->d_work.ensure(sizeof(int) * 4));
+    TW_TRY(b->d_work.ensure(sizeof(int) * (2 + kMaxTcSegsScratch)));
     TW_TRY(b->d_err.ensure(sizeof(unsigned)));
     TW_CUDA(cudaMemset(b->d_err.p, 0, sizeof(unsigned)));
     b->tune.threads = 1024;

@@ -29,10 +29,10 @@ struct IcgnTune {
     int unroll = 8;  // sample-loop unrolling of the one-POI-per-warp kernel (2, 4 or 8)
 };
 
-// Image pairs (jobs) of one batched launch: each job has its own geometry,
-// images, POI set, reference cache and outputs.  The table is a kernel
-// parameter (__grid_constant__).
-constexpr int kMaxJobs = 32;
+// Image pairs (jobs) of one batched IC-GN launch: each job has its own
+// geometry, images, POI set, reference cache and outputs.  The table is a
+// kernel parameter (__grid_constant__, at most 32 KB).
+constexpr int kMaxJobs = 128;
 
 struct IcgnJob {
     Geom g;
@@ -57,6 +57,7 @@ struct IcgnJobs {
     int total = 0;  // POIs of all jobs
     IcgnJob job[kMaxJobs];
 };
+static_assert(sizeof(IcgnJobs) < 32000, "IC-GN job table exceeds the kernel parameter limit");
 
 // Launch shape of the tensor-core FFT-CC kernel.
 struct FftccTune {
@@ -79,6 +80,28 @@ cudaError_t launch_bspline_lut(const Geom& g, const uint8_t* tar, float4* lut, c
 // full: the last ROI row and column too, bytes outside the image zero (the
 // B-spline sampler), otherwise those entries are zero (the bicubic samplers)
 cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st, bool full = false);
+// One frame of a batch's preparation launch (kernels_icgn_fast.cu): its
+// neighbourhood table (table null: none) and the output arrays set to zero
+// (null: left alone), n entries each.
+struct PrepJob {
+    Geom g;
+    const uint8_t* tar;
+    uint4* table;
+    int full;            // the B-spline form of the table
+    float* zero_f[3];    // u, v, zncc
+    int* zero_i;         // iteration counters
+    int n;
+    long long px_begin;  // first table item of the frame
+    long long z_begin;   // first zeroing item of the frame
+};
+constexpr int kMaxPrepJobs = 128;
+struct PrepJobs {
+    int njobs = 0;
+    long long px_total = 0, z_total = 0;
+    PrepJob job[kMaxPrepJobs];
+};
+static_assert(sizeof(PrepJobs) < 32000, "preparation table exceeds the kernel parameter limit");
+cudaError_t launch_batch_prepare(const PrepJobs& jobs, cudaStream_t st);
 cudaError_t launch_icgn_plain(const Geom& g, const uint8_t* tar, const int2* poi, int n, const float* subR,
                               const float2* sd, const float* chol, const float* refnorm, const uint8_t* rflag,
                               const float4* lut, float* u, float* v, float* p6, int* iters, uint8_t* flags,
@@ -107,15 +130,34 @@ int icgn_fast_residency(const Geom& g, const IcgnTune& tune);
 cudaError_t launch_icgn_fast_jobs(const IcgnJobs& jobs, int* work, const IcgnTune& tune, cudaStream_t st);
 
 // ---- tensor-core FFT-CC (kernels_fftcc_tc.cu)
-// err: error flags; work: one int of scratch (the batch counter, zeroed by the launcher)
-cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
+// The TMA descriptors of an image pair live in device memory (kTcMapsBytes,
+// 128-byte aligned), kept by the frame handle that owns the images: encoded on
+// the host by fftcc_tc_encode_maps for a launch shape (window size and
+// tuning; the key tells when a re-encoding is due) and copied by the caller.
+constexpr size_t kTcMapsBytes = 512;
+struct TcMapInfo {
+    uint64_t key;  // fftcc_tc_maps_key of the shape encoded for
+    int uw;        // width of the one-row boxes (0: not used)
+    int utoff;     // offset of the target's one-row box in a group's window region
+};
+uint64_t fftcc_tc_maps_key(const Geom& g, const FftccTune& tune);
+bool fftcc_tc_encode_maps(const Geom& g, const uint8_t* ref, const uint8_t* tar, const FftccTune& tune,
+                          void* host_buf, TcMapInfo* info);
+// err: error flags; work: scratch -- one int (one window size) or kMaxTcSegsScratch
+// ints (several), zeroed by the launcher
+cudaError_t launch_fftcc_tc(const Geom& g, const void* maps, uint64_t map_key, int uw, int utoff, const int2* poi,
+                            int n, float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
                             const FftccTune& tune, cudaStream_t st);
-// One image pair of a batched tensor-core FFT-CC launch (all jobs share rx = ry).
+// One image pair of a batched tensor-core FFT-CC launch.  Jobs of one window
+// size share one k_fftcc_tc launch; jobs of several window sizes (up to 32)
+// share one k_fftcc_tc_seg launch.
+constexpr int kMaxTcJobsPerLaunch = 128;
+constexpr int kMaxTcSegsScratch = 32;
 struct FftccJob {
     Geom g;
-    const uint8_t* ref;
-    const uint8_t* tar;
+    const void* maps;  // device TMA descriptors (fftcc_tc_encode_maps)
+    uint64_t map_key;
+    int uw, utoff;
     const int2* poi;
     int n;
     float* u;

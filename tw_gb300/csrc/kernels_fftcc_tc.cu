@@ -33,7 +33,9 @@
 #include <memory>
 #include <mutex>
 #include <map>
+#include <algorithm>
 #include <cstring>
+#include <new>
 #include <vector>
 
 #include "dic_common.cuh"
@@ -58,6 +60,15 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
 
+// The tensor maps of one image pair: boxes [N rows][BW bytes] of one window
+// and [N rows][uw bytes] holding the windows of a batch whose POIs lie on one
+// POI row.
+struct alignas(128) TcMaps {
+    CUtensorMap ref, tar, ref_u, tar_u;
+};
+constexpr int kMaxTcJobs = kMaxTcJobsPerLaunch;  // image pairs per launch
+constexpr int kMaxTcSegs = kMaxTcSegsScratch;    // window sizes per launch (N = 8 .. 64, even)
+
 struct TcShape {
     int N, H, HP, NP, PB, tiles1, K4, BW, WS, groups;
     int NW4;  // 32-bit words per window row in the exact re-evaluation
@@ -72,18 +83,13 @@ struct TcShape {
     int smem_bytes;
 };
 
-// Epilogue-4 scratch, placed in the A1/A3 region once stage 3 has read A3.
-// One image pair (job) of a launch.  All jobs of a launch share the window
-// size N; each has its own images (tensor maps), POIs and outputs.
+// One image pair (job) of a launch: its images (TMA tensor maps in device
+// memory, kept by the frame handle), POIs and outputs.  A launch's jobs are
+// ordered by window size; a segment is a run of jobs of one window size.
 struct TcJob {
-    CUtensorMap map_ref;  // 64-byte aligned
-    CUtensorMap map_tar;
-    // boxes [N rows][uw bytes] holding the windows of a whole batch when its
-    // POIs lie on one POI row (uw = 0: not used for this job)
-    CUtensorMap map_ref_u;
-    CUtensorMap map_tar_u;
-    int uw;
-    int utoff;  // offset of the target box in the window region (128-byte aligned)
+    const TcMaps* maps;  // device copy of the job's tensor maps
+    int uw;              // width of the one-row boxes (0: not used for this job)
+    int utoff;           // offset of the target box in the window region (128-byte aligned)
     Geom g;
     const int2* poi;
     float* u;
@@ -91,15 +97,29 @@ struct TcJob {
     float* zncc;
     uint8_t* status;
     int n;            // POIs of the job
-    int batch_begin;  // first global batch index of the job
+    int batch_begin;  // first batch index of the job within its segment
 };
 struct TcJobs {
     int njobs;
-    int nbatch;  // batches of all jobs
-    TcJob job[kMaxJobs];
+    int nbatch;  // batches of all jobs (one window size) or of the first segment
+    TcJob job[kMaxTcJobs];
 };
+// A segment of a mixed-size launch: its shape, twiddle tables and jobs
+// [job_lo, job_hi); CTAs [cta_begin, next segment's cta_begin) start on it.
+struct TcSeg {
+    TcShape s;
+    const uint4* tables;
+    int job_lo, job_hi;
+    int nbatch;
+    int shape;  // index of (NP, HP) in kTcShapes
+    int cta_begin;
+};
+struct TcSegs {
+    int nseg;
+    TcSeg seg[kMaxTcSegs];
+};
+static_assert(sizeof(TcJobs) + sizeof(TcSegs) + 64 < 32000, "kernel parameters exceed the 32 KB limit");
 
-// Candidates of one pass: (POI << 16 | shift index) and exact sums.
 struct PeakScratch {
     int cand[kCandChunk];
     int candS[kCandChunk];
@@ -212,32 +232,68 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 __device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast<__half*>(p) = __float2half_rn(v); }
 
 // ----------------------------------------------------------------- kernel --
-// blockDim = 128 * s.groups (up to four).  Each 128-thread group runs its
-// own batches (own operand region, TMEM columns, mbarriers and named barrier)
-// and the groups share the twiddle tables, so one group's load and MMA
-// latency overlaps other groups' epilogues.  A group's GEMM operands A1, A2,
-// A3, A4 and its peak scratch share one region: each is written only after
-// the MMA that reads the previous one has completed.
-template <int NP, int HP, bool MULTI, bool LO>
-__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
-                                                                 const uint4* __restrict__ tables, unsigned* err,
-                                                                 int* work) {
-    extern __shared__ __align__(1024) uint8_t sm[];
-    __shared__ __align__(8) uint64_t mbar_mma[kMaxGroups];
-    __shared__ __align__(8) uint64_t mbar_tma[kMaxGroups];
-    __shared__ uint32_t tmem_slot;
-    __shared__ int wsum[kMaxGroups][2 * kMaxPB][2];
-    __shared__ float sscale[kMaxGroups][kMaxPB];
-    __shared__ int sdark[kMaxGroups][kMaxPB];
-    __shared__ int cbase[kMaxGroups][kMaxPB];      // first candidate slot of each POI
-    __shared__ int cend[kMaxGroups][kMaxPB];       // one past its last
-    __shared__ int wtot[kMaxGroups][4];            // candidates per warp
-    __shared__ uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
-    __shared__ int2 spoi[kMaxGroups][kMaxPB];
-    __shared__ int wbase[kMaxGroups][2 * kMaxPB];  // byte offset of each window's (0, 0) in wwin
-    __shared__ int wrs[kMaxGroups];                // row stride of the windows in wwin
-    __shared__ int snext[kMaxGroups];
+// Each 128-thread group of a CTA runs its own batches (own operand region,
+// TMEM columns, mbarriers and named barrier) and the groups share the twiddle
+// tables, so one group's load and MMA latency overlaps other groups'
+// epilogues.  A group's GEMM operands A1, A2, A3, A4 and its peak scratch
+// share one region: each is written only after the MMA that reads the
+// previous one has completed.
 
+// Shared state of a CTA's groups (static shared memory).
+struct TcCta {
+    uint64_t mbar_mma[kMaxGroups];
+    uint64_t mbar_tma[kMaxGroups];
+    uint32_t tmem_slot;
+    int seg;
+    int wsum[kMaxGroups][2 * kMaxPB][2];
+    float sscale[kMaxGroups][kMaxPB];
+    int sdark[kMaxGroups][kMaxPB];
+    int cbase[kMaxGroups][kMaxPB];      // first candidate slot of each POI
+    int cend[kMaxGroups][kMaxPB];       // one past its last
+    int wtot[kMaxGroups][4];            // candidates per warp
+    uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
+    int2 spoi[kMaxGroups][kMaxPB];
+    int wbase[kMaxGroups][2 * kMaxPB];  // byte offset of each window's (0, 0) in wwin
+    int wrs[kMaxGroups];                // row stride of the windows in wwin
+    int snext[kMaxGroups];
+};
+
+// The tensor maps of jobs [lo, hi): visible to the tensor-map proxy (they
+// were written to device memory by copies) and prefetched.  Thread 0 of each
+// group issues the group's TMA copies, so each such thread fences.
+__device__ __forceinline__ void tc_acquire_maps(const TcJobs& J, int lo, int hi) {
+    for (int j = lo; j < hi; ++j) {
+        const TcMaps* m = J.job[j].maps;
+        const CUtensorMap* mm[4] = {&m->ref, &m->tar, &m->ref_u, &m->tar_u};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                             reinterpret_cast<uint64_t>(mm[k]))
+                         : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(mm[k])) : "memory");
+        }
+    }
+}
+
+// The twiddle tables of one window size into the start of shared memory
+// (every thread of the CTA takes part; the caller synchronises).
+__device__ __forceinline__ void tc_load_tables(uint8_t* sm, const uint4* __restrict__ tables, int bytes) {
+    uint4* dst = reinterpret_cast<uint4*>(sm);
+    for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) dst[i] = tables[i];
+    fence_async_smem();
+}
+
+// The batches of one group over jobs [job_lo, job_hi) of J, which share the
+// window size of shape s: batch indices [first, nbatch) -- the group's first
+// batch, then the next free one from `counter` plus `counter_base`, taken by
+// thread 0 at the start of a batch so that the atomic's latency is hidden.
+// phase / tphase: the parities of the group's MMA and TMA mbarriers, carried
+// across calls.  Returns false after a bounded wait gave up (err set).
+template <int NP, int HP, bool MULTI, bool LO>
+__device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape& s, int job_lo, int job_hi,
+                                                 int nbatch, int first, int* counter, int counter_base,
+                                                 unsigned* err, TcCta& cs, uint8_t* sm, uint32_t& phase,
+                                                 uint32_t& tphase) {
     const int grp = threadIdx.x >> 7;
     const int t = threadIdx.x & 127, warp = t >> 5, lane = t & 31;
     const int bar_id = 1 + grp;
@@ -247,70 +303,30 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     uint8_t* gbase = sm + s.tab_bytes + grp * s.group_bytes;
     uint8_t* wwin = gbase + s.off_win;  // [2 PB] TMA boxes of N rows x BW bytes, stride WS
     PeakScratch* ps = reinterpret_cast<PeakScratch*>(gbase + s.off_a13);
-    uint64_t* mbar = &mbar_mma[grp];
-    uint64_t* tbar = &mbar_tma[grp];
-
-    // ---- set-up: TMEM (128 columns per group), mbarriers, tables
-    const uint32_t tmem_cols = s.groups == 1 ? 128u : (s.groups == 2 ? 256u : 512u);
-    if (threadIdx.x < 32) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(tmem_cols));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < s.groups; ++k) {
-            mbar_init(&mbar_mma[k]);
-            mbar_init(&mbar_tma[k]);
-        }
-        for (int j = 0; j < J.njobs; ++j) {
-            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&J.job[j].map_ref)) : "memory");
-            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&J.job[j].map_tar)) : "memory");
-        }
-    }
-    {
-        uint4* dst = reinterpret_cast<uint4*>(sm);
-        for (int i = threadIdx.x; i < s.tab_bytes / 16; i += blockDim.x) dst[i] = tables[i];
-    }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    // TMA destinations need 128-byte alignment of the dynamic shared memory
-    if (smem_u32(sm) & 127u) {
-        if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
-        if (threadIdx.x < 32)
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
-                         "r"(tmem_cols));
-        return;
-    }
-    const uint32_t tm = tmem_slot + grp * kTmemCols;
+    uint64_t* mbar = &cs.mbar_mma[grp];
+    uint64_t* tbar = &cs.mbar_tma[grp];
+    const uint32_t tm = cs.tmem_slot + grp * kTmemCols;
     const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
     const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
-    uint32_t phase = 0, tphase = 0;
-
-    // batches: the first of every group by position, then the next free one
-    // from a launch-wide counter (taken by thread 0 at the start of a batch,
-    // so the atomic's latency is hidden by the batch), which evens out the
-    // groups' finishing times
     int nxt = 0;
-    for (int batch = blockIdx.x * s.groups + grp; batch < J.nbatch; batch = snext[grp]) {
-        if (t == 0) nxt = gridDim.x * s.groups + atomicAdd(work, 1);
+    for (int batch = first; batch < nbatch; batch = cs.snext[grp]) {
+        if (t == 0) nxt = counter_base + atomicAdd(counter, 1);
         // the job (image pair, POI set) of this batch: batches of job j are
         // [batch_begin_j, batch_begin_j + ceil(n_j / PB))
-        int jj = 0;
+        int jj = job_lo;
         if (MULTI) {
-            while (jj + 1 < J.njobs && batch >= J.job[jj + 1].batch_begin) ++jj;
+            while (jj + 1 < job_hi && batch >= J.job[jj + 1].batch_begin) ++jj;
         }
         const TcJob& jb = J.job[jj];
         const Geom& g = jb.g;
         const int2* __restrict__ poi = jb.poi;
         const int n_job = jb.n;
         const int b0 = (batch - jb.batch_begin) * PB;
-        if (t < 2 * kMaxPB * 2) (&wsum[grp][0][0])[t] = 0;
+        if (t < 2 * kMaxPB * 2) (&cs.wsum[grp][0][0])[t] = 0;
         if (t < PB) {
-            spoi[grp][t] = (b0 + t < n_job) ? poi[b0 + t] : make_int2(-1, -1);
-            smaxv[grp][t] = 0u;
+            cs.spoi[grp][t] = (b0 + t < n_job) ? poi[b0 + t] : make_int2(-1, -1);
+            cs.smaxv[grp][t] = 0u;
         }
         group_sync(bar_id);
 
@@ -322,7 +338,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             fence_async_smem();  // the previous batch's generic reads of the windows come first
             int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
             for (int p = 0; p < PB; ++p) {
-                const int2 pyx = spoi[grp][p];
+                const int2 pyx = cs.spoi[grp][p];
                 if (pyx.x < 0) continue;
                 ymin = min(ymin, pyx.x); ymax = max(ymax, pyx.x);
                 xmin = min(xmin, pyx.y); xmax = max(xmax, pyx.y);
@@ -332,42 +348,42 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             if (uni) {
                 const int y0 = ymin - g.ry;
                 mbar_expect_tx(tbar, (uint32_t)(2 * N * jb.uw));
-                tma_load_2d(wwin, &jb.map_ref_u, xau, y0, tbar);
-                tma_load_2d(wwin + jb.utoff, &jb.map_tar_u, xau, y0, tbar);
-                wrs[grp] = jb.uw;
+                tma_load_2d(wwin, &jb.maps->ref_u, xau, y0, tbar);
+                tma_load_2d(wwin + jb.utoff, &jb.maps->tar_u, xau, y0, tbar);
+                cs.wrs[grp] = jb.uw;
                 for (int p = 0; p < PB; ++p) {
-                    const int2 pyx = spoi[grp][p];
+                    const int2 pyx = cs.spoi[grp][p];
                     const int xo = pyx.x < 0 ? 0 : pyx.y - g.rx - xau;
-                    wbase[grp][2 * p] = xo;
-                    wbase[grp][2 * p + 1] = jb.utoff + xo;
+                    cs.wbase[grp][2 * p] = xo;
+                    cs.wbase[grp][2 * p + 1] = jb.utoff + xo;
                 }
             } else {
                 int nload = 0;
-                for (int wi = 0; wi < 2 * PB; ++wi) nload += spoi[grp][wi >> 1].x >= 0;
+                for (int wi = 0; wi < 2 * PB; ++wi) nload += cs.spoi[grp][wi >> 1].x >= 0;
                 mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
-                wrs[grp] = BW;
+                cs.wrs[grp] = BW;
                 for (int wi = 0; wi < 2 * PB; ++wi) {
-                    const int2 pyx = spoi[grp][wi >> 1];
-                    wbase[grp][wi] = wi * WS;  // read (harmlessly) by the row copies for absent POIs
+                    const int2 pyx = cs.spoi[grp][wi >> 1];
+                    cs.wbase[grp][wi] = wi * WS;  // read (harmlessly) by the row copies for absent POIs
                     if (pyx.x < 0) continue;
                     const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
                     const int xa = x0 & ~15;
-                    wbase[grp][wi] = wi * WS + x0 - xa;
-                    tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.map_tar : &jb.map_ref, xa, y0, tbar);
+                    cs.wbase[grp][wi] = wi * WS + x0 - xa;
+                    tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.maps->tar : &jb.maps->ref, xa, y0, tbar);
                 }
             }
         }
         bool ok = mbar_wait(tbar, tphase);
         tphase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
 
         // ---- phase L2: windows -> A1 (rows (window, x), K = y), exact FP16;
         // integer sums per window by segmented warp reductions
         for (int rr = t; rr < s.tiles1 * 128; rr += 128) {
             const int wi = rr / N, x = rr - wi * N;
-            const bool data = wi < 2 * PB && spoi[grp][wi >> 1].x >= 0;
-            const int rs = wrs[grp];
-            const uint8_t* col = wwin + (data ? wbase[grp][wi] : 0) + x;
+            const bool data = wi < 2 * PB && cs.spoi[grp][wi >> 1].x >= 0;
+            const int rs = cs.wrs[grp];
+            const uint8_t* col = wwin + (data ? cs.wbase[grp][wi] : 0) + x;
             uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
             const int row = rr & 127;
             int su = 0, sq = 0;
@@ -390,8 +406,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             const unsigned seg = __match_any_sync(kFull, key);
             const int gs = __reduce_add_sync(seg, su), gq = __reduce_add_sync(seg, sq);
             if (data && lane == __ffs(seg) - 1) {
-                atomicAdd(&wsum[grp][wi][0], gs);
-                atomicAdd(&wsum[grp][wi][1], gq);
+                atomicAdd(&cs.wsum[grp][wi][0], gs);
+                atomicAdd(&cs.wsum[grp][wi][1], gq);
             }
         }
         fence_async_smem();
@@ -416,15 +432,15 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         // nf = sum (f - mean)^2 = (n sum f^2 - (sum f)^2) / n, exact in integers
         if (t < PB) {
             const int wf = 2 * t, wg = 2 * t + 1;
-            const long long numf = (long long)n2 * wsum[grp][wf][1] - (long long)wsum[grp][wf][0] * wsum[grp][wf][0];
-            const long long numg = (long long)n2 * wsum[grp][wg][1] - (long long)wsum[grp][wg][0] * wsum[grp][wg][0];
+            const long long numf = (long long)n2 * cs.wsum[grp][wf][1] - (long long)cs.wsum[grp][wf][0] * cs.wsum[grp][wf][0];
+            const long long numg = (long long)n2 * cs.wsum[grp][wg][1] - (long long)cs.wsum[grp][wg][0] * cs.wsum[grp][wg][0];
             const bool dark = b0 + t >= n_job || numf == 0 || numg == 0;
-            sdark[grp][t] = dark ? 1 : 0;
-            sscale[grp][t] = dark ? 0.f : (float)n2 * rsqrtf((float)numf) * rsqrtf((float)numg);
+            cs.sdark[grp][t] = dark ? 1 : 0;
+            cs.sscale[grp][t] = dark ? 0.f : (float)n2 * rsqrtf((float)numf) * rsqrtf((float)numg);
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
         // ---- epilogue 1: Y -> A2 (rows (p, ky, w); K = (part, x) with split
@@ -524,7 +540,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
         // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
@@ -533,7 +549,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             const int p = rowv ? t / (2 * H) : 0;
             const int ky = rowv ? (t >> 1) % H : 0;
             const int wsel = t & 1;
-            const float sc = rowv ? sscale[grp][p] : 0.f;
+            const float sc = rowv ? cs.sscale[grp][p] : 0.f;
             const int r3 = p * H + ky;
             uint8_t* a3 = gbase + s.off_a13;
             constexpr int HALF = NP / 2;
@@ -627,7 +643,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
         // ---- epilogue 3: Z -> A4 (rows (p, x), K = (ky, part) interleaved:
@@ -689,7 +705,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); break; }
+        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
@@ -697,7 +713,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         // reading; the surface stays in TMEM and is read twice in chunks)
         const bool rowv = t < PB * N;
         const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
-        const bool live = rowv && !sdark[grp][p4];
+        const bool live = rowv && !cs.sdark[grp][p4];
         if (t < kCandChunk) ps->candS[t] = 0;
         // approximate peak value per POI: each thread's maximum over the
         // surface rows y of its column x4, then a segmented warp reduction and
@@ -715,7 +731,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         }
         const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
         const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
-        if (live && lane == __ffs(seg) - 1) atomicMax(&smaxv[grp][p4], ov);
+        if (live && lane == __ffs(seg) - 1) atomicMax(&cs.smaxv[grp][p4], ov);
         group_sync(bar_id);
         // candidates: every shift within kCandZncc (ZNCC units; the surface is
         // N^2 ZNCC) of the approximate peak, the peak itself included, as one
@@ -723,7 +739,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
         // column skips the second read
         uint64_t cmask = 0;
         {
-            const float th = live ? f32_unord(smaxv[grp][p4]) - kCandZncc * (float)n2 : 3.4e38f;
+            const float th = live ? f32_unord(cs.smaxv[grp][p4]) - kCandZncc * (float)n2 : 3.4e38f;
             if (__any_sync(kFull, live && bv >= th)) {
 #pragma unroll
                 for (int y0 = 0; y0 < NP; y0 += 8) {
@@ -748,18 +764,18 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             const int up = __shfl_up_sync(kFull, incl, o);
             if (lane >= o) incl += up;
         }
-        if (lane == 31) wtot[grp][warp] = incl;
+        if (lane == 31) cs.wtot[grp][warp] = incl;
         group_sync(bar_id);
         int wpre = 0, total = 0;
 #pragma unroll
         for (int w = 0; w < 4; ++w) {
-            const int tw = wtot[grp][w];
+            const int tw = cs.wtot[grp][w];
             wpre += (w < warp) ? tw : 0;
             total += tw;
         }
         const int excl = wpre + incl - cnt;
-        if (rowv && x4 == 0) cbase[grp][p4] = excl;
-        if (rowv && x4 == N - 1) cend[grp][p4] = excl + cnt;
+        if (rowv && x4 == 0) cs.cbase[grp][p4] = excl;
+        if (rowv && x4 == N - 1) cs.cend[grp][p4] = excl + cnt;
         // exact integer correlation of every candidate, kCandChunk slots at a
         // time (any number of candidates: a broad or periodic surface only
         // takes more chunks), read from the staged windows: tasks (slot, row)
@@ -789,7 +805,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 const int NW4 = s.NW4;
                 const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
                 const int rot = lane % NW4;
-                const int rs = wrs[grp];
+                const int rs = cs.wrs[grp];
                 for (int task = t; task < nc * N; task += 128) {
                     const int c = task / N, y = task - c * N;
                     const int code = ps->cand[c];
@@ -797,8 +813,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                     const int ky = idx / N, kx = idx - ky * N;
                     int yy = y + ky;
                     if (yy >= N) yy -= N;
-                    const uint8_t* fb = wwin + wbase[grp][2 * p] + y * rs;
-                    const uint8_t* gb = wwin + wbase[grp][2 * p + 1] + yy * rs;
+                    const uint8_t* fb = wwin + cs.wbase[grp][2 * p] + y * rs;
+                    const uint8_t* gb = wwin + cs.wbase[grp][2 * p + 1] + yy * rs;
                     const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
                     unsigned acc = 0;
                     int j = rot;
@@ -820,8 +836,8 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 }
             }
             group_sync(bar_id);
-            if (t < PB && !sdark[grp][t]) {
-                const int a = max(cbase[grp][t], lo), b = min(cend[grp][t], lo + kCandChunk);
+            if (t < PB && !cs.sdark[grp][t]) {
+                const int a = max(cs.cbase[grp][t], lo), b = min(cs.cend[grp][t], lo + kCandChunk);
                 for (int k = a; k < b; ++k) {
                     const int sc = ps->candS[k - lo], id = ps->cand[k - lo] & 0xffff;
                     if (sc > best_s || (sc == best_s && id < best_i)) {
@@ -837,15 +853,15 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
             float* v = jb.v;
             float* zncc = jb.zncc;
             uint8_t* status = jb.status;
-            if (sdark[grp][t]) {
+            if (cs.sdark[grp][t]) {
                 status[gp] = 1;  // dark subset: outputs untouched (TW_paDIC_FFTCC2D_CPU.cpp:272-275)
             } else {
                 int iu = best_i % N, iv = best_i / N;
                 if (iu > g.rx) iu -= N;
                 if (iv > g.ry) iv -= N;
-                const long long sf = wsum[grp][2 * t][0], sg = wsum[grp][2 * t + 1][0];
-                const long long numf = (long long)n2 * wsum[grp][2 * t][1] - sf * sf;
-                const long long numg = (long long)n2 * wsum[grp][2 * t + 1][1] - sg * sg;
+                const long long sf = cs.wsum[grp][2 * t][0], sg = cs.wsum[grp][2 * t + 1][0];
+                const long long numf = (long long)n2 * cs.wsum[grp][2 * t][1] - sf * sf;
+                const long long numg = (long long)n2 * cs.wsum[grp][2 * t + 1][1] - sg * sg;
                 // exact integer numerator and norms; the quotient in FP32
                 // (relative error below 5e-7: GB300's FP64 divide and square
                 // root are slow)
@@ -856,17 +872,146 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
                 status[gp] = 0;
             }
         }
-        if (t == 0) snext[grp] = nxt;
+        if (t == 0) cs.snext[grp] = nxt;
         group_sync(bar_id);
     }
+    return true;
+}
 
-    // ---- teardown
+// TMEM columns and mbarriers of the CTA's groups; false (err set, TMEM
+// freed) when the dynamic shared memory is not 128-byte aligned, which the
+// TMA destinations need.  Ends with a CTA barrier.
+__device__ __forceinline__ bool tc_setup(TcCta& cs, uint8_t* sm, int groups, uint32_t tmem_cols, unsigned* err) {
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&cs.tmem_slot)),
+                     "r"(tmem_cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < groups; ++k) {
+            mbar_init(&cs.mbar_mma[k]);
+            mbar_init(&cs.mbar_tma[k]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (smem_u32(sm) & 127u) {
+        if (threadIdx.x == 0) atomicOr(err, kErrTimeout);
+        if (threadIdx.x < 32)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cs.tmem_slot),
+                         "r"(tmem_cols));
+        return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void tc_teardown(TcCta& cs, uint32_t tmem_cols) {
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (threadIdx.x < 32)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot),
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(cs.tmem_slot),
                      "r"(tmem_cols));
+}
+
+// One window size: blockDim = 128 * s.groups (up to four).  The first batch
+// of every group by position, then the next free one from the launch-wide
+// counter, which evens out the groups' finishing times.
+template <int NP, int HP, bool MULTI, bool LO>
+__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
+                                                                 const uint4* __restrict__ tables, unsigned* err,
+                                                                 int* work) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ TcCta cs;
+    const int grp = threadIdx.x >> 7;
+    const uint32_t tmem_cols = s.groups == 1 ? 128u : (s.groups == 2 ? 256u : 512u);
+    tc_load_tables(sm, tables, s.tab_bytes);
+    if ((threadIdx.x & 127) == 0) tc_acquire_maps(J, 0, J.njobs);
+    if (!tc_setup(cs, sm, s.groups, tmem_cols, err)) return;
+    uint32_t phase = 0, tphase = 0;
+    tc_group_batches<NP, HP, MULTI, LO>(J, s, 0, J.njobs, J.nbatch, blockIdx.x * s.groups + grp, work,
+                                        gridDim.x * s.groups, err, cs, sm, phase, tphase);
+    tc_teardown(cs, tmem_cols);
+}
+
+// The (NP, HP) instantiations of the body: NP = window size rounded up to
+// 16, HP = N / 2 + 1 rounded up to 8.
+constexpr int kTcShapes[8][2] = {{16, 8}, {16, 16}, {32, 16}, {32, 24}, {48, 24}, {48, 32}, {64, 32}, {64, 40}};
+
+template <bool LO>
+__device__ __forceinline__ bool tc_run_segment(const TcJobs& J, const TcSeg& sg, int* counter, unsigned* err,
+                                               TcCta& cs, uint8_t* sm, uint32_t& phase, uint32_t& tphase) {
+    const int grp = threadIdx.x >> 7;
+    if (grp >= sg.s.groups) return true;  // this segment's shared memory holds fewer groups
+    // every batch, the first included, from the segment's counter
+    if ((threadIdx.x & 127) == 0) cs.snext[grp] = atomicAdd(counter, 1);
+    group_sync(1 + grp);
+    const int first = cs.snext[grp];
+#define TWDIC_TC_SEG(K)                                                                                     \
+    case K:                                                                                                  \
+        return tc_group_batches<kTcShapes[K][0], kTcShapes[K][1], true, LO>(J, sg.s, sg.job_lo, sg.job_hi,   \
+                                                                            sg.nbatch, first, counter, 0,    \
+                                                                            err, cs, sm, phase, tphase);
+    switch (sg.shape) {
+        TWDIC_TC_SEG(0)
+        TWDIC_TC_SEG(1)
+        TWDIC_TC_SEG(2)
+        TWDIC_TC_SEG(3)
+        TWDIC_TC_SEG(4)
+        TWDIC_TC_SEG(5)
+        TWDIC_TC_SEG(6)
+        TWDIC_TC_SEG(7)
+        default:
+            return true;
+    }
+#undef TWDIC_TC_SEG
+}
+
+// Several window sizes in one persistent launch (blockDim = 512, four groups
+// at most): jobs grouped into segments by window size.  A CTA starts on the
+// segment its index falls in (CTAs are spread over segments in proportion to
+// their work), loads that window size's twiddle tables, and its groups take
+// the segment's batches from the segment's counter; when they run out, the
+// CTA moves to the next segment with batches left, until none has.
+template <bool LO>
+__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc_seg(const __grid_constant__ TcJobs J,
+                                                                     const __grid_constant__ TcSegs S,
+                                                                     unsigned* err, int* counters) {
+    extern __shared__ __align__(1024) uint8_t sm[];
+    __shared__ TcCta cs;
+    constexpr uint32_t tmem_cols = 512u;
+    if (!tc_setup(cs, sm, kMaxGroups, tmem_cols, err)) return;
+    if ((threadIdx.x & 127) == 0) tc_acquire_maps(J, 0, J.njobs);
+    int seg = 0;
+    while (seg + 1 < S.nseg && (int)blockIdx.x >= S.seg[seg + 1].cta_begin) ++seg;
+    uint32_t phase = 0, tphase = 0;
+    for (;;) {
+        const TcSeg& sg = S.seg[seg];
+        tc_load_tables(sm, sg.tables, sg.s.tab_bytes);
+        __syncthreads();
+        const bool ok = tc_run_segment<LO>(J, sg, counters + seg, err, cs, sm, phase, tphase);
+        // every group is done with this segment's tables; the next segment
+        // with batches left (the counters only grow)
+        if (threadIdx.x == 0) {
+            int next = -1;
+            for (int d = 1; ok && d <= S.nseg; ++d) {
+                const int c = (seg + d) % S.nseg;
+                if (atomicAdd(counters + c, 0) < S.seg[c].nbatch) {
+                    next = c;
+                    break;
+                }
+            }
+            cs.seg = next;
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        seg = cs.seg;
+        if (seg < 0) break;
+    }
+    tc_teardown(cs, tmem_cols);
 }
 
 // ----------------------------------------------------------- host side ----
@@ -1054,43 +1199,149 @@ bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape&
 
 }  // namespace
 
+static_assert(sizeof(TcMaps) <= kTcMapsBytes, "TcMaps larger than its buffer");
+
+uint64_t fftcc_tc_maps_key(const Geom& g, const FftccTune& tune) {
+    TcShape s;
+    if (!make_shape(g, tune, s)) return 0;
+    return 1ull | ((uint64_t)s.PB << 8) | ((uint64_t)s.N << 16) | ((uint64_t)s.BW << 24) | ((uint64_t)s.WS << 32);
+}
+
+bool fftcc_tc_encode_maps(const Geom& g, const uint8_t* ref, const uint8_t* tar, const FftccTune& tune,
+                          void* host_buf, TcMapInfo* info) {
+    TcShape s;
+    if (!make_shape(g, tune, s)) return false;
+    if ((g.pitch % 16) != 0 || (reinterpret_cast<uintptr_t>(ref) & 15) || (reinterpret_cast<uintptr_t>(tar) & 15) ||
+        (reinterpret_cast<uintptr_t>(host_buf) & 127))
+        return false;
+    TcMaps* m = new (host_buf) TcMaps();
+    if (!image_map(&m->ref, g, ref, s) || !image_map(&m->tar, g, tar, s)) return false;
+    // one box per image for a batch on one POI row: PB windows at the grid
+    // step apart, x aligned down to 16 bytes; used when both boxes (and 8
+    // bytes of read slack) fit the window region and the box width is at
+    // most 256 (the TMA box limit)
+    int uw = round_up((s.PB - 1) * g.grid_x + s.N + 15, 16);
+    int utoff = round_up(s.N * uw, 128);
+    if (s.PB < 2 || g.grid_x <= 0 || uw > 256 || utoff + s.N * uw + 16 > 2 * s.PB * s.WS ||
+        !image_map(&m->ref_u, g, ref, s, uw) || !image_map(&m->tar_u, g, tar, s, uw)) {
+        uw = 0;
+        utoff = 0;
+        m->ref_u = m->ref;  // never read
+        m->tar_u = m->tar;
+    }
+    info->key = fftcc_tc_maps_key(g, tune);
+    info->uw = uw;
+    info->utoff = utoff;
+    return true;
+}
+
+namespace {
+
+// A job of the kernels' table from a launcher job, whose maps must have been
+// encoded for this launch's shape.
+bool fill_job(TcJob& o, const FftccJob& in, const FftccTune& tune) {
+    if (!in.maps || (reinterpret_cast<uintptr_t>(in.maps) & 127) || in.map_key != fftcc_tc_maps_key(in.g, tune))
+        return false;
+    o.maps = static_cast<const TcMaps*>(in.maps);
+    o.uw = in.uw;
+    o.utoff = in.utoff;
+    o.g = in.g;
+    o.poi = in.poi;
+    o.u = in.u;
+    o.v = in.v;
+    o.zncc = in.zncc;
+    o.status = in.status;
+    o.n = in.n;
+    return true;
+}
+
+int shape_index(const TcShape& s) {
+    for (int k = 0; k < 8; ++k)
+        if (kTcShapes[k][0] == s.NP && kTcShapes[k][1] == s.HP) return k;
+    return -1;
+}
+
+// Jobs of several window sizes in one k_fftcc_tc_seg launch.  counters:
+// kMaxTcSegs ints of scratch.
+cudaError_t launch_segments(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* counters,
+                            cudaStream_t st) {
+    // jobs grouped by window size (stable)
+    std::vector<int> order(njobs);
+    for (int j = 0; j < njobs; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return jobs[a].g.rx < jobs[b].g.rx; });
+    std::unique_ptr<TcJobs> J(new TcJobs());
+    std::unique_ptr<TcSegs> S(new TcSegs());
+    J->njobs = njobs;
+    S->nseg = 0;
+    std::vector<double> work;
+    int smem = 0;
+    for (int k = 0; k < njobs; ++k) {
+        const FftccJob& in = jobs[order[k]];
+        if (S->nseg == 0 || in.g.rx != J->job[S->seg[S->nseg - 1].job_lo].g.rx) {
+            if (S->nseg == kMaxTcSegs) return cudaErrorInvalidValue;
+            TcSeg& sg = S->seg[S->nseg++];
+            if (!make_shape(in.g, tune, sg.s)) return cudaErrorNotSupported;
+            sg.shape = shape_index(sg.s);
+            if (sg.shape < 0) return cudaErrorNotSupported;
+            cudaError_t e = tables_for(sg.s, &sg.tables);
+            if (e != cudaSuccess) return e;
+            sg.job_lo = k;
+            sg.nbatch = 0;
+            smem = std::max(smem, sg.s.smem_bytes);
+            work.push_back(0.0);
+        }
+        TcSeg& sg = S->seg[S->nseg - 1];
+        if (in.g.rx != in.g.ry) return cudaErrorInvalidValue;
+        TcJob& o = J->job[k];
+        if (!fill_job(o, in, tune)) return cudaErrorInvalidValue;
+        o.batch_begin = sg.nbatch;
+        const int nb = (in.n + sg.s.PB - 1) / sg.s.PB;
+        sg.nbatch += nb;
+        sg.job_hi = k + 1;
+        work.back() += (double)nb * sg.s.N * sg.s.N;
+    }
+    J->nbatch = S->seg[0].nbatch;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // CTAs spread over the segments in proportion to their work (batches x N^2)
+    double total = 0.0;
+    for (double w : work) total += w;
+    if (total <= 0.0) return cudaSuccess;
+    double acc = 0.0;
+    for (int k = 0; k < S->nseg; ++k) {
+        S->seg[k].cta_begin = (int)(acc / total * sms + 0.5);
+        acc += work[k];
+    }
+    auto kern = tune.twiddle_lo ? k_fftcc_tc_seg<true> : k_fftcc_tc_seg<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(counters, 0, sizeof(int) * kMaxTcSegs, st);
+    if (e != cudaSuccess) return e;
+    kern<<<sms, kThreads * kMaxGroups, smem, st>>>(*J, *S, err, counters);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* work,
                                  cudaStream_t st) {
-    if (njobs < 1 || njobs > kMaxJobs) return cudaErrorInvalidValue;
+    if (njobs < 1 || njobs > kMaxTcJobs) return cudaErrorInvalidValue;
+    for (int j = 1; j < njobs; ++j)
+        if (jobs[j].g.rx != jobs[0].g.rx || jobs[j].g.ry != jobs[0].g.ry)
+            return launch_segments(jobs, njobs, tune, err, work, st);  // several window sizes
     TcShape s;
     if (!make_shape(jobs[0].g, tune, s)) return cudaErrorNotSupported;
-    // the table is large (tensor maps); build it in heap memory
     std::unique_ptr<TcJobs> J(new TcJobs());
     J->njobs = njobs;
     int nb = 0;
     for (int j = 0; j < njobs; ++j) {
-        const FftccJob& in = jobs[j];
-        const Geom& g = in.g;
-        if (g.rx != jobs[0].g.rx || g.ry != jobs[0].g.ry) return cudaErrorInvalidValue;  // one window size
-        if ((g.pitch % 16) != 0 || (reinterpret_cast<uintptr_t>(in.ref) & 15) ||
-            (reinterpret_cast<uintptr_t>(in.tar) & 15))
-            return cudaErrorNotSupported;
         TcJob& o = J->job[j];
-        if (!image_map(&o.map_ref, g, in.ref, s) || !image_map(&o.map_tar, g, in.tar, s))
-            return cudaErrorNotSupported;
-        // one box per image for a batch on one POI row: PB windows at the grid
-        // step apart, x aligned down to 16 bytes; used when both boxes (and 8
-        // bytes of read slack) fit the window region and the box width is at
-        // most 256
-        o.uw = round_up((s.PB - 1) * g.grid_x + s.N + 15, 16);
-        o.utoff = round_up(s.N * o.uw, 128);
-        if (s.PB < 2 || g.grid_x <= 0 || o.uw > 256 || o.utoff + s.N * o.uw + 16 > 2 * s.PB * s.WS ||
-            !image_map(&o.map_ref_u, g, in.ref, s, o.uw) || !image_map(&o.map_tar_u, g, in.tar, s, o.uw))
-            o.uw = 0;
-        o.g = g;
-        o.poi = in.poi;
-        o.u = in.u;
-        o.v = in.v;
-        o.zncc = in.zncc;
-        o.status = in.status;
-        o.n = in.n;
+        if (!fill_job(o, jobs[j], tune)) return cudaErrorInvalidValue;
         o.batch_begin = nb;
-        nb += (in.n + s.PB - 1) / s.PB;
+        nb += (jobs[j].n + s.PB - 1) / s.PB;
     }
     J->nbatch = nb;
     if (nb == 0) return cudaSuccess;
@@ -1139,11 +1390,11 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     return cudaGetLastError();
 }
 
-cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
-                            float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
+cudaError_t launch_fftcc_tc(const Geom& g, const void* maps, uint64_t map_key, int uw, int utoff, const int2* poi,
+                            int n, float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
                             const FftccTune& tune, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    FftccJob job{g, ref, tar, poi, n, u, v, zncc, status};
+    FftccJob job{g, maps, map_key, uw, utoff, poi, n, u, v, zncc, status};
     return launch_fftcc_tc_jobs(&job, 1, tune, err, work, st);
 }
 

@@ -254,10 +254,7 @@ __global__ void __launch_bounds__(kFactorThreads) k_ref_factor(int n, double* hi
 // pixels stays inside the image.  B-spline (full = 1): every ROI pixel, with
 // the bytes outside the image zero, as the reference's B-spline LUT reads
 // them (TW_utils.cpp:521-602).
-__global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __restrict__ table, int full) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.rh || j >= g.rw) return;
+__device__ __forceinline__ uint4 nbhd_entry(const Geom& g, const uint8_t* __restrict__ tar, int i, int j, int full) {
     uint4 q = make_uint4(0u, 0u, 0u, 0u);
     const int y0 = i + g.sy - 1, x0 = j + g.sx - 1;
     if (!full && (i == g.rh - 1 || j == g.rw - 1)) {
@@ -287,7 +284,44 @@ __global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __r
         }
         q = make_uint4(w[0], w[1], w[2], w[3]);
     }
-    table[(size_t)i * g.rw + j] = q;
+    return q;
+}
+
+__global__ void k_nbhd_table(Geom g, const uint8_t* __restrict__ tar, uint4* __restrict__ table, int full) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.rh || j >= g.rw) return;
+    table[(size_t)i * g.rw + j] = nbhd_entry(g, tar, i, j, full);
+}
+
+// The per-frame preparation of a batch in one launch: the neighbourhood
+// tables of every frame that has one, then the zeroing of every frame's
+// output arrays that start at zero.  Items are numbered over all frames
+// (table pixels first, row-major per frame, then one item per POI); each
+// thread finds its frame by binary search over the frames' first items.
+__global__ void k_batch_prepare(const __grid_constant__ PrepJobs J) {
+    const long long total = J.px_total + J.z_total;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const bool px = k < J.px_total;
+        const long long item = px ? k : k - J.px_total;
+        int lo = 0, hi = J.njobs - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((px ? J.job[mid].px_begin : J.job[mid].z_begin) <= item) lo = mid; else hi = mid - 1;
+        }
+        const PrepJob& jb = J.job[lo];
+        if (px) {
+            const long long o = item - jb.px_begin;
+            const int i = (int)(o / jb.g.rw), j = (int)(o - (long long)i * jb.g.rw);
+            jb.table[o] = nbhd_entry(jb.g, jb.tar, i, j, jb.full);
+        } else {
+            const long long p = item - jb.z_begin;
+            for (int a = 0; a < 3; ++a)
+                if (jb.zero_f[a]) jb.zero_f[a][p] = 0.f;
+            if (jb.zero_i) jb.zero_i[p] = 0;
+        }
+    }
 }
 
 // Catmull-Rom interpolation along one row of four pixels v0..v3 (bytes of
@@ -1018,6 +1052,17 @@ cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const 
 cudaError_t launch_nbhd_table(const Geom& g, const uint8_t* tar, uint4* table, cudaStream_t st, bool full) {
     dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
     k_nbhd_table<<<grd, blk, 0, st>>>(g, tar, table, full ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_prepare(const PrepJobs& J, cudaStream_t st) {
+    const long long total = J.px_total + J.z_total;
+    if (total <= 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long blocks = std::min<long long>((total + 255) / 256, (long long)sms * 8);
+    k_batch_prepare<<<(int)blocks, 256, 0, st>>>(J);
     return cudaGetLastError();
 }
 

@@ -8,9 +8,11 @@
 // its device memory fits the server's HBM budget.  A submit to a full ring is
 // dropped (the reference's bounded frame queue drops when full,
 // TW_Concurrent_Buffer.cpp).  One scheduler thread batches the oldest pending
-// frame of every idle stream into one twdic_batch launch on a free lane (CUDA
-// stream): frames that arrive while batches are on the GPU are taken by the
-// next free lane, so several batches overlap on the device.
+// frame of every idle stream (by default only frames within a factor of two
+// of the oldest one's POI count) into one twdic_batch launch on a free lane
+// (CUDA stream): frames that arrive while batches are on the GPU are taken by
+// the next free lane, so several batches overlap on the device.  Each batch's
+// device interval is timed by events on its lane.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -111,11 +113,23 @@ void fps_update(CamStream& cs, int elapsed_ms) {
 
 struct Lane {
     cudaStream_t st = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr;  // recorded when the lane's stream reaches the batch (timing)
+    cudaEvent_t done = nullptr;   // after the batch's result copies (timing)
     bool busy = false;
     int rc = TWDIC_OK;
     std::vector<std::pair<int, int>> work;  // (stream id, slot)
 };
+
+// Expected device time of a frame for the scheduler's ordering: a fixed part
+// and a part per POI (about what a 31x31-subset frame takes on GB300).
+constexpr int64_t kServiceNs = 200000;
+constexpr int64_t kServiceNsPerPoi = 30;
+
+// Device-side interval of one batch, milliseconds after the server's base event.
+struct Interval {
+    float t0, t1;
+};
+constexpr size_t kMaxIntervals = 1 << 20;
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
@@ -138,7 +152,11 @@ struct twdic_server {
     bool paused = false;
     std::thread worker;
     uint64_t submitted = 0, completed = 0, dropped = 0, nbatches = 0, batched_frames = 0, replays = 0;
+    uint64_t max_batch_formed = 0;  // frames in the largest batch launched
+    int32_t peak_lanes = 0;         // most batches in flight at one time (host view)
     std::vector<double> lat_ms;
+    cudaEvent_t base = nullptr;     // time origin of the batch intervals
+    std::vector<Interval> intervals;
 };
 
 namespace {
@@ -222,6 +240,7 @@ int launch_batch(twdic_server* s, Lane& lane, std::vector<CamStream*>& picked) {
     std::vector<int32_t*> it(k);
     std::vector<uint8_t*> fl(k);
     int rc = TWDIC_OK;
+    if (cudaEventRecord(lane.start, lane.st) != cudaSuccess) rc = fail_msg(TWDIC_ERR_CUDA, "event record failed");
     for (int i = 0; i < k; ++i) {
         CamStream* cs = picked[i];
         const int si = cs->queue.front();
@@ -269,12 +288,22 @@ int launch_batch(twdic_server* s, Lane& lane, std::vector<CamStream*>& picked) {
     s->nbatches += 1;
     s->batched_frames += (uint64_t)k;
     s->replays += replayed ? 1 : 0;
+    s->max_batch_formed = std::max(s->max_batch_formed, (uint64_t)k);
+    int in_flight = 0;
+    for (const Lane& l : s->lanes) in_flight += l.busy ? 1 : 0;
+    s->peak_lanes = std::max(s->peak_lanes, in_flight);
     return rc;
 }
 
 // Mark the frames of a finished lane done (lock held).
 void retire(twdic_server* s, Lane& lane) {
     const Clock::time_point now = Clock::now();
+    if (lane.rc == TWDIC_OK && s->intervals.size() < kMaxIntervals) {
+        float a = 0.f, b = 0.f;
+        if (cudaEventElapsedTime(&a, s->base, lane.start) == cudaSuccess &&
+            cudaEventElapsedTime(&b, s->base, lane.done) == cudaSuccess)
+            s->intervals.push_back({a, b});
+    }
     for (auto& w : lane.work) {
         auto it = s->streams.find(w.first);
         if (it == s->streams.end()) continue;
@@ -323,16 +352,38 @@ void worker_main(twdic_server* s) {
         if (!s->stop && !s->paused) {
             for (Lane& lane : s->lanes) {
                 if (lane.busy) continue;
-                // the oldest pending frame of every idle stream, oldest first
+                // the next pending frame of every idle stream
                 std::vector<CamStream*> ready;
                 for (auto& kv : s->streams) {
                     CamStream& cs = *kv.second;
                     if (!cs.busy && cs.has_ref && !cs.queue.empty()) ready.push_back(&cs);
                 }
                 if (ready.empty()) break;
-                std::sort(ready.begin(), ready.end(), [](CamStream* a, CamStream* b) {
-                    return a->slots[a->queue.front()].t_submit < b->slots[b->queue.front()].t_submit;
-                });
+                if (s->cfg.mix_sizes) {
+                    // oldest pending frame first
+                    std::sort(ready.begin(), ready.end(), [](CamStream* a, CamStream* b) {
+                        return a->slots[a->queue.front()].t_submit < b->slots[b->queue.front()].t_submit;
+                    });
+                } else {
+                    // earliest expected finish first: submit time plus an estimate
+                    // of the frame's device time from its POI count, so that a small
+                    // frame is not queued behind a much larger one submitted just
+                    // before it, while a large frame still ages to the front
+                    auto key = [](CamStream* c) {
+                        return c->slots[c->queue.front()].t_submit +
+                               std::chrono::nanoseconds(kServiceNs + kServiceNsPerPoi * (int64_t)c->n);
+                    };
+                    std::sort(ready.begin(), ready.end(), [&](CamStream* a, CamStream* b) { return key(a) < key(b); });
+                    // size-aware: the first frame and the frames whose POI count is
+                    // within a factor of two of it, so that a small frame does not
+                    // wait for a much larger one in the same batch (the others take
+                    // the next free lane)
+                    const int n0 = ready.front()->n;
+                    std::vector<CamStream*> same;
+                    for (CamStream* cs : ready)
+                        if (2 * (int64_t)cs->n >= n0 && cs->n <= 2 * (int64_t)n0) same.push_back(cs);
+                    ready.swap(same);
+                }
                 if ((int)ready.size() > s->cfg.max_batch) ready.resize(s->cfg.max_batch);
                 launch_batch(s, lane, ready);
                 progressed = true;
@@ -371,9 +422,12 @@ int twdic_server_create(const twdic_server_config* cfg, twdic_server** out) {
     s->lanes.resize(cfg->lanes);
     for (Lane& l : s->lanes) {
         if (cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreate(&l.start) != cudaSuccess || cudaEventCreate(&l.done) != cudaSuccess)
             return fail_msg(TWDIC_ERR_CUDA, "lane stream creation failed");
     }
+    if (cudaEventCreate(&s->base) != cudaSuccess || cudaEventRecord(s->base, s->lanes[0].st) != cudaSuccess ||
+        cudaEventSynchronize(s->base) != cudaSuccess)
+        return fail_msg(TWDIC_ERR_CUDA, "base event failed");
     twdic_server* raw = s.get();
     s->worker = std::thread(worker_main, raw);
     *out = s.release();
@@ -582,6 +636,35 @@ int twdic_server_stats(twdic_server* s, twdic_server_counters* out) {
     out->committed_bytes = s->committed;
     out->budget_bytes = s->cfg.hbm_budget_bytes;
     out->streams = (int32_t)s->streams.size();
+    out->max_batch_formed = s->max_batch_formed;
+    out->peak_lanes_in_flight = s->peak_lanes;
+    // device time: union of the batches' intervals, the part of it covered by
+    // two or more batches at once, and the most batches running at one time
+    if (!s->intervals.empty()) {
+        std::vector<std::pair<float, int>> ev;
+        ev.reserve(2 * s->intervals.size());
+        for (const Interval& iv : s->intervals) {
+            ev.push_back({iv.t0, +1});
+            ev.push_back({iv.t1, -1});
+        }
+        std::sort(ev.begin(), ev.end(), [](const std::pair<float, int>& a, const std::pair<float, int>& b) {
+            return a.first < b.first || (a.first == b.first && a.second < b.second);
+        });
+        int active = 0, peak = 0;
+        double busy = 0.0, overlap = 0.0;
+        for (size_t i = 0; i < ev.size(); ++i) {
+            if (i > 0) {
+                const double dt = (double)ev[i].first - (double)ev[i - 1].first;
+                if (active >= 1) busy += dt;
+                if (active >= 2) overlap += dt;
+            }
+            active += ev[i].second;
+            peak = std::max(peak, active);
+        }
+        out->device_busy_ms = busy;
+        out->device_overlap_ms = overlap;
+        out->peak_device_batches = peak;
+    }
     if (!s->lat_ms.empty()) {
         std::vector<double> l = s->lat_ms;
         std::sort(l.begin(), l.end());
@@ -637,9 +720,11 @@ int twdic_server_destroy(twdic_server* s) {
     for (auto& kv : s->streams) free_stream_buffers(*kv.second);
     s->streams.clear();
     for (Lane& l : s->lanes) {
+        if (l.start) cudaEventDestroy(l.start);
         if (l.done) cudaEventDestroy(l.done);
         if (l.st) cudaStreamDestroy(l.st);
     }
+    if (s->base) cudaEventDestroy(s->base);
     delete s;
     return TWDIC_OK;
 }

@@ -24,10 +24,11 @@ def frame_device_bytes(params: Params) -> int:
 
 class DICServer:
     def __init__(self, hbm_budget_bytes: int = 0, max_batch: int = 32, queue_depth: int = 4, lanes: int = 2,
-                 use_graph: bool = True, start_paused: bool = False, icgn_threads: int = 0, icgn_sampler: int = 2):
+                 use_graph: bool = True, start_paused: bool = False, icgn_threads: int = 0, icgn_sampler: int = 2,
+                 mix_sizes: bool = False):
         self._lib = _lib.load()
         self.cfg = ServerConfig(hbm_budget_bytes, max_batch, queue_depth, lanes, 1 if use_graph else 0,
-                                1 if start_paused else 0, icgn_threads, icgn_sampler)
+                                1 if start_paused else 0, icgn_threads, icgn_sampler, 1 if mix_sizes else 0)
         h = ctypes.c_void_p()
         check(self._lib.twdic_server_create(ctypes.byref(self.cfg), ctypes.byref(h)))
         self._h = h

@@ -313,10 +313,11 @@ TWDIC_API int twdic_icgn_compute_noalloc(const twdic_params* p, const uint8_t* d
                                          float* d_p6, int32_t* d_iters, uint8_t* d_flags, void* stream);
 
 /* ---- batches (no reference counterpart) ----
- * Several frame handles' targets in one set of launches: fast-path frames
- * with the same subset radius share one tensor-core FFT-CC launch, all
- * fast-path frames share one persistent IC-GN launch (up to 32 frames per
- * launch; larger batches take several).  Image pairs and POI sets may differ
+ * Several frame handles' targets in one set of launches: one launch builds
+ * every frame's per-frame table and zeroes its outputs, the fast-path frames
+ * share one tensor-core FFT-CC launch (all window sizes) and one persistent
+ * IC-GN launch (per interpolant; up to 128 frames per launch, larger batches
+ * take several).  Image pairs and POI sets may differ
  * in size.  Results equal those of twdic_frame_process on each frame.  Each
  * frame appears at most once per call; frames must live on the current
  * device.  The batch's IC-GN launch shape (set_tuning) applies to all its
@@ -342,6 +343,12 @@ TWDIC_API int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* co
                                   const uint8_t* const* tars, const int32_t* strides, int mem_in, float* const* u,
                                   float* const* v, float* const* zncc, float* const* p6, int32_t* const* iters,
                                   uint8_t* const* flags, int mem_out, int32_t* replayed);
+/* Device time of the phases of the last batch call that ran without a graph
+ * (the first of a graph-mode pair, or any call with graphs off), in
+ * milliseconds: t[0] target copies and the preparation launch (tables,
+ * zeroed outputs), t[1] FFT-CC, t[2] float LUTs (LUT sampler and plain
+ * frames only), t[3] IC-GN. */
+TWDIC_API int twdic_batch_phase_times(twdic_batch* b, float* t4);
 TWDIC_API int twdic_batch_destroy(twdic_batch* b);
 
 /* Device memory a frame handle with these parameters holds after its first

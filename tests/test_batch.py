@@ -48,6 +48,9 @@ def test_batch_equals_frames_alone():
         assert (w["flags"] == 0).mean() > 0.9, i
         for k in w:
             np.testing.assert_array_equal(o[k], w[k], err_msg=f"frame {i} {k}")
+    # the phases of the call (no graph): preparation, FFT-CC and IC-GN took time
+    ph = b.phase_times()
+    assert ph["prepare"] > 0 and ph["fftcc"] > 0 and ph["icgn"] > 0, ph
     # a second call on the same handles (caches warm) gives the same results
     outs2 = [f.alloc_outputs() for f in frames]
     b.process(frames, tars, outs2)

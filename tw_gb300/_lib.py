@@ -43,7 +43,7 @@ EXPORTED = (
     "twdic_frame_table",
     "twdic_frame_set_tuning", "twdic_frame_set_icgn_layout", "twdic_frame_set_icgn_unroll", "twdic_frame_set_guess_mode", "twdic_frame_set_fftcc_twiddles", "twdic_icgn_compute_noalloc",
     "twdic_batch_create", "twdic_batch_set_stream", "twdic_batch_set_tuning", "twdic_batch_set_icgn_layout", "twdic_batch_set_icgn_unroll", "twdic_batch_set_graph",
-    "twdic_batch_process", "twdic_batch_destroy", "twdic_frame_device_bytes",
+    "twdic_batch_process", "twdic_batch_phase_times", "twdic_batch_destroy", "twdic_frame_device_bytes",
     "twdic_server_create", "twdic_server_add_stream", "twdic_server_remove_stream", "twdic_server_set_reference",
     "twdic_submit", "twdic_poll", "twdic_server_resume", "twdic_server_stats", "twdic_server_stream_stats", "twdic_server_set_stream_guess", "twdic_server_destroy",
     "twdic_frame_set_fftcc_tuning", "twdic_frame_get_tuning", "twdic_frame_autotune",
@@ -168,6 +168,7 @@ def load():
         "twdic_batch_set_graph": ([_VP, _I], _I),
         "twdic_batch_process": ([_VP, ctypes.c_int32, _VP, _VP, _VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, _I,
                                  _I32P], _I),
+        "twdic_batch_phase_times": ([_VP, _VP], _I),
         "twdic_batch_destroy": ([_VP], _I),
         "twdic_frame_device_bytes": ([P, ctypes.POINTER(ctypes.c_uint64)], _I),
         "twdic_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(_VP)], _I),

@@ -9,7 +9,9 @@ Workload: `pairs` image pairs with sizes drawn from {512x384, 1024x768,
 ~ U[3, 12], margin 20, all seeded.  Pairs of one size share their image
 content (one synthetic reference/target per size: strain ramp plus drift).
 Prints one JSON line with POIs/s of the batched graph replay and of the
-one-call-per-frame loop (device-resident inputs and outputs, CUDA events)."""
+one-call-per-frame loop (device-resident inputs and outputs, CUDA events), the
+batched call's per-phase device times and the roofline fractions of its
+FFT-CC and IC-GN phases."""
 import argparse
 import json
 import os
@@ -73,6 +75,23 @@ def run_batched(pairs=48, steps=5, warmup=3, seed=3, data=None):
         for _ in range(warmup):
             one_by_one()
         ms_loop = timed(one_by_one, steps)
+        # per-phase device times of the batched call, from calls run without
+        # a graph (the same launches), and the mean IC-GN iterations per frame
+        eager = dic.DICBatch(graph=False)
+        eager.set_stream(stream)
+        phases = []
+        for _ in range(steps):
+            eager.process(frames, tars, outs)
+            phases.append(eager.phase_times())
+        kbar = []
+        for o in outs:
+            fl = o["flags"].cpu().numpy()
+            it = o["iters"].cpu().numpy()
+            kbar.append(float(it[fl == 0].mean()) if (fl == 0).any() else 0.0)
+    ph = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
+    flops_fft = sum(j["pois"] * 48.0 * (2 * j["r"]) ** 3 for j in jobs)
+    flops_icgn = sum(j["pois"] * k * (2 * j["r"] + 1) ** 2 * 64.0 for j, k in zip(jobs, kbar))
+    peaks = _peaks()
     sizes = {}
     for j in jobs:
         sizes[j["size"]] = sizes.get(j["size"], 0) + 1
@@ -82,7 +101,37 @@ def run_batched(pairs=48, steps=5, warmup=3, seed=3, data=None):
                         "pois_per_s": round(total / (float(np.median(ms_batch)) / 1000.0), 1),
                         "graph_replay": bool(replayed)},
             "one_call_per_frame": {"ms": round(float(np.median(ms_loop)), 3),
-                                   "pois_per_s": round(total / (float(np.median(ms_loop)) / 1000.0), 1)}}
+                                   "pois_per_s": round(total / (float(np.median(ms_loop)) / 1000.0), 1)},
+            "kernel_launches": "preparation (every frame's table and zeroed outputs), tensor-core FFT-CC (every "
+                               "window size), IC-GN (every frame): 3",
+            "phases_ms": {k: round(v, 3) for k, v in ph.items()},
+            "roofline": {"fftcc": {"flops": flops_fft,
+                                   "achieved_tflops": round(flops_fft / (ph["fftcc"] / 1e3) / 1e12, 1),
+                                   "peak_tflops": peaks["tensor"], "frac": round(
+                                       flops_fft / (ph["fftcc"] / 1e3) / 1e12 / peaks["tensor"], 4),
+                                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
+                         "icgn": {"flops": flops_icgn,
+                                  "achieved_tflops": round(flops_icgn / (ph["icgn"] / 1e3) / 1e12, 1),
+                                  "peak_tflops": peaks["fp32"], "frac": round(
+                                      flops_icgn / (ph["icgn"] / 1e3) / 1e12 / peaks["fp32"], 4),
+                                  "peak_source": "derived: SMs x 128 FP32 lanes x 2 flops x max SM clock"},
+                         "note": "48 N^3 flops per POI for FFT-CC (N = 2r), k S 64 for IC-GN (k the frame's mean "
+                                 "iterations, S = (2r + 1)^2)"}}
+
+
+def _peaks():
+    """Tensor (bf16 burst) and FP32 peaks in TFLOP/s: MEASURED_PEAKS.json where
+    present, else the fallback figures; FP32 is derived from the SM count and
+    the maximum SM clock."""
+    import torch
+    tensor, mhz = 1900.0, 2070.0
+    try:
+        m = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        tensor, mhz = m.get("bf16_tflops", tensor), m.get("sm_max_mhz", mhz)
+    except Exception:
+        pass
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return {"tensor": tensor, "fp32": round(sms * 128 * 2 * mhz * 1e6 / 1e12, 2)}
 
 
 def main(argv=None):

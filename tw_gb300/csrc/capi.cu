@@ -1094,9 +1094,15 @@ struct twdic_batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<uintptr_t> key;  // the call the instantiated graph replays
     cudaEvent_t done = nullptr;
+    // phase boundaries of the last call run without a graph: start,
+    // preparation done, FFT-CC done, float LUTs done, IC-GN done
+    cudaEvent_t ph[5] = {};
+    bool ph_recorded = false;
     ~twdic_batch() {
         if (exec) cudaGraphExecDestroy(exec);
         if (done) cudaEventDestroy(done);
+        for (auto& e : ph)
+            if (e) cudaEventDestroy(e);
         if (own_stream) cudaStreamDestroy(own_stream);
     }
 };
@@ -1167,6 +1173,15 @@ int prepare_target_for(Engine& e, int sampler) {
 // exist, so a second identical call can be captured into a graph.
 int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
     const int count = a.count;
+    // phase events on calls that run now (a capture records none)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TW_CUDA(cudaStreamIsCapturing(b->stream, &cap));
+    const bool timed = cap == cudaStreamCaptureStatusNone;
+    auto mark = [&](int k) -> int {
+        if (timed) TW_CUDA(cudaEventRecord(b->ph[k], b->stream));
+        return TWDIC_OK;
+    };
+    TW_TRY(mark(0));
     std::vector<int> fast_tc, fast_ic;
     // per frame: its target into the handle, guesses in (host outputs), and
     // its part of the preparation launch (neighbourhood table; outputs that
@@ -1221,6 +1236,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         }
         TW_CUDA(launch_batch_prepare(P, b->stream));
     }
+    TW_TRY(mark(1));
     // FFT-CC of the frames off the tensor-core path, one call each
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
@@ -1246,6 +1262,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             }
         }
     }
+    TW_TRY(mark(2));
     // float LUTs (the LUT samplers and the plain path), one launch per frame
     for (int i = 0; i < count; ++i) {
         Engine& e = a.frames[i]->e;
@@ -1256,6 +1273,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             TW_TRY(e.prepare_target());
         }
     }
+    TW_TRY(mark(3));
     // one launch per residency level and sampler (and per kMaxJobs frames): a
     // launch sizes shared memory for its largest subset, so frames whose
     // subsets allow more resident CTAs are not launched with larger ones
@@ -1313,6 +1331,8 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         const FrameOut o = frame_out(e, a, i);
         TW_TRY(e.icgn_solve(o.u, o.v, o.p6, o.it, o.fl));
     }
+    TW_TRY(mark(4));
+    if (timed) b->ph_recorded = true;
     return TWDIC_OK;
 }
 
@@ -1326,6 +1346,7 @@ int twdic_batch_create(twdic_batch** out) {
     TW_CUDA(cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking));
     b->stream = b->own_stream;
     TW_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+    for (auto& e : b->ph) TW_CUDA(cudaEventCreate(&e));
     TW_TRY(b->d_work.ensure(sizeof(int) * (2 + kMaxTcSegsScratch)));
     TW_TRY(b->d_err.ensure(sizeof(unsigned)));
     TW_CUDA(cudaMemset(b->d_err.p, 0, sizeof(unsigned)));
@@ -1485,6 +1506,14 @@ int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frame
             return fail(TWDIC_ERR_TIMEOUT, "a bounded device-side wait gave up");
         }
     }
+    return TWDIC_OK;
+}
+
+int twdic_batch_phase_times(twdic_batch* b, float* t4) {
+    if (!b || !t4) return fail(TWDIC_ERR_INVALID_ARG, "NULL argument");
+    if (!b->ph_recorded) return fail(TWDIC_ERR_STATE, "no batch call has run without a graph");
+    TW_CUDA(cudaEventSynchronize(b->ph[4]));
+    for (int k = 0; k < 4; ++k) TW_CUDA(cudaEventElapsedTime(&t4[k], b->ph[k], b->ph[k + 1]));
     return TWDIC_OK;
 }
 

@@ -429,6 +429,14 @@ class DICBatch:
                                             arr("p6"), arr("iters"), arr("flags"), mem_out, ctypes.byref(rep)))
         self.replayed = bool(rep.value)
 
+    def phase_times(self):
+        """Device time (ms) of the phases of the last call run without a
+        graph: preparation (target copies, tables, zeroed outputs), FFT-CC,
+        float LUTs, IC-GN."""
+        t = np.zeros(4, np.float32)
+        check(self._lib.twdic_batch_phase_times(self._h, _ptr(t)))
+        return dict(prepare=float(t[0]), fftcc=float(t[1]), lut=float(t[2]), icgn=float(t[3]))
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.twdic_batch_destroy(self._h)

@@ -191,8 +191,8 @@ TWDIC_API int twdic_frame_destroy(twdic_frame* h);
  *       (BicubicSplineCoefficients_s, TW_utils.cpp:521-602)
  *   TWDIC_TABLE_REF_GRADIENT   roi_h x roi_w x 2: (R_x, R_y) of the reference
  *       over the ROI, central differences (GradientXY_2Images_s,
- *       TW_utils.cpp:232-305), as the fast path keeps them (half precision,
- *       exact: halves of integers below 128)
+ *       TW_utils.cpp:232-305), as the fast path keeps them (halves of
+ *       integers below 128, exact in FP32)
  *   TWDIC_TABLE_SUBSET_GRADIENT num_pois x S x 2 (S = subset pixels, row
  *       major): (R_x, R_y) of every POI's subset as the plain path's
  *       per-reference cache keeps them (plain path handles only)
@@ -228,7 +228,7 @@ TWDIC_API int twdic_frame_set_tuning(twdic_frame* h, int icgn_threads, int icgn_
  * 32 to 256).  chunk > 0: one POI per warp; the warps of a CTA (threads 128
  * to 1024, a table sampler) take POIs from runs of `chunk` consecutive POIs,
  * so the subsets in flight on an SM overlap and are re-read from L1, and the
- * reference gradients come from a per-reference image (4 B per ROI pixel). */
+ * reference gradients come from a per-reference image (8 B per ROI pixel). */
 TWDIC_API int twdic_frame_set_icgn_layout(twdic_frame* h, int chunk);
 /* Initial guesses of a frame handle in batched calls (twdic_batch_process and
  * the server): mode 0 (default) runs FFT-CC and starts IC-GN from its integer

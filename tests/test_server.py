@@ -24,7 +24,7 @@ def test_frame_device_bytes_formula():
     r = lambda b: -(-b // (2 << 20)) * (2 << 20)  # noqa: E731
     pitch = (197 + 15) // 16 * 16
     want = (2 * r(pitch * 160) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 4 * r(1024)
-            + r(64 * n) + r(168 * n) + r(n) + r(4 * g.roi_w * g.roi_h) + r(16 * g.roi_w * g.roi_h))
+            + r(64 * n) + r(168 * n) + r(n) + r(8 * g.roi_w * g.roi_h) + r(16 * g.roi_w * g.roi_h))
     assert frame_device_bytes(p) == want
     big = _params(synth.Geometry(2048, 2048, 1, 1, 2046, 2046, 20, 5, 20))
     assert frame_device_bytes(big) > 128 << 20  # 155k POIs: 67 MB neighbourhood table, 36 MB cache

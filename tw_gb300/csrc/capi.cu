@@ -309,8 +309,8 @@ struct Engine {
             TW_TRY(c_flag64.ensure((size_t)n));
             TW_CUDA(launch_ref_precompute_fast(g, d_ref.as<uint8_t>(), d_poi.as<int2>(), n, c_stat.as<float>(),
                                                c_chol64.as<double>(), c_flag64.as<uint8_t>(), stream));
-            TW_TRY(c_grad.ensure(sizeof(__half2) * (size_t)g.rw * g.rh));
-            TW_CUDA(launch_ref_grad(g, d_ref.as<uint8_t>(), c_grad.as<__half2>(), stream));
+            TW_TRY(c_grad.ensure(sizeof(float2) * (size_t)g.rw * g.rh));
+            TW_CUDA(launch_ref_grad(g, d_ref.as<uint8_t>(), c_grad.as<float2>(), stream));
         }
         cache_valid = true;
         if (t_pre) *t_pre = 1.f;
@@ -365,7 +365,7 @@ struct Engine {
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.p,
                                      d_work.as<int>(), u, v, p6, iters, flags, solve_tune(), stream,
-                                     c_grad.as<__half2>()));
+                                     c_grad.as<float2>()));
         }
         return TWDIC_OK;
     }
@@ -690,14 +690,14 @@ int twdic_frame_table(twdic_frame* h, int which, float* dst) {
     if (which == TWDIC_TABLE_REF_GRADIENT) {
         if (!e.have_ref) return fail(TWDIC_ERR_STATE, "the gradients need a reference image");
         DevBuf grad;
-        TW_TRY(grad.ensure(sizeof(__half2) * px));
-        TW_CUDA(launch_ref_grad(g, e.d_ref.as<uint8_t>(), grad.as<__half2>(), e.stream));
-        std::vector<__half2> hb(px);
-        TW_CUDA(cudaMemcpyAsync(hb.data(), grad.p, sizeof(__half2) * px, cudaMemcpyDeviceToHost, e.stream));
+        TW_TRY(grad.ensure(sizeof(float2) * px));
+        TW_CUDA(launch_ref_grad(g, e.d_ref.as<uint8_t>(), grad.as<float2>(), e.stream));
+        std::vector<float2> hb(px);
+        TW_CUDA(cudaMemcpyAsync(hb.data(), grad.p, sizeof(float2) * px, cudaMemcpyDeviceToHost, e.stream));
         TW_CUDA(cudaStreamSynchronize(e.stream));
         for (size_t o = 0; o < px; ++o) {
-            dst[2 * o] = __low2float(hb[o]);
-            dst[2 * o + 1] = __high2float(hb[o]);
+            dst[2 * o] = hb[o].x;
+            dst[2 * o + 1] = hb[o].y;
         }
         return TWDIC_OK;
     }
@@ -774,7 +774,7 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
         t += r(64 * (uint64_t)p->roi_width * p->roi_height);  // float LUT
     } else {
         t += r(64 * n) + r(168 * n) + r(n);                 // statistics, inverse Hessian, flags
-        t += r(4 * (uint64_t)p->roi_width * p->roi_height);   // reference gradient image (half2)
+        t += r(8 * (uint64_t)p->roi_width * p->roi_height);   // reference gradient image (float2)
         t += r(16 * (uint64_t)p->roi_width * p->roi_height);  // neighbourhood table
     }
     *bytes = t;
@@ -1312,7 +1312,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             jb.hinv = e.c_chol64.as<double>();
             jb.rflag = e.c_flag64.as<uint8_t>();
             jb.table = tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
-            jb.grad = e.c_grad.as<__half2>();
+            jb.grad = e.c_grad.as<float2>();
             jb.u = o.u;
             jb.v = o.v;
             jb.p6 = o.p6;

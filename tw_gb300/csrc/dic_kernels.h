@@ -43,7 +43,7 @@ struct IcgnJob {
     const double* hinv;   // 21 doubles per POI
     const uint8_t* rflag;
     const void* table;    // per-frame target table of the sampler (or null: window)
-    const __half2* grad = nullptr;  // per-reference gradient image, rw x rh (or null: staged per POI)
+    const float2* grad = nullptr;  // per-reference gradient image, rw x rh (or null: staged per POI)
     float* u;
     float* v;
     float* p6;
@@ -117,9 +117,9 @@ cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                              const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
-                             const IcgnTune& tune, cudaStream_t st, const __half2* grad = nullptr);
-// Per-reference gradient image (R_x, R_y) of the ROI, half2, rw x rh (kernels_icgn_fast.cu)
-cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, __half2* grad, cudaStream_t st);
+                             const IcgnTune& tune, cudaStream_t st, const float2* grad = nullptr);
+// Per-reference gradient image (R_x, R_y) of the ROI, float2, rw x rh (kernels_icgn_fast.cu)
+cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, float2* grad, cudaStream_t st);
 int icgn_fast_window(const Geom& g);
 // CTAs per SM the fast IC-GN kernel can keep resident for this geometry and
 // launch shape (shared memory, registers, the 32-CTA limit): jobs batched

@@ -4,7 +4,7 @@
 // the subset sums of the six steepest-descent images SD_k and of
 // SD_k * (R - mean(R))) and the packed FP64 inverse Hessian (21 doubles, from
 // an FP64 Cholesky factor), and per ROI pixel the reference gradients
-// (R_x, R_y) as half2 -- exact half integers (TW_utils.cpp:232-305).  The
+// (R_x, R_y) as float2 -- half integers, exact (TW_utils.cpp:232-305).  The
 // steepest-descent images are never stored: SD = (R_x, R_x dx, R_x dy, R_y,
 // R_y dx, R_y dy) is formed per sample.
 //
@@ -778,15 +778,16 @@ __global__ void __launch_bounds__(THREADS, (THREADS == 64 ? 16 : 2048 / THREADS 
     }
 }
 
-// Reference gradients of every ROI pixel as half2 (R_x, R_y): central
-// differences (TW_utils.cpp:232-305), half integers of magnitude <= 127.5,
-// exact in FP16.  The ROI has one pixel of border on every side, so every
+// Reference gradients of every ROI pixel as float2 (R_x, R_y): central
+// differences (TW_utils.cpp:232-305), half integers of magnitude <= 127.5.
+// (FP32 rather than FP16 pairs: the sample loop of k_icgn_warp then loads them
+// without conversion, 2 % faster at 2048^2.)  The ROI has one pixel of border on every side, so every
 // neighbour read lies in the image.
-__global__ void k_ref_grad(Geom g, const uint8_t* __restrict__ ref, __half2* __restrict__ grad) {
+__global__ void k_ref_grad(Geom g, const uint8_t* __restrict__ ref, float2* __restrict__ grad) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.rh || j >= g.rw) return;
     const uint8_t* r = ref + (size_t)(i + g.sy) * g.pitch + (j + g.sx);
-    grad[(size_t)i * g.rw + j] = __floats2half2_rn(0.5f * (float)((int)r[1] - (int)r[-1]),
+    grad[(size_t)i * g.rw + j] = make_float2(0.5f * (float)((int)r[1] - (int)r[-1]),
                                                    0.5f * (float)((int)r[g.pitch] - (int)r[-g.pitch]));
 }
 
@@ -794,7 +795,7 @@ __global__ void k_ref_grad(Geom g, const uint8_t* __restrict__ ref, __half2* __r
 // of CHUNK consecutive POIs (CTA b takes runs b, b + gridDim.x, ...; its
 // warps draw POIs from them in order through a shared counter), so the
 // subsets a CTA has in flight overlap and their target-table entries and
-// reference gradients (global, per-reference half2 image) are re-read from
+// reference gradients (global, per-reference float2 image) are re-read from
 // L1 across neighbouring POIs and across iterations.  The arithmetic per
 // POI is that of k_icgn_fast<32, ...>: the same sample order per lane, the
 // same sums, reduction, solve and update, so the results are identical.
@@ -859,7 +860,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
         __syncwarp();
         // sample k = lane + 32 j at subset offset (dx, dy); its gradient at
         // ROI offset gofs, stepped with the same carry
-        const __half2* grad0 = jb.grad + ((size_t)(py - g.ry - g.sy) * g.rw + (px - g.rx - g.sx));
+        const float2* grad0 = jb.grad + ((size_t)(py - g.ry - g.sy) * g.rw + (px - g.rx - g.sx));
         const int gofs_first = (lane / SW) * g.rw + lane % SW;
         const int dgofs = (32 / SW) * g.rw + 32 % SW, gwrap = g.rw - SW;
         const float2 d_first = make_float2((float)(lane % SW - g.rx), (float)(lane / SW - g.ry));
@@ -883,7 +884,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                         const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
                                                       __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
                         const int ix = (int)wxy.x, iy = (int)wxy.y;
-                        ps.add((float)jb.tar[(size_t)iy * g.pitch + ix] - c, __half22float2(grad0[gofs]), d);
+                        ps.add((float)jb.tar[(size_t)iy * g.pitch + ix] - c, grad0[gofs], d);
                         gofs += dgofs;
                         d = __fadd2_rn(d, dd);
                         if (d.x > rxf) {
@@ -922,7 +923,7 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                                 tx, make_float2(a2.x, a3.x));
                             tp = (((r23.y * fy + r23.x) * fy + r01.y) * fy + r01.x) - c;
                         }
-                        ps.add(tp, __half22float2(grad0[gofs]), d);
+                        ps.add(tp, grad0[gofs], d);
                         gofs += dgofs;
                         d = __fadd2_rn(d, dd);
                         if (d.x > rxf) {
@@ -1109,7 +1110,7 @@ int icgn_fast_residency(const Geom& g, const IcgnTune& tune) {
     return std::max(1, std::min(std::min(32, by_regs), by_smem));
 }
 
-cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, __half2* grad, cudaStream_t st) {
+cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, float2* grad, cudaStream_t st) {
     dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
     k_ref_grad<<<grd, blk, 0, st>>>(g, ref, grad);
     return cudaGetLastError();
@@ -1201,7 +1202,7 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                              const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
-                             const IcgnTune& tune, cudaStream_t st, const __half2* grad) {
+                             const IcgnTune& tune, cudaStream_t st, const float2* grad) {
     if (n <= 0) return cudaSuccess;
     IcgnJobs J;
     J.njobs = 1;

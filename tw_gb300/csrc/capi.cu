@@ -167,6 +167,10 @@ struct Engine {
     DevBuf d_tcmaps;
     void* h_tcmaps = nullptr;
     TcMapInfo tcmaps{0, 0, 0};
+    // per-reference cache of the tensor-core FFT-CC: the reference windows'
+    // spectra and integer sums at the POIs (dropped with the IC-GN cache)
+    DevBuf c_fspec, c_fsum;
+    bool fspec_valid = false;
     cudaEvent_t ev[7] = {};
     cudaEvent_t ev_sync = nullptr;  // orders this handle's stream with a batch stream
     float last_times[6] = {0, 0, 0, 0, 0, 0};
@@ -195,7 +199,9 @@ struct Engine {
         stream = own_stream;
         for (auto& e : ev) TW_CUDA(cudaEventCreate(&e));
         TW_CUDA(cudaEventCreateWithFlags(&ev_sync, cudaEventDisableTiming));
-        const size_t img = (size_t)g.pitch * p.img_height;
+        // 16 spare bytes: the FFT-CC kernel reads whole aligned 32-bit words
+        // around a window's last byte
+        const size_t img = (size_t)g.pitch * p.img_height + 16;
         TW_TRY(d_ref.ensure(img));
         TW_TRY(d_tar.ensure(img));
         TW_TRY(d_poi.ensure(sizeof(int2) * (size_t)n));
@@ -242,6 +248,7 @@ struct Engine {
         TW_TRY(upload_image(d_ref, img, stride, mem));
         have_ref = true;
         cache_valid = false;
+        fspec_valid = false;
         return TWDIC_OK;
     }
 
@@ -276,13 +283,31 @@ struct Engine {
         return TWDIC_OK;
     }
 
+    // The reference spectra of the tensor-core FFT-CC: once per reference
+    // (and POI set), by the per-reference pass, on this handle's stream.
+    int ensure_fspec(const FftccTune& tune) {
+        if (fspec_valid) return TWDIC_OK;
+        if (!have_ref) return fail(TWDIC_ERR_STATE, "FFT-CC needs a reference image");
+        TW_TRY(c_fspec.ensure(fftcc_tc_spectrum_bytes(g, n)));
+        TW_TRY(c_fsum.ensure(sizeof(int2) * (size_t)n));
+        TW_TRY(ensure_tc_maps(tune));
+        TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), d_tcmaps.p, tcmaps.key, tcmaps.uw,
+                                tcmaps.utoff, c_fspec.as<uint32_t>(), c_fsum.as<int2>(), d_poi.as<int2>(), n, nullptr,
+                                nullptr, nullptr, nullptr, d_err.as<unsigned>(), d_work.as<int>() + 1, tune, stream,
+                                true));
+        fspec_valid = true;
+        return TWDIC_OK;
+    }
+
     // FFT-CC of all POIs into device arrays.
     int fftcc(float* u, float* v, float* z, uint8_t* st) {
         if (!have_ref || !have_tar) return fail(TWDIC_ERR_STATE, "FFT-CC needs a reference and a target image");
         const int2* poi = d_poi.as<int2>();
         if (prm.path == TWDIC_PATH_FAST && fftcc_tune.use_tc && fftcc_tc_supported(g)) {
+            TW_TRY(ensure_fspec(fftcc_tune));
             TW_TRY(ensure_tc_maps(fftcc_tune));
-            TW_CUDA(launch_fftcc_tc(g, d_tcmaps.p, tcmaps.key, tcmaps.uw, tcmaps.utoff, poi, n, u, v, z, st,
+            TW_CUDA(launch_fftcc_tc(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), d_tcmaps.p, tcmaps.key, tcmaps.uw,
+                                    tcmaps.utoff, c_fspec.as<uint32_t>(), c_fsum.as<int2>(), poi, n, u, v, z, st,
                                     d_err.as<unsigned>(), d_work.as<int>() + 1, fftcc_tune, stream));
         } else {
             TW_CUDA(launch_fftcc_plain(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, d_tw.as<float2>(), u, v, z,
@@ -540,6 +565,7 @@ int twdic_icgn_compute(twdic_icgn* h, const uint8_t* tar, int32_t stride, const 
             e.cache_poi_host.assign(poi_yx, poi_yx + 2 * n);
             TW_TRY(copy_in(e.d_poi.p, poi_yx, 8 * n, mem_in, e.stream));
             e.cache_valid = false;
+            e.fspec_valid = false;
         }
     } else {
         int* changed_d = e.d_work.as<int>() + 2;
@@ -551,6 +577,7 @@ int twdic_icgn_compute(twdic_icgn* h, const uint8_t* tar, int32_t stride, const 
         if (changed) {
             e.cache_poi_host.clear();
             e.cache_valid = false;
+            e.fspec_valid = false;
         }
     }
     float *du = u, *dv = v, *dp6 = p6 ? p6 : e.d_p6.as<float>();
@@ -761,7 +788,7 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
     TW_TRY(num_pois_of(*p, &nx, &ny));
     const uint64_t n = (uint64_t)nx * ny;
     const uint64_t pitch = (uint64_t)((p->img_width + 15) & ~15);
-    const uint64_t img = pitch * (uint64_t)p->img_height;
+    const uint64_t img = pitch * (uint64_t)p->img_height + 16;
     auto r = [](uint64_t b) { return (b + (2ull << 20) - 1) / (2ull << 20) * (2ull << 20); };
     uint64_t t = 0;
     t += 2 * r(img);                                        // reference, target
@@ -775,6 +802,12 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
     } else {
         t += r(64 * n) + r(168 * n) + r(n);                 // statistics, inverse Hessian, flags
         t += r(8 * (uint64_t)p->roi_width * p->roi_height);   // reference gradient image (float2)
+        if (p->subset_x == p->subset_y && p->subset_x >= 4 && p->subset_x <= 32) {
+            // the tensor-core FFT-CC's reference spectra (N/2 + 1 rows of N
+            // rounded up to 4 FP16 pairs per POI) and window sums
+            const uint64_t N = 2 * (uint64_t)p->subset_x;
+            t += r(n * (N / 2 + 1) * ((N + 3) / 4 * 4) * 4) + r(8 * n);
+        }
         t += r(16 * (uint64_t)p->roi_width * p->roi_height);  // neighbourhood table
     }
     *bytes = t;
@@ -837,7 +870,7 @@ int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll) {
 
 int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (groups < 0 || groups > 2 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
+    if (groups < 0 || groups > 4 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
     h->e.fftcc_tune.use_tc = use_tc;
     h->e.fftcc_tune.groups = groups;
     h->e.fftcc_tune.pois_per_group = pois_per_group;
@@ -1251,10 +1284,12 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
         for (size_t m = 0; m < fast_tc.size(); ++m) {
             const int i = fast_tc[m];
             Engine& e = a.frames[i]->e;
+            TW_TRY(e.ensure_fspec(b->fftcc_tune));
             TW_TRY(e.ensure_tc_maps(b->fftcc_tune));
             const FrameOut o = frame_out(e, a, i);
             jobs.push_back(FftccJob{e.g, e.d_tcmaps.p, e.tcmaps.key, e.tcmaps.uw, e.tcmaps.utoff,
-                                    e.d_poi.as<int2>(), e.n, o.u, o.v, o.z, e.d_fst.as<uint8_t>()});
+                                    e.d_ref.as<uint8_t>(), e.d_tar.as<uint8_t>(), e.c_fspec.as<uint32_t>(), e.c_fsum.as<int2>(), e.d_poi.as<int2>(), e.n, o.u,
+                                    o.v, o.z, e.d_fst.as<uint8_t>()});
             if ((int)jobs.size() == kMaxTcJobsPerLaunch || m + 1 == fast_tc.size()) {
                 TW_CUDA(launch_fftcc_tc_jobs(jobs.data(), (int)jobs.size(), b->fftcc_tune, b->d_err.as<unsigned>(),
                                              b->d_work.as<int>() + 1, b->stream));
@@ -1443,6 +1478,9 @@ int twdic_batch_process(twdic_batch* b, int32_t count, twdic_frame* const* frame
         for (int i = 0; i < count; ++i) {
             const Engine& e = frames[i]->e;
             caches_ok = caches_ok && e.cache_valid;
+            // tensor-core FFT-CC frames read the reference spectra
+            if (e.prm.path == TWDIC_PATH_FAST && e.fftcc_tune.use_tc && !e.guess && fftcc_tc_supported(e.g))
+                caches_ok = caches_ok && e.fspec_valid;
             // the frame's own settings that batch_enqueue reads, then its arrays
             for (uintptr_t x : {(uintptr_t)frames[i], (uintptr_t)e.guess, (uintptr_t)e.interp,
                                 (uintptr_t)e.fftcc_tune.use_tc, (uintptr_t)tars[i],

@@ -145,9 +145,14 @@ bool fftcc_tc_encode_maps(const Geom& g, const uint8_t* ref, const uint8_t* tar,
                           void* host_buf, TcMapInfo* info);
 // err: error flags; work: scratch -- one int (one window size) or kMaxTcSegsScratch
 // ints (several), zeroed by the launcher
-cudaError_t launch_fftcc_tc(const Geom& g, const void* maps, uint64_t map_key, int uw, int utoff, const int2* poi,
-                            int n, float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
-                            const FftccTune& tune, cudaStream_t st);
+// The reference windows' spectra are cached per reference: fspec [n][N/2+1][FS]
+// FP16 (Re, Im) pairs with FS = N rounded up to 4 (fftcc_tc_spectrum_bytes),
+// fsum [n] the windows' (sum f, sum f^2).  ref = true runs the per-reference
+// pass that writes them; ref = false the per-frame FFT-CC that reads them.
+cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref_img, const uint8_t* tar_img, const void* maps,
+                            uint64_t map_key, int uw, int utoff, uint32_t* fspec, int2* fsum, const int2* poi, int n, float* u, float* v, float* zncc, uint8_t* status,
+                            unsigned* err, int* work, const FftccTune& tune, cudaStream_t st, bool ref = false);
+size_t fftcc_tc_spectrum_bytes(const Geom& g, int n);
 // One image pair of a batched tensor-core FFT-CC launch.  Jobs of one window
 // size share one k_fftcc_tc launch; jobs of several window sizes (up to 32)
 // share one k_fftcc_tc_seg launch.
@@ -158,6 +163,10 @@ struct FftccJob {
     const void* maps;  // device TMA descriptors (fftcc_tc_encode_maps)
     uint64_t map_key;
     int uw, utoff;
+    const uint8_t* ref;  // the images the maps describe
+    const uint8_t* tar;
+    uint32_t* fspec;  // the job's cached reference spectra (launch_fftcc_tc)
+    int2* fsum;
     const int2* poi;
     int n;
     float* u;
@@ -166,7 +175,7 @@ struct FftccJob {
     uint8_t* status;
 };
 cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* work,
-                                 cudaStream_t st);
+                                 cudaStream_t st, bool ref = false);
 bool fftcc_tc_supported(const Geom& g);
 
 // ---- tracking loop (kernels_track.cu)

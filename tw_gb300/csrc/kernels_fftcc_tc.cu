@@ -60,17 +60,20 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kTmemCols = 128;
 constexpr unsigned kWaitLimit = 1u << 24;
 
-// The tensor maps of one image pair: boxes [N rows][BW bytes] of one window
-// and [N rows][uw bytes] holding the windows of a batch whose POIs lie on one
-// POI row.
+// The tensor maps of one image pair: boxes [N rows][uw bytes] holding the
+// windows of a batch whose POIs lie on one POI row.
 struct alignas(128) TcMaps {
-    CUtensorMap ref, tar, ref_u, tar_u;
+    CUtensorMap ref_u, tar_u;
 };
 constexpr int kMaxTcJobs = kMaxTcJobsPerLaunch;  // image pairs per launch
 constexpr int kMaxTcSegs = kMaxTcSegsScratch;    // window sizes per launch (N = 8 .. 64, even)
 
 struct TcShape {
-    int N, H, HP, NP, PB, tiles1, K4, BW, WS, groups;
+    int N, H, HP, NP, PB, tiles1, K4, groups;
+    int uw, utoff;  // one-row boxes: width (0: none for this geometry) and the target box's offset
+    int win_bytes;  // a group's window region
+    int tiles4;  // 128-row tiles of the surface (stage 4)
+    int FS;      // complex values per cached spectrum row: N rounded up to 4
     int NW4;  // 32-bit words per window row in the exact re-evaluation
     int lo;   // 1: twiddles as FP16 hi + lo (two MMAs per product), 0: hi only
     // shared twiddle tables
@@ -88,6 +91,10 @@ struct TcShape {
 // ordered by window size; a segment is a run of jobs of one window size.
 struct TcJob {
     const TcMaps* maps;  // device copy of the job's tensor maps
+    const uint8_t* ref;  // the images (windows of batches off one POI row are read from here)
+    const uint8_t* tar;
+    uint32_t* fspec;     // reference spectra [n][H][FS] FP16 pairs (per-reference cache)
+    int2* fsum;          // reference windows' (sum f, sum f^2) [n]
     int uw;              // width of the one-row boxes (0: not used for this job)
     int utoff;           // offset of the target box in the window region (128-byte aligned)
     Geom g;
@@ -250,10 +257,10 @@ struct TcCta {
     int sdark[kMaxGroups][kMaxPB];
     int cbase[kMaxGroups][kMaxPB];      // first candidate slot of each POI
     int cend[kMaxGroups][kMaxPB];       // one past its last
-    int wtot[kMaxGroups][4];            // candidates per warp
+    int wtot[kMaxGroups][2][4];         // candidates per warp and surface tile
     uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
     int2 spoi[kMaxGroups][kMaxPB];
-    int wbase[kMaxGroups][2 * kMaxPB];  // byte offset of each window's (0, 0) in wwin
+    const uint8_t* wptr[kMaxGroups][2 * kMaxPB];  // each window's (0, 0): staged box or the image
     int wrs[kMaxGroups];                // row stride of the windows in wwin
     int snext[kMaxGroups];
 };
@@ -264,9 +271,9 @@ struct TcCta {
 __device__ __forceinline__ void tc_acquire_maps(const TcJobs& J, int lo, int hi) {
     for (int j = lo; j < hi; ++j) {
         const TcMaps* m = J.job[j].maps;
-        const CUtensorMap* mm[4] = {&m->ref, &m->tar, &m->ref_u, &m->tar_u};
+        const CUtensorMap* mm[2] = {&m->ref_u, &m->tar_u};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 2; ++k) {
             asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
                              reinterpret_cast<uint64_t>(mm[k]))
                          : "memory");
@@ -289,7 +296,11 @@ __device__ __forceinline__ void tc_load_tables(uint8_t* sm, const uint4* __restr
 // thread 0 at the start of a batch so that the atomic's latency is hidden.
 // phase / tphase: the parities of the group's MMA and TMA mbarriers, carried
 // across calls.  Returns false after a bounded wait gave up (err set).
-template <int NP, int HP, bool MULTI, bool LO>
+// REF: the per-reference pass -- stages 1 and 2 of the reference windows,
+// whose spectra (scaled by sqrt(n2) / ||f - mean f||, FP16 pairs) and integer
+// sums go to the job's cache.  Otherwise the per-frame pass: stages 1 and 2 of
+// the target windows only, the reference spectra read from that cache.
+template <int NP, int HP, bool MULTI, bool LO, bool REF>
 __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape& s, int job_lo, int job_hi,
                                                  int nbatch, int first, int* counter, int counter_base,
                                                  unsigned* err, TcCta& cs, uint8_t* sm, uint32_t& phase,
@@ -297,11 +308,11 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
     const int grp = threadIdx.x >> 7;
     const int t = threadIdx.x & 127, warp = t >> 5, lane = t & 31;
     const int bar_id = 1 + grp;
-    const int N = s.N, H = s.H, PB = s.PB, K4 = s.K4, BW = s.BW, WS = s.WS;
+    const int N = s.N, H = s.H, PB = s.PB, K4 = s.K4;
     const int n2 = N * N;
     constexpr int K1 = NP;
     uint8_t* gbase = sm + s.tab_bytes + grp * s.group_bytes;
-    uint8_t* wwin = gbase + s.off_win;  // [2 PB] TMA boxes of N rows x BW bytes, stride WS
+    uint8_t* wwin = gbase + s.off_win;  // the two one-row TMA boxes: reference at 0, target at utoff
     PeakScratch* ps = reinterpret_cast<PeakScratch*>(gbase + s.off_a13);
     uint64_t* mbar = &cs.mbar_mma[grp];
     uint64_t* tbar = &cs.mbar_tma[grp];
@@ -309,6 +320,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
     const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
     const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
+    const int FS = s.FS;  // cached spectrum: complex values per (POI, ky) row
     int nxt = 0;
     for (int batch = first; batch < nbatch; batch = cs.snext[grp]) {
         if (t == 0) nxt = counter_base + atomicAdd(counter, 1);
@@ -330,10 +342,10 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         group_sync(bar_id);
 
-        // ---- phase L1: the windows by TMA (x aligned down to 16 bytes;
-        // out-of-bounds parts are zero-filled).  When the batch's POIs lie on
-        // one POI row, one [N][uw] box per image holds all its windows (two
-        // copies instead of 2 PB); otherwise one [N][BW] box per window
+        // ---- phase L1: the windows.  When the batch's POIs lie on one POI row,
+        // one [N][uw] TMA box per image holds all its windows (x aligned down
+        // to 16 bytes); otherwise (a batch across POI rows, POIs off the grid)
+        // the windows are read from the images in global memory
         if (t == 0) {
             fence_async_smem();  // the previous batch's generic reads of the windows come first
             int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
@@ -354,36 +366,50 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 for (int p = 0; p < PB; ++p) {
                     const int2 pyx = cs.spoi[grp][p];
                     const int xo = pyx.x < 0 ? 0 : pyx.y - g.rx - xau;
-                    cs.wbase[grp][2 * p] = xo;
-                    cs.wbase[grp][2 * p + 1] = jb.utoff + xo;
+                    cs.wptr[grp][2 * p] = wwin + xo;
+                    cs.wptr[grp][2 * p + 1] = wwin + jb.utoff + xo;
                 }
             } else {
-                int nload = 0;
-                for (int wi = 0; wi < 2 * PB; ++wi) nload += cs.spoi[grp][wi >> 1].x >= 0;
-                mbar_expect_tx(tbar, (uint32_t)(nload * N * BW));
-                cs.wrs[grp] = BW;
-                for (int wi = 0; wi < 2 * PB; ++wi) {
-                    const int2 pyx = cs.spoi[grp][wi >> 1];
-                    cs.wbase[grp][wi] = wi * WS;  // read (harmlessly) by the row copies for absent POIs
-                    if (pyx.x < 0) continue;
-                    const int x0 = pyx.y - g.rx, y0 = pyx.x - g.ry;
-                    const int xa = x0 & ~15;
-                    cs.wbase[grp][wi] = wi * WS + x0 - xa;
-                    tma_load_2d(wwin + wi * WS, (wi & 1) ? &jb.maps->tar : &jb.maps->ref, xa, y0, tbar);
+                mbar_expect_tx(tbar, 0u);  // completes the phase: nothing to load
+                cs.wrs[grp] = g.pitch;
+                for (int p = 0; p < PB; ++p) {
+                    const int2 pyx = cs.spoi[grp][p];
+                    const size_t o = pyx.x < 0 ? 0 : (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
+                    cs.wptr[grp][2 * p] = jb.ref + o;
+                    cs.wptr[grp][2 * p + 1] = jb.tar + o;
                 }
+            }
+        }
+        if (!REF) {
+            // the batch's reference spectra towards L2 (epilogue 2 reads them)
+            // and the reference windows' integer sums
+            if (t == 0) {
+                const int np = min(PB, n_job - b0);
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                                 reinterpret_cast<uint64_t>(jb.fspec + (size_t)b0 * H * FS)),
+                             "r"((uint32_t)(np * H * FS * 4))
+                             : "memory");
+            }
+            if (t < PB && b0 + t < n_job) {
+                const int2 fsum = jb.fsum[b0 + t];
+                cs.wsum[grp][2 * t][0] = fsum.x;
+                cs.wsum[grp][2 * t][1] = fsum.y;
             }
         }
         bool ok = mbar_wait(tbar, tphase);
         tphase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
 
-        // ---- phase L2: windows -> A1 (rows (window, x), K = y), exact FP16;
-        // integer sums per window by segmented warp reductions
+        // ---- phase L2: windows -> A1 (rows (POI, x), K = y), exact FP16: the
+        // reference windows in the per-reference pass, the target windows in
+        // the per-frame pass; integer sums per window by segmented warp
+        // reductions
         for (int rr = t; rr < s.tiles1 * 128; rr += 128) {
-            const int wi = rr / N, x = rr - wi * N;
-            const bool data = wi < 2 * PB && cs.spoi[grp][wi >> 1].x >= 0;
+            const int pw = rr / N, x = rr - pw * N;
+            const int wi = 2 * pw + (REF ? 0 : 1);
+            const bool data = pw < PB && cs.spoi[grp][pw].x >= 0;
             const int rs = cs.wrs[grp];
-            const uint8_t* col = wwin + (data ? cs.wbase[grp][wi] : 0) + x;
+            const uint8_t* col = (data ? cs.wptr[grp][wi] : wwin) + x;
             uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
             const int row = rr & 127;
             int su = 0, sq = 0;
@@ -428,28 +454,30 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             }
             mma_commit(mbar);
         }
-        // per-POI normalisation while the MMAs run: 1/sqrt(nf ng) with
-        // nf = sum (f - mean)^2 = (n sum f^2 - (sum f)^2) / n, exact in integers
+        // per-POI normalisation while the MMAs run: nf = n sum (f - mean)^2 =
+        // n sum f^2 - (sum f)^2, exact in integers (likewise ng); the scale of
+        // the cached reference spectrum is sqrt(n) / sqrt(nf), of the target's
+        // sqrt(n) / sqrt(ng), so the cross power is n / sqrt(nf ng) conj(F) G
         if (t < PB) {
             const int wf = 2 * t, wg = 2 * t + 1;
             const long long numf = (long long)n2 * cs.wsum[grp][wf][1] - (long long)cs.wsum[grp][wf][0] * cs.wsum[grp][wf][0];
             const long long numg = (long long)n2 * cs.wsum[grp][wg][1] - (long long)cs.wsum[grp][wg][0] * cs.wsum[grp][wg][0];
-            const bool dark = b0 + t >= n_job || numf == 0 || numg == 0;
+            const bool dark = b0 + t >= n_job || numf == 0 || (!REF && numg == 0);
             cs.sdark[grp][t] = dark ? 1 : 0;
-            cs.sscale[grp][t] = dark ? 0.f : (float)n2 * rsqrtf((float)numf) * rsqrtf((float)numg);
+            cs.sscale[grp][t] = dark ? 0.f : sqrtf((float)n2) * rsqrtf((float)(REF ? numf : numg));
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
-        // ---- epilogue 1: Y -> A2 (rows (p, ky, w); K = (part, x) with split
+        // ---- epilogue 1: Y -> A2 (rows (p, ky); K = (part, x) with split
         // twiddles, K = (x, part) interleaved with single ones, so that a row's
         // Re and Im of one x are one 32-bit store), FP16.  A2 overwrites A1 (the
         // region is shared), so the K padding x in [N, NP) of the data rows is
         // zeroed first, then the data is written
         {
-            const int rows = 2 * PB * H;
+            const int rows = PB * H;
             if (LO) {
                 const int c0 = N >> 3, nc = NP / 8 - c0;  // 8-column chunks holding padding
                 for (int i = t; i < rows * 2 * nc; i += 128) {
@@ -469,12 +497,11 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         for (int tile = 0; tile < s.tiles1; ++tile) {
             const int rr = tile * 128 + t;
-            const int wi = rr / N, x = rr - wi * N;
-            const bool data = wi < 2 * PB;
-            const int p = wi >> 1, wsel = wi & 1;
-            // rows r2 = (p H + ky) 2 + wsel step by 2: +32 B inside an 8-row
-            // group, +SBO - 96 B when the step crosses into the next group
-            int r2 = (p * H) * 2 + wsel;
+            const int p = rr / N, x = rr - p * N;
+            const bool data = p < PB;
+            // rows r2 = p H + ky step by 1: +16 B inside an 8-row group,
+            // +SBO - 112 B when the step crosses into the next group
+            int r2 = p * H;
             uint8_t* rowp = gbase + s.off_a2 + kmaj144(data ? r2 : 0, 0, 2 * NP);
             const int kre = LO ? (x >> 3) * 144 + (x & 7) * 2 : ((2 * x) >> 3) * 144 + ((2 * x) & 7) * 2;
             const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
@@ -495,8 +522,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                             } else {
                                 *reinterpret_cast<uint32_t*>(rowp + kre) = pack2(dre[j], dim[j]);
                             }
-                            r2 += 2;
-                            rowp += ((r2 & 7) < 2) ? (sbo - 96) : 32;
+                            r2 += 1;
+                            rowp += ((r2 & 7) == 0) ? (sbo - 112) : 16;
                         }
                     }
                 }
@@ -543,60 +570,85 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
-        // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C)
-        {
-            const bool rowv = t < 2 * PB * H;
-            const int p = rowv ? t / (2 * H) : 0;
-            const int ky = rowv ? (t >> 1) % H : 0;
-            const int wsel = t & 1;
-            const float sc = rowv ? cs.sscale[grp][p] : 0.f;
-            const int r3 = p * H + ky;
-            uint8_t* a3 = gbase + s.off_a13;
-            constexpr int HALF = NP / 2;
+        if (REF) {
+            // ---- the reference spectra to the cache: row (p, ky) of FS FP16
+            // pairs (Re, Im), scaled by sqrt(n2) / ||f - mean f|| (zero for a
+            // dark subset), kx >= N zero; then the windows' integer sums
+            const bool rowv = t < PB * H;
+            const int p = rowv ? t / H : 0, ky = rowv ? t - p * H : 0;
+            const bool live = rowv && b0 + p < n_job;
+            const float sc = live ? cs.sscale[grp][p] : 0.f;
+            uint4* dst = reinterpret_cast<uint4*>(jb.fspec + ((size_t)(live ? b0 + p : 0) * H + ky) * FS);
 #pragma unroll
-            for (int c = 0; c < HALF; c += 8) {
-                // columns [c, c+8) and [HALF+c, HALF+c+8) of Re and Im
-                float re_lo[8], re_hi[8], im_lo[8], im_hi[8];
-                tmem_ld8(tm_warp + c, re_lo);
-                tmem_ld8(tm_warp + HALF + c, re_hi);
-                tmem_ld8(tm_warp + NP + c, im_lo);
-                tmem_ld8(tm_warp + NP + HALF + c, im_hi);
+            for (int c = 0; c < NP; c += 8) {
+                float re[8], im[8];
+                tmem_ld8(tm_warp + c, re);
+                tmem_ld8(tm_warp + NP + c, im);
                 tmem_ld_wait();
+                uint32_t w[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) w[i] = (c + i < N) ? pack2(re[i] * sc, im[i] * sc) : 0u;
+                if (live && c < FS) {
+                    dst[c >> 2] = make_uint4(w[0], w[1], w[2], w[3]);
+                    if (c + 8 <= FS) dst[(c >> 2) + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+            }
+            if (t < PB && b0 + t < n_job) jb.fsum[b0 + t] = make_int2(cs.wsum[grp][2 * t][0], cs.wsum[grp][2 * t][1]);
+            tc_fence_before();
+            if (t == 0) cs.snext[grp] = nxt;
+            group_sync(bar_id);
+            continue;
+        }
+
+        // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C),
+        // F the cached reference spectrum (row (POI, ky), read from L2), G the
+        // target's from TMEM; row t of A3 is (p, ky) = t
+        {
+            const bool rowv = t < PB * H;
+            const int p = rowv ? t / H : 0, ky = rowv ? t - p * H : 0;
+            const bool live = rowv && !cs.sdark[grp][p];
+            const float sc = live ? cs.sscale[grp][p] : 0.f;
+            const uint4* frow = reinterpret_cast<const uint4*>(jb.fspec + ((size_t)(live ? b0 + p : 0) * H + ky) * FS);
+            uint8_t* a3 = gbase + s.off_a13;
+#pragma unroll
+            for (int c = 0; c < NP; c += 8) {
+                float gr[8], gi[8];
+                tmem_ld8(tm_warp + c, gr);
+                tmem_ld8(tm_warp + NP + c, gi);
+                uint4 fa = make_uint4(0u, 0u, 0u, 0u), fb = make_uint4(0u, 0u, 0u, 0u);
+                if (live && c < FS) {
+                    fa = __ldg(frow + (c >> 2));
+                    if (c + 8 <= FS) fb = __ldg(frow + (c >> 2) + 1);
+                }
+                tmem_ld_wait();
+                const uint32_t fw[8] = {fa.x, fa.y, fa.z, fa.w, fb.x, fb.y, fb.z, fb.w};
                 float br[8], bi[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const float own_r = wsel ? re_hi[i] : re_lo[i];
-                    const float own_i = wsel ? im_hi[i] : im_lo[i];
-                    const float snd_r = wsel ? re_lo[i] : re_hi[i];
-                    const float snd_i = wsel ? im_lo[i] : im_hi[i];
-                    const float oth_r = __shfl_xor_sync(kFull, snd_r, 1);
-                    const float oth_i = __shfl_xor_sync(kFull, snd_i, 1);
-                    const float fr = wsel ? oth_r : own_r, fi = wsel ? oth_i : own_i;
-                    const float gr = wsel ? own_r : oth_r, gi = wsel ? own_i : oth_i;
-                    const int kx = (wsel ? HALF : 0) + c + i;
-                    float cr = (fr * gr + fi * gi) * sc;
-                    float ci = (fr * gi - fi * gr) * sc;
+                    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&fw[i]));
+                    const int kx = c + i;
+                    float cr = (f.x * gr[i] + f.y * gi[i]) * sc;
+                    float ci = (f.x * gi[i] - f.y * gr[i]) * sc;
                     if (kx >= N || (ky == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
                     br[i] = cr;
                     bi[i] = -ci;  // conj(C) feeds the forward matrices of stage 3
                 }
                 if (rowv) {
-                    const int k0 = (wsel ? HALF : 0) + c;
                     uint4 q;
                     if (LO) {  // K = (part, kx)
                         q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
                         q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, k0, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, c, 2 * NP)) = q;
                         q.x = pack2(bi[0], bi[1]); q.y = pack2(bi[2], bi[3]);
                         q.z = pack2(bi[4], bi[5]); q.w = pack2(bi[6], bi[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, NP + k0, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, NP + c, 2 * NP)) = q;
                     } else {  // K = (kx, part) interleaved
                         q.x = pack2(br[0], bi[0]); q.y = pack2(br[1], bi[1]);
                         q.z = pack2(br[2], bi[2]); q.w = pack2(br[3], bi[3]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, 2 * k0, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c, 2 * NP)) = q;
                         q.x = pack2(br[4], bi[4]); q.y = pack2(br[5], bi[5]);
                         q.z = pack2(br[6], bi[6]); q.w = pack2(br[7], bi[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(r3, 2 * k0 + 8, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c + 8, 2 * NP)) = q;
                     }
                 }
             }
@@ -694,12 +746,14 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         // ---- stage 4: c[(p,x)][y] = A4 * B4
         if (t == 0) {
             tc_fence_after();
-            for (int kk = 0; kk < K4 / 16; ++kk) {
-                const uint64_t a = sdesc(gaddr + s.off_a4 + kk * 288, 144, 18 * K4);
-                const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
-                const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
-                mma_f16(tm, a, bh, idesc_f16(NP, false), kk > 0);
-                if (LO) mma_f16(tm, a, bl, idesc_f16(NP, false), 1);
+            for (int tile = 0; tile < s.tiles4; ++tile) {
+                for (int kk = 0; kk < K4 / 16; ++kk) {
+                    const uint64_t a = sdesc(gaddr + s.off_a4 + tile * (16 * 18 * K4) + kk * 288, 144, 18 * K4);
+                    const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
+                    const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
+                    mma_f16(tm + tile * NP, a, bh, idesc_f16(NP, false), kk > 0);
+                    if (LO) mma_f16(tm + tile * NP, a, bl, idesc_f16(NP, false), 1);
+                }
             }
             mma_commit(mbar);
         }
@@ -710,72 +764,107 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
         // (scratch in the shared operand region, which stage 4 has finished
-        // reading; the surface stays in TMEM and is read twice in chunks)
-        const bool rowv = t < PB * N;
-        const int p4 = rowv ? t / N : 0, x4 = rowv ? t - (t / N) * N : 0;
-        const bool live = rowv && !cs.sdark[grp][p4];
+        // reading; the surface stays in TMEM and is read twice in chunks).
+        // Thread t holds surface row R = 128 k + t of tile k (R = p N + x:
+        // POI p, column x, the values over y in the row's TMEM columns)
+        const int ntile = s.tiles4;
         if (t < kCandChunk) ps->candS[t] = 0;
-        // approximate peak value per POI: each thread's maximum over the
-        // surface rows y of its column x4, then a segmented warp reduction and
-        // one shared atomic per warp segment
-        float bv = -3.4e38f;
+        // approximate peak value per POI: each thread's maximum over y of its
+        // rows, then a segmented warp reduction and one shared atomic per warp
+        // segment, tile by tile
+        float bvk[2] = {-3.4e38f, -3.4e38f};
 #pragma unroll
-        for (int y0 = 0; y0 < NP; y0 += 8) {
-            if (y0 >= N) break;  // padding columns
-            float cv[8];
-            tmem_ld8(tm_warp + y0, cv);
-            tmem_ld_wait();
+        for (int k = 0; k < 2; ++k) {
+            if (k >= ntile) break;
+            const int R = 128 * k + t;
+            const bool rowv = R < PB * N;
+            const int p4 = rowv ? R / N : 0;
+            const bool live = rowv && !cs.sdark[grp][p4];
+            float bv = -3.4e38f;
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (live && y0 + j < N && cv[j] > bv) bv = cv[j];
+            for (int y0 = 0; y0 < NP; y0 += 8) {
+                if (y0 >= N) break;  // padding columns
+                float cv[8];
+                tmem_ld8(tm_warp + k * NP + y0, cv);
+                tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (live && y0 + j < N && cv[j] > bv) bv = cv[j];
+            }
+            const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
+            const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
+            if (live && lane == __ffs(seg) - 1) atomicMax(&cs.smaxv[grp][p4], ov);
+            bvk[k] = bv;
         }
-        const unsigned seg = __match_any_sync(kFull, live ? p4 : -1);
-        const uint32_t ov = __reduce_max_sync(seg, f32_ord(bv));
-        if (live && lane == __ffs(seg) - 1) atomicMax(&cs.smaxv[grp][p4], ov);
         group_sync(bar_id);
         // candidates: every shift within kCandZncc (ZNCC units; the surface is
         // N^2 ZNCC) of the approximate peak, the peak itself included, as one
-        // bit per surface row y of this thread's column; a warp with no such
-        // column skips the second read
-        uint64_t cmask = 0;
-        {
+        // bit per y of each row; a warp with no such row skips the second read
+        uint64_t cmk[2] = {0ull, 0ull};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (k >= ntile) break;
+            const int R = 128 * k + t;
+            const bool rowv = R < PB * N;
+            const int p4 = rowv ? R / N : 0;
+            const bool live = rowv && !cs.sdark[grp][p4];
             const float th = live ? f32_unord(cs.smaxv[grp][p4]) - kCandZncc * (float)n2 : 3.4e38f;
-            if (__any_sync(kFull, live && bv >= th)) {
+            if (__any_sync(kFull, live && bvk[k] >= th)) {
+                uint64_t m = 0ull;
 #pragma unroll
                 for (int y0 = 0; y0 < NP; y0 += 8) {
                     if (y0 >= N) break;  // padding columns
                     float cv[8];
-                    tmem_ld8(tm_warp + y0, cv);
+                    tmem_ld8(tm_warp + k * NP + y0, cv);
                     tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (live && y0 + j < N && cv[j] >= th) cmask |= 1ull << (y0 + j);
+                        if (live && y0 + j < N && cv[j] >= th) m |= 1ull << (y0 + j);
                 }
+                cmk[k] = m;
             }
         }
         tc_fence_before();
-        // candidate slots in a fixed order (thread, then row) by a group-wide
-        // exclusive scan of the per-thread counts; a POI's threads are
+        // candidate slots in row order (R, then y) by group-wide exclusive
+        // scans of the per-row counts, tile 0 first; a POI's rows are
         // consecutive, so POI p owns the slots [cbase[p], cend[p])
-        const int cnt = __popcll(cmask);
-        int incl = cnt;
+        int exk[2] = {0, 0}, cnk[2] = {0, 0}, ink[2] = {0, 0};
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int up = __shfl_up_sync(kFull, incl, o);
-            if (lane >= o) incl += up;
+        for (int k = 0; k < 2; ++k) {
+            cnk[k] = __popcll(cmk[k]);
+            int incl = cnk[k];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int up = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += up;
+            }
+            ink[k] = incl;
+            if (lane == 31) cs.wtot[grp][k][warp] = incl;
         }
-        if (lane == 31) cs.wtot[grp][warp] = incl;
         group_sync(bar_id);
-        int wpre = 0, total = 0;
+        int total = 0;
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            const int tw = cs.wtot[grp][w];
-            wpre += (w < warp) ? tw : 0;
-            total += tw;
+        for (int k = 0; k < 2; ++k) {
+            int wpre = 0, tk = 0;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const int tw = cs.wtot[grp][k][w];
+                wpre += (w < warp) ? tw : 0;
+                tk += tw;
+            }
+            exk[k] = total + wpre + ink[k] - cnk[k];
+            total += tk;
         }
-        const int excl = wpre + incl - cnt;
-        if (rowv && x4 == 0) cs.cbase[grp][p4] = excl;
-        if (rowv && x4 == N - 1) cs.cend[grp][p4] = excl + cnt;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            if (k >= ntile) break;
+            const int R = 128 * k + t;
+            if (R < PB * N) {
+                const int p4 = R / N, x4 = R - p4 * N;
+                if (x4 == 0) cs.cbase[grp][p4] = exk[k];
+                if (x4 == N - 1) cs.cend[grp][p4] = exk[k] + cnk[k];
+            }
+        }
         // exact integer correlation of every candidate, kCandChunk slots at a
         // time (any number of candidates: a broad or periodic surface only
         // takes more chunks), read from the staged windows: tasks (slot, row)
@@ -791,12 +880,17 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 group_sync(bar_id);  // the previous chunk's sums have been read
                 if (t < kCandChunk) ps->candS[t] = 0;
             }
-            if (cnt > 0 && excl < lo + kCandChunk && excl + cnt > lo) {
-                uint64_t m = cmask;
-                for (int k = excl; m != 0; ++k) {
-                    const int y = __ffsll((long long)m) - 1;
-                    m &= m - 1;
-                    if (k >= lo && k < lo + kCandChunk) ps->cand[k - lo] = (p4 << 16) | (y * N + x4);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (cnk[k] > 0 && exk[k] < lo + kCandChunk && exk[k] + cnk[k] > lo) {
+                    const int R = 128 * k + t;
+                    const int p4 = R / N, x4 = R - p4 * N;
+                    uint64_t m = cmk[k];
+                    for (int q = exk[k]; m != 0; ++q) {
+                        const int y = __ffsll((long long)m) - 1;
+                        m &= m - 1;
+                        if (q >= lo && q < lo + kCandChunk) ps->cand[q - lo] = (p4 << 16) | (y * N + x4);
+                    }
                 }
             }
             group_sync(bar_id);
@@ -813,8 +907,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                     const int ky = idx / N, kx = idx - ky * N;
                     int yy = y + ky;
                     if (yy >= N) yy -= N;
-                    const uint8_t* fb = wwin + cs.wbase[grp][2 * p] + y * rs;
-                    const uint8_t* gb = wwin + cs.wbase[grp][2 * p + 1] + yy * rs;
+                    const uint8_t* fb = cs.wptr[grp][2 * p] + y * rs;
+                    const uint8_t* gb = cs.wptr[grp][2 * p + 1] + yy * rs;
                     const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
                     unsigned acc = 0;
                     int j = rot;
@@ -919,7 +1013,7 @@ __device__ __forceinline__ void tc_teardown(TcCta& cs, uint32_t tmem_cols) {
 // One window size: blockDim = 128 * s.groups (up to four).  The first batch
 // of every group by position, then the next free one from the launch-wide
 // counter, which evens out the groups' finishing times.
-template <int NP, int HP, bool MULTI, bool LO>
+template <int NP, int HP, bool MULTI, bool LO, bool REF>
 __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
                                                                  const uint4* __restrict__ tables, unsigned* err,
                                                                  int* work) {
@@ -931,7 +1025,7 @@ __global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_c
     if ((threadIdx.x & 127) == 0) tc_acquire_maps(J, 0, J.njobs);
     if (!tc_setup(cs, sm, s.groups, tmem_cols, err)) return;
     uint32_t phase = 0, tphase = 0;
-    tc_group_batches<NP, HP, MULTI, LO>(J, s, 0, J.njobs, J.nbatch, blockIdx.x * s.groups + grp, work,
+    tc_group_batches<NP, HP, MULTI, LO, REF>(J, s, 0, J.njobs, J.nbatch, blockIdx.x * s.groups + grp, work,
                                         gridDim.x * s.groups, err, cs, sm, phase, tphase);
     tc_teardown(cs, tmem_cols);
 }
@@ -951,9 +1045,10 @@ __device__ __forceinline__ bool tc_run_segment(const TcJobs& J, const TcSeg& sg,
     const int first = cs.snext[grp];
 #define TWDIC_TC_SEG(K)                                                                                     \
     case K:                                                                                                  \
-        return tc_group_batches<kTcShapes[K][0], kTcShapes[K][1], true, LO>(J, sg.s, sg.job_lo, sg.job_hi,   \
-                                                                            sg.nbatch, first, counter, 0,    \
-                                                                            err, cs, sm, phase, tphase);
+        return tc_group_batches<kTcShapes[K][0], kTcShapes[K][1], true, LO, false>(J, sg.s, sg.job_lo,       \
+                                                                            sg.job_hi, sg.nbatch, first,     \
+                                                                            counter, 0, err, cs, sm, phase,  \
+                                                                            tphase);
     switch (sg.shape) {
         TWDIC_TC_SEG(0)
         TWDIC_TC_SEG(1)
@@ -1025,18 +1120,22 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     s.H = N / 2 + 1;
     s.HP = round_up(s.H, 8);
     s.NP = round_up(N, 16);
-    int pb = 256 / (2 * N);
-    pb = std::min(pb, 64 / s.H);
-    pb = std::min(pb, 128 / N);
-    pb = std::min(pb, kMaxPB);
+    // POIs per batch: the (POI, ky) rows of stages 2 and 3 fill one 128-row
+    // tile; the (POI, x) rows of stages 1 and 4 take up to two, each with its
+    // own TMEM columns (2 HP at stage 1, NP at stage 4) within the group's 128
+    int pb = std::min(128 / s.H, kMaxPB);
     if (tune.pois_per_group > 0) pb = std::min(pb, tune.pois_per_group);  // tuned batch size
-    if (pb < 1 || 2 * s.HP > 80) return false;
+    int tiles = 0;
+    for (; pb >= 1; --pb) {
+        tiles = (pb * N + 127) / 128;
+        if (tiles <= 2 && tiles * 2 * s.HP <= kTmemCols && tiles * s.NP <= kTmemCols) break;
+    }
+    if (pb < 1 || 2 * s.NP > kTmemCols || 2 * s.HP > 80) return false;
     s.PB = pb;
-    s.tiles1 = (pb * 2 * N + 127) / 128;
+    s.tiles1 = tiles;
+    s.tiles4 = tiles;
     s.K4 = 2 * s.HP;
-    // tensor-memory columns used by the stages must fit the allocation
-    if (s.tiles1 * 2 * s.HP > kTmemCols || 2 * s.NP > kTmemCols || s.tiles1 > 2) return false;
-    if (2 * pb * s.H > 128 || pb * N > 128) return false;
+    s.FS = round_up(N, 4);
     const int K1 = s.NP, N1 = 2 * s.HP, NP = s.NP, K4 = s.K4;
     s.lo = tune.twiddle_lo ? 1 : 0;
     int o = 0;
@@ -1058,20 +1157,25 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     o = s.tab_bytes;
     // per-group regions: one operand region shared by A1, A2, A3, A4 and the
     // peak scratch, then the windows
-    s.BW = round_up(N + 15, 16);  // TMA box width: window + up to 15 bytes of x alignment
     s.NW4 = (N + 3) / 4;
-    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = 16 * 18 * K4;
+    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = s.tiles4 * 16 * 18 * K4;
     const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
                                 128);
     s.off_a13 = 0;
     s.off_a2 = 0;
     s.off_a4 = 0;
-    // window stride: TMA destinations are 128-byte aligned, and 16 spare bytes
-    // keep the 8-byte reads of ld_unaligned_p inside the window
-    s.WS = round_up(N * s.BW + 16, 128);
+    // windows: the batch's two one-row boxes (PB windows at the grid step
+    // apart, x aligned down to 16 bytes, at most 256 bytes wide), the target's
+    // 128-byte aligned; 16 spare bytes keep the 8-byte reads of
+    // ld_unaligned_p inside the region
+    s.uw = round_up((pb - 1) * g.grid_x + N + 15, 16);
+    if (g.grid_x <= 0 || s.uw > 256) s.uw = 0;
+    s.utoff = round_up(N * s.uw, 128);
+    s.win_bytes = round_up(s.utoff + N * s.uw + 16, 128);
     s.off_win = region;
-    s.group_bytes = round_up(region + 2 * pb * s.WS, 1024);
-    const int limit = 225 * 1024;
+    s.group_bytes = round_up(region + s.win_bytes, 1024);
+    // 227 KB per CTA, less the static state (the dynamic part starts 1024-byte aligned)
+    const int limit = 227 * 1024 - round_up((int)sizeof(TcCta), 1024);
     s.groups = std::min(kMaxGroups, (limit - o) / s.group_bytes);
     if (tune.groups > 0) s.groups = std::min(s.groups, tune.groups);  // tuned group count
     if (s.groups < 1) return false;
@@ -1184,13 +1288,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 8-bit image as a 2D tensor (x = column, y = row) read in boxes of
-// BW x N bytes; reads outside the image are zero-filled
-bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape& s, int box_w = 0) {
+// box_w x N bytes; reads outside the image are zero-filled
+bool image_map(CUtensorMap* m, const Geom& g, const uint8_t* img, const TcShape& s, int box_w) {
     auto fn = encode_fn();
     if (!fn) return false;
     const cuuint64_t dims[2] = {(cuuint64_t)g.img_w, (cuuint64_t)g.img_h};
     const cuuint64_t strides[1] = {(cuuint64_t)g.pitch};
-    const cuuint32_t box[2] = {(cuuint32_t)(box_w > 0 ? box_w : s.BW), (cuuint32_t)s.N};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)s.N};
     const cuuint32_t estr[2] = {1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(img), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1204,7 +1308,7 @@ static_assert(sizeof(TcMaps) <= kTcMapsBytes, "TcMaps larger than its buffer");
 uint64_t fftcc_tc_maps_key(const Geom& g, const FftccTune& tune) {
     TcShape s;
     if (!make_shape(g, tune, s)) return 0;
-    return 1ull | ((uint64_t)s.PB << 8) | ((uint64_t)s.N << 16) | ((uint64_t)s.BW << 24) | ((uint64_t)s.WS << 32);
+    return 1ull | ((uint64_t)s.PB << 8) | ((uint64_t)s.N << 16) | ((uint64_t)s.uw << 24) | ((uint64_t)s.utoff << 40);
 }
 
 bool fftcc_tc_encode_maps(const Geom& g, const uint8_t* ref, const uint8_t* tar, const FftccTune& tune,
@@ -1215,19 +1319,11 @@ bool fftcc_tc_encode_maps(const Geom& g, const uint8_t* ref, const uint8_t* tar,
         (reinterpret_cast<uintptr_t>(host_buf) & 127))
         return false;
     TcMaps* m = new (host_buf) TcMaps();
-    if (!image_map(&m->ref, g, ref, s) || !image_map(&m->tar, g, tar, s)) return false;
-    // one box per image for a batch on one POI row: PB windows at the grid
-    // step apart, x aligned down to 16 bytes; used when both boxes (and 8
-    // bytes of read slack) fit the window region and the box width is at
-    // most 256 (the TMA box limit)
-    int uw = round_up((s.PB - 1) * g.grid_x + s.N + 15, 16);
-    int utoff = round_up(s.N * uw, 128);
-    if (s.PB < 2 || g.grid_x <= 0 || uw > 256 || utoff + s.N * uw + 16 > 2 * s.PB * s.WS ||
-        !image_map(&m->ref_u, g, ref, s, uw) || !image_map(&m->tar_u, g, tar, s, uw)) {
-        uw = 0;
+    int uw = s.uw, utoff = s.utoff;
+    if (uw > 0 && (!image_map(&m->ref_u, g, ref, s, uw) || !image_map(&m->tar_u, g, tar, s, uw))) return false;
+    if (uw == 0) {
         utoff = 0;
-        m->ref_u = m->ref;  // never read
-        m->tar_u = m->tar;
+        std::memset(m, 0, sizeof(TcMaps));  // never read
     }
     info->key = fftcc_tc_maps_key(g, tune);
     info->uw = uw;
@@ -1239,12 +1335,21 @@ namespace {
 
 // A job of the kernels' table from a launcher job, whose maps must have been
 // encoded for this launch's shape.
-bool fill_job(TcJob& o, const FftccJob& in, const FftccTune& tune) {
+bool fill_job(TcJob& o, const FftccJob& in, const FftccTune& tune, const TcShape& launch) {
     if (!in.maps || (reinterpret_cast<uintptr_t>(in.maps) & 127) || in.map_key != fftcc_tc_maps_key(in.g, tune))
         return false;
+    if (!in.fspec || !in.fsum) return false;
     o.maps = static_cast<const TcMaps*>(in.maps);
+    o.fspec = in.fspec;
+    o.fsum = in.fsum;
+    o.ref = in.ref;
+    o.tar = in.tar;
     o.uw = in.uw;
     o.utoff = in.utoff;
+    // the one-row boxes only where they fit this launch's window region
+    // (a job of a mixed-size launch may have another grid step than the one
+    // the segment's shape was made for); otherwise the windows come from the images
+    if (o.uw > 0 && (o.utoff + launch.N * o.uw + 16 > launch.win_bytes || in.g.rx * 2 != launch.N)) o.uw = 0;
     o.g = in.g;
     o.poi = in.poi;
     o.u = in.u;
@@ -1293,7 +1398,7 @@ cudaError_t launch_segments(const FftccJob* jobs, int njobs, const FftccTune& tu
         TcSeg& sg = S->seg[S->nseg - 1];
         if (in.g.rx != in.g.ry) return cudaErrorInvalidValue;
         TcJob& o = J->job[k];
-        if (!fill_job(o, in, tune)) return cudaErrorInvalidValue;
+        if (!fill_job(o, in, tune, sg.s)) return cudaErrorInvalidValue;
         o.batch_begin = sg.nbatch;
         const int nb = (in.n + sg.s.PB - 1) / sg.s.PB;
         sg.nbatch += nb;
@@ -1327,19 +1432,25 @@ cudaError_t launch_segments(const FftccJob* jobs, int njobs, const FftccTune& tu
 }  // namespace
 
 cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTune& tune, unsigned* err, int* work,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, bool ref) {
+    // the per-reference pass runs with single twiddles whatever the tuning
+    // (its spectra are rounded to FP16 when cached)
+    FftccTune tn = tune;
+    if (ref) tn.twiddle_lo = 0;
     if (njobs < 1 || njobs > kMaxTcJobs) return cudaErrorInvalidValue;
     for (int j = 1; j < njobs; ++j)
-        if (jobs[j].g.rx != jobs[0].g.rx || jobs[j].g.ry != jobs[0].g.ry)
+        if (jobs[j].g.rx != jobs[0].g.rx || jobs[j].g.ry != jobs[0].g.ry) {
+            if (ref) return cudaErrorInvalidValue;  // the per-reference pass runs one window size per launch
             return launch_segments(jobs, njobs, tune, err, work, st);  // several window sizes
+        }
     TcShape s;
-    if (!make_shape(jobs[0].g, tune, s)) return cudaErrorNotSupported;
+    if (!make_shape(jobs[0].g, tn, s)) return cudaErrorNotSupported;
     std::unique_ptr<TcJobs> J(new TcJobs());
     J->njobs = njobs;
     int nb = 0;
     for (int j = 0; j < njobs; ++j) {
         TcJob& o = J->job[j];
-        if (!fill_job(o, jobs[j], tune)) return cudaErrorInvalidValue;
+        if (!fill_job(o, jobs[j], tn, s)) return cudaErrorInvalidValue;
         o.batch_begin = nb;
         nb += (jobs[j].n + s.PB - 1) / s.PB;
     }
@@ -1355,12 +1466,15 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     void (*kern)(const TcJobs, TcShape, const uint4*, unsigned*, int*) = nullptr;
     const bool multi = njobs > 1;
-#define TWDIC_TC_CASE(NPV, HPV)                                                                      \
-    case NPV * 100 + HPV:                                                                            \
-        if (s.lo)                                                                                    \
-            kern = multi ? k_fftcc_tc<NPV, HPV, true, true> : k_fftcc_tc<NPV, HPV, false, true>;     \
-        else                                                                                         \
-            kern = multi ? k_fftcc_tc<NPV, HPV, true, false> : k_fftcc_tc<NPV, HPV, false, false>;   \
+#define TWDIC_TC_CASE(NPV, HPV)                                                                          \
+    case NPV * 100 + HPV:                                                                                \
+        if (ref)                                                                                         \
+            kern = multi ? k_fftcc_tc<NPV, HPV, true, false, true> : k_fftcc_tc<NPV, HPV, false, false, true>; \
+        else if (s.lo)                                                                                   \
+            kern = multi ? k_fftcc_tc<NPV, HPV, true, true, false> : k_fftcc_tc<NPV, HPV, false, true, false>; \
+        else                                                                                             \
+            kern = multi ? k_fftcc_tc<NPV, HPV, true, false, false>                                      \
+                         : k_fftcc_tc<NPV, HPV, false, false, false>;                                    \
         break;
     switch (s.NP * 100 + s.HP) {
         TWDIC_TC_CASE(16, 8)
@@ -1390,12 +1504,17 @@ cudaError_t launch_fftcc_tc_jobs(const FftccJob* jobs, int njobs, const FftccTun
     return cudaGetLastError();
 }
 
-cudaError_t launch_fftcc_tc(const Geom& g, const void* maps, uint64_t map_key, int uw, int utoff, const int2* poi,
-                            int n, float* u, float* v, float* zncc, uint8_t* status, unsigned* err, int* work,
-                            const FftccTune& tune, cudaStream_t st) {
+cudaError_t launch_fftcc_tc(const Geom& g, const uint8_t* ref_img, const uint8_t* tar_img, const void* maps,
+                            uint64_t map_key, int uw, int utoff, uint32_t* fspec, int2* fsum, const int2* poi, int n, float* u, float* v, float* zncc, uint8_t* status,
+                            unsigned* err, int* work, const FftccTune& tune, cudaStream_t st, bool ref) {
     if (n <= 0) return cudaSuccess;
-    FftccJob job{g, maps, map_key, uw, utoff, poi, n, u, v, zncc, status};
-    return launch_fftcc_tc_jobs(&job, 1, tune, err, work, st);
+    FftccJob job{g, maps, map_key, uw, utoff, ref_img, tar_img, fspec, fsum, poi, n, u, v, zncc, status};
+    return launch_fftcc_tc_jobs(&job, 1, tune, err, work, st, ref);
+}
+
+size_t fftcc_tc_spectrum_bytes(const Geom& g, int n) {
+    const int N = 2 * g.rx;
+    return (size_t)n * (N / 2 + 1) * round_up(N, 4) * 4;
 }
 
 }  // namespace twdic

@@ -3,12 +3,14 @@
 //
 // For an N x N window (N = 2r, no padding of the data: the correlation stays
 // circular as in the reference), with w = exp(-2 pi i / N):
-//   stage 1  Y[ky][x]  = sum_y f[y][x] w^(ky y)          ky <= N/2 (real input)
-//   stage 2  F[ky][kx] = sum_x Y[ky][x] w^(kx x)
+//   stage 1  Y[kx][y]  = sum_x f[y][x] w^(kx x)          kx <= N/2 (real input)
+//   stage 2  F[kx][ky] = sum_y Y[kx][y] w^(ky y)
 //   cross    C = conj(F) G / (||f-mean|| ||g-mean||), C[0][0] = 0 (mean removal)
-//   stage 3  conj(Z[ky][x]) = sum_kx conj(C[ky][kx]) w^(kx x)   (the forward
+//   stage 3  conj(Z[kx][v]) = sum_ky conj(C[kx][ky]) w^(ky v)   (the forward
 //            matrices serve the inverse transform through the conjugate)
-//   stage 4  c[y][x]  = sum_ky weight(ky) Re(Z[ky][x] w^(-ky y))  (c2r)
+//   stage 4  c[v][u]  = sum_kx weight(kx) Re(Z[kx][v] w^(-kx u))  (c2r)
+// so that c[v][u] is the correlation at the shift (u, v) = (x, y).  Stage 1
+// runs along the window rows, which are contiguous in memory.
 // Every stage is D[128 x n] += A[128 x k] B[k x n] with the data as A
 // (rows = window rows / spectrum rows of several POIs, K-major in shared
 // memory) and constant twiddle matrices as B (K-major), FP16 operands, FP32
@@ -21,9 +23,13 @@
 // correlation), with the reference's first-maximum rule.
 // ZNCC is the quotient of the exact integer sums, evaluated in FP32.
 //
-// One CTA of 128 threads (one warpgroup) per SM slot, persistent over POI
-// batches; thread 0 issues the MMAs, completion is signalled through an
-// mbarrier (bounded wait), the epilogues read TMEM with tcgen05.ld.
+// Up to four groups of 128 threads (one warpgroup each, 128 TMEM columns
+// each) per CTA, one CTA per SM, persistent over batches of POIs; thread 0
+// of a group issues its MMAs, completion is signalled through an mbarrier
+// (bounded wait), the epilogues read TMEM with tcgen05.ld.  The reference
+// windows' spectra are computed once per reference (the per-reference pass)
+// and read back by the per-frame pass, which transforms the target windows
+// only.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
@@ -83,6 +89,13 @@ struct TcShape {
     int off_w2re, off_w2im;
     // per-group operand regions, relative to the group's base
     int off_a13, off_a2, off_a4, off_win, group_bytes;
+    // row-contiguous operands A2, A4 (row r at 16 r, 8-column chunk c at c lbo):
+    // chunk strides, the chunks without data that the MMAs read [z lo, z hi)
+    int lbo2, lbo4, z2lo, z2hi, z4lo, z4hi;
+    int z2part, z4part;  // the first zeroed chunk holds data too
+    int z4early;         // A4's zeroed chunks lie past A3: zeroed in epilogue 2
+    int ks2;  // K steps (16) of stages 2 and 3: the data columns only
+    int k3w;  // K width of A3's layout
     int smem_bytes;
 };
 
@@ -134,9 +147,6 @@ struct PeakScratch {
 
 __host__ __device__ __forceinline__ int kmaj(int r, int k, int K) {  // LBO 128 B, SBO 16*K B
     return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
-}
-__host__ __device__ __forceinline__ int kmaj144(int r, int k, int K) {  // LBO 144 B, SBO 18*K B
-    return (r >> 3) * (K * 18) + (k >> 3) * 144 + (r & 7) * 16 + (k & 7) * 2;
 }
 
 // ------------------------------------------------------------ PTX glue ----
@@ -216,6 +226,14 @@ __device__ __forceinline__ int group_sync_or(int id, int v) {
     return r;
 }
 
+// FP16 pair of two bytes of w (PRMT selector 0x4140: bytes 0, 1; 0x4342:
+// bytes 2, 3): the halves 0x64bb are 1024 + bb, less 1024 exactly
+__device__ __forceinline__ uint32_t bytes_h2(uint32_t w, uint32_t sel) {
+    const uint32_t b = __byte_perm(w, 0x64646464u, sel);
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(b), "r"(0x64006400u));
+    return r;
+}
 // 4 bytes from any shared-memory byte pointer derived from the dynamic
 // shared buffer (two aligned words, funnel shift)
 __device__ __forceinline__ uint32_t ld_unaligned_p(const uint8_t* a) {
@@ -300,6 +318,14 @@ __device__ __forceinline__ void tc_load_tables(uint8_t* sm, const uint4* __restr
 // whose spectra (scaled by sqrt(n2) / ||f - mean f||, FP16 pairs) and integer
 // sums go to the job's cache.  Otherwise the per-frame pass: stages 1 and 2 of
 // the target windows only, the reference spectra read from that cache.
+// Zeros in the chunks of A4 (rows [0, rows)) that hold stage-4 K columns
+// past the data.
+__device__ __forceinline__ void zero_a4_padding(uint8_t* a4, const TcShape& s, int rows, int t) {
+    for (int c = s.z4lo; c < s.z4hi; ++c)
+        for (int r = t; r < rows; r += 128)
+            *reinterpret_cast<uint4*>(a4 + c * s.lbo4 + r * 16) = make_uint4(0, 0, 0, 0);
+}
+
 template <int NP, int HP, bool MULTI, bool LO, bool REF>
 __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape& s, int job_lo, int job_hi,
                                                  int nbatch, int first, int* counter, int counter_base,
@@ -400,37 +426,53 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         tphase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
 
-        // ---- phase L2: windows -> A1 (rows (POI, x), K = y), exact FP16: the
-        // reference windows in the per-reference pass, the target windows in
-        // the per-frame pass; integer sums per window by segmented warp
-        // reductions
+        // ---- phase L2: windows -> A1, exact FP16: row (POI, window row y),
+        // K = window column x; the reference windows in the per-reference
+        // pass, the target windows in the per-frame pass.  A thread reads its
+        // row as aligned 32-bit words (one funnel shift per word for the
+        // window's byte offset), makes FP16 of the bytes by PRMT (the half
+        // 0x64bb is 1024 + bb) and one packed subtraction, and sums the bytes
+        // and their squares by DP4A; integer sums per window by segmented
+        // warp reductions.  Rows past the batch's windows are not written
+        // (the rows of D1 they give are never read).
         for (int rr = t; rr < s.tiles1 * 128; rr += 128) {
-            const int pw = rr / N, x = rr - pw * N;
+            const int pw = rr / N, y = rr - pw * N;
             const int wi = 2 * pw + (REF ? 0 : 1);
-            const bool data = pw < PB && cs.spoi[grp][pw].x >= 0;
-            const int rs = cs.wrs[grp];
-            const uint8_t* col = (data ? cs.wptr[grp][wi] : wwin) + x;
-            uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2);
-            const int row = rr & 127;
-            int su = 0, sq = 0;
+            const bool inb = pw < PB;
+            const bool data = inb && cs.spoi[grp][pw].x >= 0;
+            unsigned su = 0u, sq = 0u;
+            if (inb) {
+                const uint8_t* src = data ? cs.wptr[grp][wi] + y * cs.wrs[grp] : wwin;
+                const unsigned sh = 8u * (unsigned)(reinterpret_cast<uintptr_t>(src) & 3);
+                const uint32_t* ws = reinterpret_cast<const uint32_t*>(src - (sh >> 3));
+                uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2) + kmaj(rr & 127, 0, K1);
+                uint32_t lo = data ? ws[0] : 0u;
 #pragma unroll
-            for (int c = 0; c < K1 / 8; ++c) {
-                float f[8];
+                for (int c = 0; c < K1 / 8; ++c) {
+                    uint32_t w[2];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int y = c * 8 + j;
-                    const int val = (data && y < N) ? (int)col[y * rs] : 0;
-                    su += val;
-                    sq += val * val;
-                    f[j] = (float)val;
+                    for (int h = 0; h < 2; ++h) {
+                        const int j = 2 * c + h;  // bytes x = 4 j .. 4 j + 3
+                        w[h] = 0u;
+                        if (data && 4 * j < N) {
+                            const uint32_t hi = ws[j + 1];
+                            w[h] = __funnelshift_r(lo, hi, sh);
+                            lo = hi;
+                            if (4 * j + 4 > N) w[h] &= 0xffffffffu >> (8 * (4 * j + 4 - N));
+                        }
+                    }
+                    su = __dp4a(w[0], 0x01010101u, su);
+                    su = __dp4a(w[1], 0x01010101u, su);
+                    sq = __dp4a(w[0], w[0], sq);
+                    sq = __dp4a(w[1], w[1], sq);
+                    *reinterpret_cast<uint4*>(a1 + c * 128) =
+                        make_uint4(bytes_h2(w[0], 0x4140u), bytes_h2(w[0], 0x4342u), bytes_h2(w[1], 0x4140u),
+                                   bytes_h2(w[1], 0x4342u));
                 }
-                uint4 q;
-                q.x = pack2(f[0], f[1]); q.y = pack2(f[2], f[3]); q.z = pack2(f[4], f[5]); q.w = pack2(f[6], f[7]);
-                *reinterpret_cast<uint4*>(a1 + kmaj(row, c * 8, K1)) = q;
             }
             const int key = data ? wi : -1;
             const unsigned seg = __match_any_sync(kFull, key);
-            const int gs = __reduce_add_sync(seg, su), gq = __reduce_add_sync(seg, sq);
+            const int gs = __reduce_add_sync(seg, (int)su), gq = __reduce_add_sync(seg, (int)sq);
             if (data && lane == __ffs(seg) - 1) {
                 atomicAdd(&cs.wsum[grp][wi][0], gs);
                 atomicAdd(&cs.wsum[grp][wi][1], gq);
@@ -439,7 +481,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         fence_async_smem();
         group_sync(bar_id);
 
-        // ---- stage 1: D1[(w,x)][(part,ky)] = A1 * B1
+        // ---- stage 1: D1[(w,y)][(part,kx)] = A1 * B1 (the real DFT along x)
         if (t == 0) {
             tc_fence_after();
             for (int tile = 0; tile < s.tiles1; ++tile) {
@@ -471,59 +513,49 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
-        // ---- epilogue 1: Y -> A2 (rows (p, ky); K = (part, x) with split
-        // twiddles, K = (x, part) interleaved with single ones, so that a row's
-        // Re and Im of one x are one 32-bit store), FP16.  A2 overwrites A1 (the
-        // region is shared), so the K padding x in [N, NP) of the data rows is
-        // zeroed first, then the data is written
+        // ---- epilogue 1: D1 -> A2 (rows (p, kx); K = (y, part) interleaved
+        // with single twiddles, so that a row's Re and Im of one y are one
+        // 32-bit store; K = (part, y) with split ones), FP16.  A2 is
+        // row-contiguous per 8-column chunk: a thread's rows (p, kx),
+        // kx = 0 .. H-1, are 16 bytes apart.  Columns of the stage-2 K past
+        // the data are zero: the chunks they lie in are zeroed row by row
+        // first (a chunk holding data too, only when N % 4 = 2, then waits
+        // for the zeros before its data).  A2 overwrites A1 (the region is
+        // shared; stage 1 has completed).
         {
+            const int LB2 = s.lbo2;
+            uint8_t* a2 = gbase + s.off_a2;
             const int rows = PB * H;
-            if (LO) {
-                const int c0 = N >> 3, nc = NP / 8 - c0;  // 8-column chunks holding padding
-                for (int i = t; i < rows * 2 * nc; i += 128) {
-                    const int r2 = i / (2 * nc), rem = i - r2 * (2 * nc);
-                    const int part = rem / nc, c = c0 + rem - part * nc;
-                    *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, part * NP + 8 * c, 2 * NP)) =
-                        make_uint4(0, 0, 0, 0);
+            for (int c = s.z2lo; c < s.z2hi; ++c)
+                for (int r = t; r < rows; r += 128) {
+                    *reinterpret_cast<uint4*>(a2 + c * LB2 + r * 16) = make_uint4(0, 0, 0, 0);
+                    if (LO) *reinterpret_cast<uint4*>(a2 + (NP / 8 + c) * LB2 + r * 16) = make_uint4(0, 0, 0, 0);
                 }
-            } else {
-                const int c0 = (2 * N) >> 3, nc = 2 * NP / 8 - c0;
-                for (int i = t; i < rows * nc; i += 128) {
-                    const int r2 = i / nc, c = c0 + i - r2 * nc;
-                    *reinterpret_cast<uint4*>(gbase + s.off_a2 + kmaj144(r2, 8 * c, 2 * NP)) = make_uint4(0, 0, 0, 0);
-                }
-            }
-            group_sync(bar_id);
-        }
-        for (int tile = 0; tile < s.tiles1; ++tile) {
-            const int rr = tile * 128 + t;
-            const int p = rr / N, x = rr - p * N;
-            const bool data = p < PB;
-            // rows r2 = p H + ky step by 1: +16 B inside an 8-row group,
-            // +SBO - 112 B when the step crosses into the next group
-            int r2 = p * H;
-            uint8_t* rowp = gbase + s.off_a2 + kmaj144(data ? r2 : 0, 0, 2 * NP);
-            const int kre = LO ? (x >> 3) * 144 + (x & 7) * 2 : ((2 * x) >> 3) * 144 + ((2 * x) & 7) * 2;
-            const int kim = ((NP + x) >> 3) * 144 + ((NP + x) & 7) * 2;
-            const int sbo = 36 * NP;
+            if (s.z2part) group_sync(bar_id);
+            for (int tile = 0; tile < s.tiles1; ++tile) {
+                const int rr = tile * 128 + t;
+                const int p = rr / N, y = rr - p * N;
+                const bool data = p < PB;
+                uint8_t* rowp = a2 + (data ? p * H : 0) * 16 +
+                                (LO ? (y >> 3) * LB2 + (y & 7) * 2 : (y >> 2) * LB2 + (y & 3) * 4);
+                uint8_t* rowi = a2 + (data ? p * H : 0) * 16 + ((NP + y) >> 3) * LB2 + ((NP + y) & 7) * 2;
 #pragma unroll
-            for (int ky0 = 0; ky0 < HP; ky0 += 8) {
-                float dre[8], dim[8];
-                tmem_ld8(tm_warp + tile * 2 * HP + ky0, dre);
-                tmem_ld8(tm_warp + tile * 2 * HP + HP + ky0, dim);
-                tmem_ld_wait();
-                if (data) {
+                for (int ky0 = 0; ky0 < HP; ky0 += 8) {
+                    float dre[8], dim[8];
+                    tmem_ld8(tm_warp + tile * 2 * HP + ky0, dre);
+                    tmem_ld8(tm_warp + tile * 2 * HP + HP + ky0, dim);
+                    tmem_ld_wait();
+                    if (data) {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (ky0 + j < H) {
-                            if (LO) {
-                                st_half(rowp + kre, dre[j]);
-                                st_half(rowp + kim, dim[j]);
-                            } else {
-                                *reinterpret_cast<uint32_t*>(rowp + kre) = pack2(dre[j], dim[j]);
+                        for (int j = 0; j < 8; ++j) {
+                            if (ky0 + j < H) {
+                                if (LO) {
+                                    st_half(rowp + (ky0 + j) * 16, dre[j]);
+                                    st_half(rowi + (ky0 + j) * 16, dim[j]);
+                                } else {
+                                    *reinterpret_cast<uint32_t*>(rowp + (ky0 + j) * 16) = pack2(dre[j], dim[j]);
+                                }
                             }
-                            r2 += 1;
-                            rowp += ((r2 & 7) == 0) ? (sbo - 112) : 16;
                         }
                     }
                 }
@@ -533,22 +565,25 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         fence_async_smem();
         group_sync(bar_id);
 
-        // ---- stage 2: F = Y * W (rows (p,ky,w); columns Re kx | Im kx)
+        // ---- stage 2: F = Y * W (rows (p,kx); columns Re ky | Im ky), K
+        // steps over the data columns only
         if (t == 0) {
             tc_fence_after();
+            const int LB2 = s.lbo2;
+            const uint32_t a2 = gaddr + s.off_a2;
             if (!LO) {
-                // K = (x, part) interleaved: one MMA per output part and K step
-                for (int kk = 0; kk < 2 * NP / 16; ++kk) {
-                    const uint64_t a = sdesc(gaddr + s.off_a2 + kk * 288, 144, 36 * NP);
+                // K = (y, part) interleaved: one MMA per output part and K step
+                for (int kk = 0; kk < s.ks2; ++kk) {
+                    const uint64_t a = sdesc(a2 + 2 * kk * LB2, LB2, 128);
                     const uint64_t wr = sdesc(sbase + s.off_w2re + kk * 256, 128, 32 * NP);
                     const uint64_t wi = sdesc(sbase + s.off_w2im + kk * 256, 128, 32 * NP);
                     mma_f16(tm, a, wr, idesc_f16(NP, false), kk > 0);       // Re = Yr cos + Yi sin
                     mma_f16(tm + NP, a, wi, idesc_f16(NP, false), kk > 0);  // Im = -Yr sin + Yi cos
                 }
             }
-            for (int kk = 0; LO && kk < NP / 16; ++kk) {
-                const uint64_t ar = sdesc(gaddr + s.off_a2 + kk * 288, 144, 36 * NP);
-                const uint64_t ai = sdesc(gaddr + s.off_a2 + (NP / 8 + 2 * kk) * 144, 144, 36 * NP);
+            for (int kk = 0; LO && kk < s.ks2; ++kk) {
+                const uint64_t ar = sdesc(a2 + 2 * kk * LB2, LB2, 128);
+                const uint64_t ai = sdesc(a2 + (NP / 8 + 2 * kk) * LB2, LB2, 128);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
                 const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
                 const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
@@ -565,20 +600,31 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             }
             mma_commit(mbar);
         }
+        // row t of the spectra is (p, kx); in the per-frame pass the cached
+        // reference row is read from L2 while stage 2 runs (with split
+        // twiddles chunk by chunk in epilogue 2: registers)
+        const bool rowv2 = t < PB * H;
+        const int p2 = rowv2 ? t / H : 0, ky2 = rowv2 ? t - p2 * H : 0;
+        const bool live2 = rowv2 && !REF && !cs.sdark[grp][p2];
+        const uint4* frow = reinterpret_cast<const uint4*>(jb.fspec + ((size_t)(live2 ? b0 + p2 : 0) * H + ky2) * FS);
+        uint4 fr[LO ? 1 : NP / 4];
+        if (!REF && !LO) {
+#pragma unroll
+            for (int i = 0; i < (LO ? 1 : NP / 4); ++i)
+                fr[i] = (live2 && 4 * i < FS) ? __ldg(frow + i) : make_uint4(0u, 0u, 0u, 0u);
+        }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
         if (REF) {
-            // ---- the reference spectra to the cache: row (p, ky) of FS FP16
+            // ---- the reference spectra to the cache: row (p, kx) of FS FP16
             // pairs (Re, Im), scaled by sqrt(n2) / ||f - mean f|| (zero for a
-            // dark subset), kx >= N zero; then the windows' integer sums
-            const bool rowv = t < PB * H;
-            const int p = rowv ? t / H : 0, ky = rowv ? t - p * H : 0;
-            const bool live = rowv && b0 + p < n_job;
-            const float sc = live ? cs.sscale[grp][p] : 0.f;
-            uint4* dst = reinterpret_cast<uint4*>(jb.fspec + ((size_t)(live ? b0 + p : 0) * H + ky) * FS);
+            // dark subset), ky >= N zero; then the windows' integer sums
+            const bool live = rowv2 && b0 + p2 < n_job;
+            const float sc = live ? cs.sscale[grp][p2] : 0.f;
+            uint4* dst = reinterpret_cast<uint4*>(jb.fspec + ((size_t)(live ? b0 + p2 : 0) * H + ky2) * FS);
 #pragma unroll
             for (int c = 0; c < NP; c += 8) {
                 float re[8], im[8];
@@ -601,26 +647,30 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
 
         // ---- epilogue 2: cross power C = conj(F) G * scale -> A3 = conj(C),
-        // F the cached reference spectrum (row (POI, ky), read from L2), G the
-        // target's from TMEM; row t of A3 is (p, ky) = t
+        // F the cached reference spectrum, G the target's from TMEM; row t of
+        // A3 is (p, kx) = t.  Columns ky >= N within the stage-3 K are zero;
+        // rows past the data are not written (the rows of D3 they give are
+        // never read)
         {
-            const bool rowv = t < PB * H;
-            const int p = rowv ? t / H : 0, ky = rowv ? t - p * H : 0;
-            const bool live = rowv && !cs.sdark[grp][p];
-            const float sc = live ? cs.sscale[grp][p] : 0.f;
-            const uint4* frow = reinterpret_cast<const uint4*>(jb.fspec + ((size_t)(live ? b0 + p : 0) * H + ky) * FS);
+            if (s.z4early) zero_a4_padding(gbase + s.off_a4, s, PB * N, t);
+            const float sc = live2 ? cs.sscale[grp][p2] : 0.f;
+            const int K3 = s.k3w;
             uint8_t* a3 = gbase + s.off_a13;
 #pragma unroll
             for (int c = 0; c < NP; c += 8) {
+                if (c >= N) break;  // past the data (split twiddles: zero chunks below)
                 float gr[8], gi[8];
                 tmem_ld8(tm_warp + c, gr);
                 tmem_ld8(tm_warp + NP + c, gi);
-                uint4 fa = make_uint4(0u, 0u, 0u, 0u), fb = make_uint4(0u, 0u, 0u, 0u);
-                if (live && c < FS) {
-                    fa = __ldg(frow + (c >> 2));
-                    if (c + 8 <= FS) fb = __ldg(frow + (c >> 2) + 1);
-                }
                 tmem_ld_wait();
+                uint4 fa, fb;
+                if (LO) {
+                    fa = (live2 && c < FS) ? __ldg(frow + (c >> 2)) : make_uint4(0u, 0u, 0u, 0u);
+                    fb = (live2 && c + 8 <= FS) ? __ldg(frow + (c >> 2) + 1) : make_uint4(0u, 0u, 0u, 0u);
+                } else {
+                    fa = fr[LO ? 0 : c >> 2];
+                    fb = fr[LO ? 0 : (c >> 2) + 1];
+                }
                 const uint32_t fw[8] = {fa.x, fa.y, fa.z, fa.w, fb.x, fb.y, fb.z, fb.w};
                 float br[8], bi[8];
 #pragma unroll
@@ -629,54 +679,58 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                     const int kx = c + i;
                     float cr = (f.x * gr[i] + f.y * gi[i]) * sc;
                     float ci = (f.x * gi[i] - f.y * gr[i]) * sc;
-                    if (kx >= N || (ky == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
+                    if (kx >= N || (ky2 == 0 && kx == 0)) { cr = 0.f; ci = 0.f; }
                     br[i] = cr;
                     bi[i] = -ci;  // conj(C) feeds the forward matrices of stage 3
                 }
-                if (rowv) {
+                if (rowv2) {
                     uint4 q;
-                    if (LO) {  // K = (part, kx)
+                    if (LO) {  // K = (part, ky)
                         q.x = pack2(br[0], br[1]); q.y = pack2(br[2], br[3]);
                         q.z = pack2(br[4], br[5]); q.w = pack2(br[6], br[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(t, c, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, c, K3)) = q;
                         q.x = pack2(bi[0], bi[1]); q.y = pack2(bi[2], bi[3]);
                         q.z = pack2(bi[4], bi[5]); q.w = pack2(bi[6], bi[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(t, NP + c, 2 * NP)) = q;
-                    } else {  // K = (kx, part) interleaved
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, NP + c, K3)) = q;
+                    } else {  // K = (ky, part) interleaved
                         q.x = pack2(br[0], bi[0]); q.y = pack2(br[1], bi[1]);
                         q.z = pack2(br[2], bi[2]); q.w = pack2(br[3], bi[3]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c, K3)) = q;
                         q.x = pack2(br[4], bi[4]); q.y = pack2(br[5], bi[5]);
                         q.z = pack2(br[6], bi[6]); q.w = pack2(br[7], bi[7]);
-                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c + 8, 2 * NP)) = q;
+                        *reinterpret_cast<uint4*>(a3 + kmaj(t, 2 * c + 8, K3)) = q;
                     }
                 }
             }
-            // rows of A3 past the data are zero (A3 shares memory with A1, A2)
-            if (t >= PB * H) {
-                for (int k0 = 0; k0 < 2 * NP; k0 += 8)
-                    *reinterpret_cast<uint4*>(a3 + kmaj(t, k0, 2 * NP)) = make_uint4(0, 0, 0, 0);
+            // split twiddles: whole chunks of each part block past the data
+            // within the stage-3 K
+            if (LO && rowv2) {
+                for (int c = (N + 7) & ~7; c < 16 * s.ks2; c += 8) {
+                    *reinterpret_cast<uint4*>(a3 + kmaj(t, c, K3)) = make_uint4(0, 0, 0, 0);
+                    *reinterpret_cast<uint4*>(a3 + kmaj(t, NP + c, K3)) = make_uint4(0, 0, 0, 0);
+                }
             }
         }
         tc_fence_before();
         fence_async_smem();
         group_sync(bar_id);
 
-        // ---- stage 3: conj(Z) = conj(C) * W (rows (p,ky); columns Re x | Im x)
+        // ---- stage 3: conj(Z) = conj(C) * W (rows (p,kx); columns Re v | Im v)
         if (t == 0) {
             tc_fence_after();
+            const int K3 = s.k3w;
             if (!LO) {
-                for (int kk = 0; kk < 2 * NP / 16; ++kk) {
-                    const uint64_t a = sdesc(gaddr + s.off_a13 + kk * 256, 128, 32 * NP);
+                for (int kk = 0; kk < s.ks2; ++kk) {
+                    const uint64_t a = sdesc(gaddr + s.off_a13 + kk * 256, 128, 16 * K3);
                     const uint64_t wr = sdesc(sbase + s.off_w2re + kk * 256, 128, 32 * NP);
                     const uint64_t wi = sdesc(sbase + s.off_w2im + kk * 256, 128, 32 * NP);
                     mma_f16(tm, a, wr, idesc_f16(NP, false), kk > 0);
                     mma_f16(tm + NP, a, wi, idesc_f16(NP, false), kk > 0);
                 }
             }
-            for (int kk = 0; LO && kk < NP / 16; ++kk) {
-                const uint64_t ar = sdesc(gaddr + s.off_a13 + kk * 256, 128, 32 * NP);
-                const uint64_t ai = sdesc(gaddr + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 32 * NP);
+            for (int kk = 0; LO && kk < s.ks2; ++kk) {
+                const uint64_t ar = sdesc(gaddr + s.off_a13 + kk * 256, 128, 16 * K3);
+                const uint64_t ai = sdesc(gaddr + s.off_a13 + (NP / 8 + 2 * kk) * 128, 128, 16 * K3);
                 const uint64_t ch = sdesc(sbase + s.off_c2h + kk * 256, 128, 16 * NP);
                 const uint64_t cl = sdesc(sbase + s.off_c2l + kk * 256, 128, 16 * NP);
                 const uint64_t sh = sdesc(sbase + s.off_s2h + kk * 256, 128, 16 * NP);
@@ -698,28 +752,25 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
         tc_fence_after();
 
-        // ---- epilogue 3: Z -> A4 (rows (p, x), K = (ky, part) interleaved:
-        // k = 2 ky + part, so a POI row's Re and Im of one ky are one 32-bit
-        // store), c2r weights folded in; core matrices 144 B apart along K so
-        // the lanes' stores to one row fall in distinct banks.  A4 overwrites
-        // A3 (stage 3 has completed), so the K padding k in [2H, 2HP) of the
-        // data rows is zeroed first
+        // ---- epilogue 3: D3 -> A4 (rows (p, v), K = (kx, part) interleaved:
+        // k = 2 kx + part, so a POI row's Re and Im of one kx are one 32-bit
+        // store), c2r weights folded in.  A4 is row-contiguous per chunk like
+        // A2: a thread's rows (p, v), v = 0 .. N-1, are 16 bytes apart.  The
+        // chunks holding columns past the data are zeroed first: in
+        // epilogue 2 when A3 does not reach them, else here, and a chunk
+        // holding data too then waits for the zeros.  A4 overwrites A3
+        // (stage 3 has completed)
         {
-            const int c0 = (2 * H) >> 3, nc = K4 / 8 - c0;
-            const int rows = PB * N;
-            for (int i = t; i < rows * nc; i += 128) {
-                const int r4 = i / nc, c = c0 + i - r4 * nc;
-                *reinterpret_cast<uint4*>(gbase + s.off_a4 + kmaj144(r4, 8 * c, K4)) = make_uint4(0, 0, 0, 0);
+            const int LB4 = s.lbo4;
+            uint8_t* a4 = gbase + s.off_a4;
+            if (!s.z4early) {
+                zero_a4_padding(a4, s, PB * N, t);
+                if (s.z4part) group_sync(bar_id);
             }
-            group_sync(bar_id);
             const bool rowv = t < PB * H;
             const int p = rowv ? t / H : 0, ky = rowv ? t - (t / H) * H : 0;
             const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
-            // rows r4 = p N + x step by 1: +16 B inside an 8-row group,
-            // +SBO - 112 B when the step crosses into the next group
-            int r4 = p * N;
-            uint8_t* rowp = gbase + s.off_a4 + kmaj144(r4, 2 * ky, K4);
-            const int sbo = 18 * K4;
+            uint8_t* rowp = a4 + (p * N) * 16 + (ky >> 2) * LB4 + (ky & 3) * 4;
 #pragma unroll
             for (int x0 = 0; x0 < NP; x0 += 8) {
                 if (x0 >= N) break;  // columns N .. NP-1 are padding (N is even: N..N+7 too when N % 8)
@@ -731,9 +782,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         if (x0 + j < N) {
-                            *reinterpret_cast<uint32_t*>(rowp) = pack2(wgt * re[j], -wgt * im[j]);  // Zi = -D_i
-                            ++r4;
-                            rowp += ((r4 & 7) == 0) ? (sbo - 112) : 16;
+                            // Zi = -D_i
+                            *reinterpret_cast<uint32_t*>(rowp + (x0 + j) * 16) = pack2(wgt * re[j], -wgt * im[j]);
                         }
                     }
                 }
@@ -743,12 +793,13 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         fence_async_smem();
         group_sync(bar_id);
 
-        // ---- stage 4: c[(p,x)][y] = A4 * B4
+        // ---- stage 4: c[(p,v)][u] = A4 * B4 (the c2r inverse along kx)
         if (t == 0) {
             tc_fence_after();
+            const int LB4 = s.lbo4;
             for (int tile = 0; tile < s.tiles4; ++tile) {
                 for (int kk = 0; kk < K4 / 16; ++kk) {
-                    const uint64_t a = sdesc(gaddr + s.off_a4 + tile * (16 * 18 * K4) + kk * 288, 144, 18 * K4);
+                    const uint64_t a = sdesc(gaddr + s.off_a4 + tile * 2048 + 2 * kk * LB4, LB4, 128);
                     const uint64_t bh = sdesc(sbase + s.off_b4h + kk * 256, 128, 16 * K4);
                     const uint64_t bl = sdesc(sbase + s.off_b4l + kk * 256, 128, 16 * K4);
                     mma_f16(tm + tile * NP, a, bh, idesc_f16(NP, false), kk > 0);
@@ -765,8 +816,9 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
         // (scratch in the shared operand region, which stage 4 has finished
         // reading; the surface stays in TMEM and is read twice in chunks).
-        // Thread t holds surface row R = 128 k + t of tile k (R = p N + x:
-        // POI p, column x, the values over y in the row's TMEM columns)
+        // Thread t holds surface row R = 128 k + t of tile k (R = p N + v:
+        // POI p, y shift v, the values over the x shift u in the row's TMEM
+        // columns)
         const int ntile = s.tiles4;
         if (t < kCandChunk) ps->candS[t] = 0;
         // approximate peak value per POI: each thread's maximum over y of its
@@ -889,7 +941,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                     for (int q = exk[k]; m != 0; ++q) {
                         const int y = __ffsll((long long)m) - 1;
                         m &= m - 1;
-                        if (q >= lo && q < lo + kCandChunk) ps->cand[q - lo] = (p4 << 16) | (y * N + x4);
+                        // shift index v N + u: row v = x4, bit u = y
+                        if (q >= lo && q < lo + kCandChunk) ps->cand[q - lo] = (p4 << 16) | (x4 * N + y);
                     }
                 }
             }
@@ -1158,7 +1211,25 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     // per-group regions: one operand region shared by A1, A2, A3, A4 and the
     // peak scratch, then the windows
     s.NW4 = (N + 3) / 4;
-    const int a1 = s.tiles1 * 128 * K1 * 2, a2 = 16 * 36 * NP, a3 = 128 * 2 * NP * 2, a4 = s.tiles4 * 16 * 18 * K4;
+    // stages 2 and 3 take K over the data columns only: (y, part) interleaved
+    // 2N with single twiddles, N per part block with split ones
+    s.ks2 = s.lo ? (N + 15) / 16 : (2 * N + 15) / 16;
+    s.k3w = s.lo ? 2 * NP : 16 * s.ks2;
+    // A2 [<= 128 rows], A4 [tiles4 x 128 rows]: chunk strides of 16 (rows + 1)
+    // bytes put one row's chunks in distinct banks
+    s.lbo2 = 16 * (128 + 1);
+    s.lbo4 = 16 * (s.tiles4 * 128 + 1);
+    s.z2lo = s.lo ? N / 8 : 2 * N / 8;
+    s.z2hi = 2 * s.ks2;
+    s.z2part = (s.lo ? N % 8 : 2 * N % 8) != 0 && s.z2lo < s.z2hi;
+    s.z4lo = 2 * s.H / 8;
+    s.z4hi = K4 / 8;
+    s.z4part = 2 * s.H % 8 != 0 && s.z4lo < s.z4hi;
+    const int a1 = s.tiles1 * 128 * K1 * 2;
+    const int a2 = (s.lo ? NP / 8 + 2 * s.ks2 : 2 * s.ks2) * s.lbo2;
+    const int a3 = 128 * s.k3w * 2;
+    const int a4 = (K4 / 8) * s.lbo4;
+    s.z4early = a3 <= s.z4lo * s.lbo4;
     const int region = round_up(std::max(std::max(a1, a2), std::max(std::max(a3, a4), (int)sizeof(PeakScratch))),
                                 128);
     s.off_a13 = 0;

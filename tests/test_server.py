@@ -16,7 +16,7 @@ def _params(g, path=PATH_FAST):
 def test_frame_device_bytes_formula():
     """Host-only estimate used for admission: images padded to 16-byte rows,
     per-POI buffers, the small buffers (error flag, work counter, twiddles,
-    TMA descriptors) and the fast path's cache, gradient image,
+    TMA descriptors) and the fast path's cache, gradient image, sample table,
     neighbourhood table and the FFT-CC's reference spectra, each rounded up
     to 2 MiB."""
     _, g = synth.small_case(h=160, w=197, r=10, grid=7)
@@ -25,7 +25,7 @@ def test_frame_device_bytes_formula():
     r = lambda b: -(-b // (2 << 20)) * (2 << 20)  # noqa: E731
     pitch = (197 + 15) // 16 * 16
     want = (2 * r(pitch * 160 + 16) + r(8 * n) + 3 * r(4 * n) + r(n) + r(24 * n) + r(4 * n) + r(n) + 4 * r(1024)
-            + r(64 * n) + r(168 * n) + r(n) + r(8 * g.roi_w * g.roi_h) + r(16 * g.roi_w * g.roi_h)
+            + r(64 * n) + r(168 * n) + r(n) + r(8 * g.roi_w * g.roi_h) + r(16 * 21 * 21) + r(16 * g.roi_w * g.roi_h)
             + r(n * 11 * 20 * 4) + r(8 * n))  # reference spectra (N = 20: 11 rows of 20 FP16 pairs), window sums
     assert frame_device_bytes(p) == want
     big = _params(synth.Geometry(2048, 2048, 1, 1, 2046, 2046, 20, 5, 20))

@@ -159,7 +159,7 @@ struct Engine {
     bool cache_valid = false;
     std::vector<int32_t> cache_poi_host;
     DevBuf c_subR, c_sd, c_chol, c_norm, c_flag;  // plain
-    DevBuf c_stat, c_chol64, c_flag64, c_grad;    // fast
+    DevBuf c_stat, c_chol64, c_flag64, c_grad, c_samp;  // fast
     DevBuf d_lut;
     // TMA descriptors of d_ref / d_tar for the tensor-core FFT-CC: a pinned
     // host copy and the device copy the kernels read, re-encoded when the
@@ -336,6 +336,8 @@ struct Engine {
                                                c_chol64.as<double>(), c_flag64.as<uint8_t>(), stream));
             TW_TRY(c_grad.ensure(sizeof(float2) * (size_t)g.rw * g.rh));
             TW_CUDA(launch_ref_grad(g, d_ref.as<uint8_t>(), c_grad.as<float2>(), stream));
+            TW_TRY(c_samp.ensure(sizeof(float4) * (size_t)S));
+            TW_CUDA(launch_sample_table(g.rx, g.ry, c_samp.as<float4>(), stream));
         }
         cache_valid = true;
         if (t_pre) *t_pre = 1.f;
@@ -390,7 +392,7 @@ struct Engine {
             TW_CUDA(launch_icgn_fast(g, d_ref.as<uint8_t>(), d_tar.as<uint8_t>(), poi, n, c_stat.as<float>(),
                                      c_chol64.as<double>(), c_flag64.as<uint8_t>(), d_lut.p,
                                      d_work.as<int>(), u, v, p6, iters, flags, solve_tune(), stream,
-                                     c_grad.as<float2>()));
+                                     c_grad.as<float2>(), c_samp.as<float4>()));
         }
         return TWDIC_OK;
     }
@@ -802,6 +804,7 @@ int twdic_frame_device_bytes(const twdic_params* p, uint64_t* bytes) {
     } else {
         t += r(64 * n) + r(168 * n) + r(n);                 // statistics, inverse Hessian, flags
         t += r(8 * (uint64_t)p->roi_width * p->roi_height);   // reference gradient image (float2)
+        t += r(16 * (uint64_t)(2 * p->subset_x + 1) * (2 * p->subset_y + 1));  // sample table
         if (p->subset_x == p->subset_y && p->subset_x >= 4 && p->subset_x <= 32) {
             // the tensor-core FFT-CC's reference spectra (N/2 + 1 rows of N
             // rounded up to 4 FP16 pairs per POI) and window sums
@@ -1348,6 +1351,7 @@ int batch_enqueue(twdic_batch* b, const BatchArgs& a) {
             jb.rflag = e.c_flag64.as<uint8_t>();
             jb.table = tune.sampler == kSampWindow ? nullptr : e.d_lut.p;
             jb.grad = e.c_grad.as<float2>();
+            jb.samples = e.c_samp.as<float4>();
             jb.u = o.u;
             jb.v = o.v;
             jb.p6 = o.p6;

@@ -44,6 +44,7 @@ struct IcgnJob {
     const uint8_t* rflag;
     const void* table;    // per-frame target table of the sampler (or null: window)
     const float2* grad = nullptr;  // per-reference gradient image, rw x rh (or null: staged per POI)
+    const float4* samples = nullptr;  // subset sample table (launch_sample_table)
     float* u;
     float* v;
     float* p6;
@@ -117,7 +118,12 @@ cudaError_t launch_ref_precompute_fast(const Geom& g, const uint8_t* ref, const 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                              const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
-                             const IcgnTune& tune, cudaStream_t st, const float2* grad = nullptr);
+                             const IcgnTune& tune, cudaStream_t st, const float2* grad = nullptr,
+                             const float4* samples = nullptr);
+// The samples of a (2 rx + 1) x (2 ry + 1) subset in the reference's order
+// (row by row): entry k = (dx, dy) as floats, then the column and row
+// within the subset as int bits (kernels_icgn_fast.cu)
+cudaError_t launch_sample_table(int rx, int ry, float4* out, cudaStream_t st);
 // Per-reference gradient image (R_x, R_y) of the ROI, float2, rw x rh (kernels_icgn_fast.cu)
 cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, float2* grad, cudaStream_t st);
 int icgn_fast_window(const Geom& g);

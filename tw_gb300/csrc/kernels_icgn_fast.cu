@@ -827,7 +827,6 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
         const int p = pg - jb.begin;
         const int SW = 2 * g.rx + 1, SH = 2 * g.ry + 1, S = SW * SH;
         const float inv_s = 1.0f / (float)S;
-        const float rxf = (float)g.rx, swf = (float)SW;
         const size_t plane = (size_t)g.rw * g.rh;
         const float4* lut0 = static_cast<const float4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
         const uint4* nb0 = static_cast<const uint4*>(jb.table) - ((size_t)g.sy * g.rw + g.sx);
@@ -858,13 +857,12 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
             for (int j = 0; j < 6; ++j) hw[lane * 6 + j] = hi[lane >= j ? tri(lane, j) : tri(j, lane)];
         }
         __syncwarp();
-        // sample k = lane + 32 j at subset offset (dx, dy); its gradient at
-        // ROI offset gofs, stepped with the same carry
+        // sample k = lane + 32 j: its offset (dx, dy) and its column and row
+        // in the subset from the sample table (one L1-resident load in place
+        // of stepping with a carry), its reference gradient at ROI offset
+        // row * rw + column from grad0
         const float2* grad0 = jb.grad + ((size_t)(py - g.ry - g.sy) * g.rw + (px - g.rx - g.sx));
-        const int gofs_first = (lane / SW) * g.rw + lane % SW;
-        const int dgofs = (32 / SW) * g.rw + 32 % SW, gwrap = g.rw - SW;
-        const float2 d_first = make_float2((float)(lane % SW - g.rx), (float)(lane / SW - g.ry));
-        const float2 dd = make_float2((float)(32 % SW), (float)(32 / SW)), wrap = make_float2(-swf, 1.f);
+        const float4* smp0 = jb.samples + lane;
         int it = 0;
         for (;;) {
             const float bx = (float)px + Wm[2], by = (float)py + Wm[5];
@@ -873,28 +871,29 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
             float v8 = 0.f;
             if (!oor) {
                 PassSums ps;
-                float2 d = d_first;
-                int gofs = gofs_first;
+                const float4* smp = smp0;
                 const float2 w03 = make_float2(Wm[0], Wm[3]), w14 = make_float2(Wm[1], Wm[4]);
                 const float2 bxy = make_float2(bx, by);
                 if (it == 0) {
                     // first pass: integer pixels (TW_paDIC_ICGN2D_CPU.cpp:609-637)
 #pragma unroll UNROLL
                     for (int k = lane; k < S; k += 32) {
+                        const float4 e4 = __ldg(smp);
+                        smp += 32;
+                        const float2 d = make_float2(e4.x, e4.y);
+                        const int gofs = __float_as_int(e4.w) * g.rw + __float_as_int(e4.z);
                         const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
                                                       __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
                         const int ix = (int)wxy.x, iy = (int)wxy.y;
                         ps.add((float)jb.tar[(size_t)iy * g.pitch + ix] - c, grad0[gofs], d);
-                        gofs += dgofs;
-                        d = __fadd2_rn(d, dd);
-                        if (d.x > rxf) {
-                            d = __fadd2_rn(d, wrap);
-                            gofs += gwrap;
-                        }
                     }
                 } else {
 #pragma unroll UNROLL
                     for (int k = lane; k < S; k += 32) {
+                        const float4 e4 = __ldg(smp);
+                        smp += 32;
+                        const float2 d = make_float2(e4.x, e4.y);
+                        const int gofs = __float_as_int(e4.w) * g.rw + __float_as_int(e4.z);
                         const float2 wxy = __ffma2_rn(w03, make_float2(d.x, d.x),
                                                       __ffma2_rn(w14, make_float2(d.y, d.y), bxy));
                         const int ix = (int)wxy.x, iy = (int)wxy.y;
@@ -924,12 +923,6 @@ __global__ void __launch_bounds__(NW * 32, (NW >= 32 ? 1 : 32 / NW))
                             tp = (((r23.y * fy + r23.x) * fy + r01.y) * fy + r01.x) - c;
                         }
                         ps.add(tp, grad0[gofs], d);
-                        gofs += dgofs;
-                        d = __fadd2_rn(d, dd);
-                        if (d.x > rxf) {
-                            d = __fadd2_rn(d, wrap);
-                            gofs += gwrap;
-                        }
                     }
                 }
                 ps.unpack(s);
@@ -1110,6 +1103,22 @@ int icgn_fast_residency(const Geom& g, const IcgnTune& tune) {
     return std::max(1, std::min(std::min(32, by_regs), by_smem));
 }
 
+// Entry k of the sample table: the offset (dx, dy) from the POI and the
+// column and row within the subset, k = row * (2 rx + 1) + column.
+__global__ void k_sample_table(int rx, int ry, float4* out) {
+    const int SW = 2 * rx + 1, S = SW * (2 * ry + 1);
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= S) return;
+    const int ox = k % SW, oy = k / SW;
+    out[k] = make_float4((float)(ox - rx), (float)(oy - ry), __int_as_float(ox), __int_as_float(oy));
+}
+
+cudaError_t launch_sample_table(int rx, int ry, float4* out, cudaStream_t st) {
+    const int S = (2 * rx + 1) * (2 * ry + 1);
+    k_sample_table<<<(S + 255) / 256, 256, 0, st>>>(rx, ry, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ref_grad(const Geom& g, const uint8_t* ref, float2* grad, cudaStream_t st) {
     dim3 blk(32, 8), grd((g.rw + 31) / 32, (g.rh + 7) / 8);
     k_ref_grad<<<grd, blk, 0, st>>>(g, ref, grad);
@@ -1140,13 +1149,13 @@ static cudaError_t launch_icgn_warp_t(const IcgnJobs& J, int chunk, int ctas_per
 }
 
 // One POI per warp over a per-reference gradient image: every job needs
-// grad, a table sampler and table offsets below 2^31 (otherwise the
-// one-POI-per-CTA kernel runs).
+// grad, the sample table, a table sampler and table offsets below 2^31
+// (otherwise the one-POI-per-CTA kernel runs).
 static bool icgn_warp_eligible(const IcgnJobs& J, const IcgnTune& tune) {
     if (tune.chunk <= 0 || tune.sampler == kSampWindow) return false;
     if (tune.threads != 128 && tune.threads != 256 && tune.threads != 512 && tune.threads != 1024) return false;
     for (int j = 0; j < J.njobs; ++j) {
-        if (!J.job[j].grad) return false;
+        if (!J.job[j].grad || !J.job[j].samples) return false;
         // the kernel indexes the table with 32-bit image offsets iy * rw + ix
         if ((long long)J.job[j].g.img_h * J.job[j].g.rw >= (1ll << 31)) return false;
     }
@@ -1202,7 +1211,8 @@ cudaError_t launch_icgn_fast_jobs(const IcgnJobs& J, int* work, const IcgnTune& 
 cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* tar, const int2* poi, int n,
                              const float* stats, const double* chol, const uint8_t* rflag, const void* table,
                              int* work, float* u, float* v, float* p6, int* iters, uint8_t* flags,
-                             const IcgnTune& tune, cudaStream_t st, const float2* grad) {
+                             const IcgnTune& tune, cudaStream_t st, const float2* grad,
+                             const float4* samples) {
     if (n <= 0) return cudaSuccess;
     IcgnJobs J;
     J.njobs = 1;
@@ -1217,6 +1227,7 @@ cudaError_t launch_icgn_fast(const Geom& g, const uint8_t* ref, const uint8_t* t
     jb.rflag = rflag;
     jb.table = table;
     jb.grad = grad;
+    jb.samples = samples;
     jb.u = u;
     jb.v = v;
     jb.p6 = p6;

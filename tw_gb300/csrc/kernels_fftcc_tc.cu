@@ -234,6 +234,34 @@ __device__ __forceinline__ uint32_t bytes_h2(uint32_t w, uint32_t sel) {
     asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(b), "r"(0x64006400u));
     return r;
 }
+// one aligned 32-bit word of shared memory
+__device__ __forceinline__ uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+// sum_{i < len} f[i] g[i] of two byte runs at any shared-memory addresses:
+// aligned words, one load and one funnel shift per word of each run (the
+// words past a run's end, up to 7 bytes, lie in the same region)
+__device__ __forceinline__ unsigned dot_bytes_s(uint32_t fa, uint32_t ga, int len, unsigned acc) {
+    const uint32_t fal = fa & ~3u, fsh = (fa & 3) * 8;
+    const uint32_t gal = ga & ~3u, gsh = (ga & 3) * 8;
+    uint32_t fp = lds_u32(fal), gp = lds_u32(gal);
+    int i = 0;
+#pragma unroll 4
+    for (; i + 4 <= len; i += 4) {
+        const uint32_t fn = lds_u32(fal + i + 4), gn = lds_u32(gal + i + 4);
+        acc = __dp4a(__funnelshift_r(fp, fn, fsh), __funnelshift_r(gp, gn, gsh), acc);
+        fp = fn;
+        gp = gn;
+    }
+    if (i < len) {  // 1 to 3 bytes left
+        const uint32_t fn = lds_u32(fal + i + 4), gn = lds_u32(gal + i + 4);
+        const uint32_t m = 0xffffffffu >> (8 * (4 - (len - i)));
+        acc = __dp4a(__funnelshift_r(fp, fn, fsh) & m, __funnelshift_r(gp, gn, gsh), acc);
+    }
+    return acc;
+}
 // 4 bytes from any shared-memory byte pointer derived from the dynamic
 // shared buffer (two aligned words, funnel shift)
 __device__ __forceinline__ uint32_t ld_unaligned_p(const uint8_t* a) {
@@ -279,7 +307,8 @@ struct TcCta {
     uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
     int2 spoi[kMaxGroups][kMaxPB];
     const uint8_t* wptr[kMaxGroups][2 * kMaxPB];  // each window's (0, 0): staged box or the image
-    int wrs[kMaxGroups];                // row stride of the windows in wwin
+    int wrs[kMaxGroups];                // row stride of the windows
+    int wsm[kMaxGroups];                // 1: the windows are the staged boxes (shared memory)
     int snext[kMaxGroups];
 };
 
@@ -389,6 +418,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 tma_load_2d(wwin, &jb.maps->ref_u, xau, y0, tbar);
                 tma_load_2d(wwin + jb.utoff, &jb.maps->tar_u, xau, y0, tbar);
                 cs.wrs[grp] = jb.uw;
+                cs.wsm[grp] = 1;
                 for (int p = 0; p < PB; ++p) {
                     const int2 pyx = cs.spoi[grp][p];
                     const int xo = pyx.x < 0 ? 0 : pyx.y - g.rx - xau;
@@ -398,6 +428,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             } else {
                 mbar_expect_tx(tbar, 0u);  // completes the phase: nothing to load
                 cs.wrs[grp] = g.pitch;
+                cs.wsm[grp] = 0;
                 for (int p = 0; p < PB; ++p) {
                     const int2 pyx = cs.spoi[grp][p];
                     const size_t o = pyx.x < 0 ? 0 : (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
@@ -941,8 +972,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                     for (int q = exk[k]; m != 0; ++q) {
                         const int y = __ffsll((long long)m) - 1;
                         m &= m - 1;
-                        // shift index v N + u: row v = x4, bit u = y
-                        if (q >= lo && q < lo + kCandChunk) ps->cand[q - lo] = (p4 << 16) | (x4 * N + y);
+                        // POI, y shift v (the row x4), x shift u (the bit y)
+                        if (q >= lo && q < lo + kCandChunk) ps->cand[q - lo] = (p4 << 16) | (x4 << 8) | y;
                     }
                 }
             }
@@ -953,40 +984,67 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
                 const int rot = lane % NW4;
                 const int rs = cs.wrs[grp];
-                for (int task = t; task < nc * N; task += 128) {
-                    const int c = task / N, y = task - c * N;
-                    const int code = ps->cand[c];
-                    const int p = code >> 16, idx = code & 0xffff;
-                    const int ky = idx / N, kx = idx - ky * N;
-                    int yy = y + ky;
-                    if (yy >= N) yy -= N;
-                    const uint8_t* fb = cs.wptr[grp][2 * p] + y * rs;
-                    const uint8_t* gb = cs.wptr[grp][2 * p + 1] + yy * rs;
-                    const uint32_t g0 = ld_unaligned_p(gb);  // row start, for words that wrap
-                    unsigned acc = 0;
-                    int j = rot;
+                const bool wsm = cs.wsm[grp] != 0;
+                // task (c, y) = c N + y for thread t, stepped by 128 (all lanes
+                // of a warp take the same number of steps: the warp's sums
+                // per candidate are reduced before one shared atomic each)
+                const int ntask = nc * N, dc = 128 / N, dy = 128 - dc * N;
+                int c = t / N, y = t - (t / N) * N;
+                for (int base = 0; base < ntask; base += 128) {
+                    const bool valid = base + t < ntask;
+                    unsigned acc0 = 0u, acc1 = 0u;
+                    if (valid) {
+                        const int code = ps->cand[c];
+                        const int p = code >> 16, ky = (code >> 8) & 0xff, kx = code & 0xff;
+                        int yy = y + ky;
+                        if (yy >= N) yy -= N;
+                        int j = rot;
+                        if (wsm) {
+                            // the staged boxes: the circular row product as
+                            // two linear segments, f[0, N - kx) g[kx, N) and
+                            // f[N - kx, N) g[0, kx)
+                            const uint32_t fb = smem_u32(cs.wptr[grp][2 * p]) + y * rs;
+                            const uint32_t gb = smem_u32(cs.wptr[grp][2 * p + 1]) + yy * rs;
+                            acc0 = dot_bytes_s(fb, gb + kx, N - kx, acc0);
+                            acc1 = dot_bytes_s(fb + N - kx, gb, kx, acc1);
+                        } else {
+                            const uint8_t* fb = cs.wptr[grp][2 * p] + y * rs;
+                            const uint8_t* gb = cs.wptr[grp][2 * p + 1] + yy * rs;
+                            const uint32_t g0 = ld_unaligned_p(gb);
 #pragma unroll 2
-                    for (int jj = 0; jj < NW4; ++jj) {
-                        uint32_t fw = ld_unaligned_p(fb + 4 * j);
-                        if (j == NW4 - 1) fw &= tail;
-                        int a = kx + 4 * j;  // g bytes (x + kx) mod N for x = 4j .. 4j+3
-                        if (a >= N) a -= N;
-                        uint32_t gw = ld_unaligned_p(gb + a);
-                        if (a + 4 > N) {
-                            const int nlo = N - a;
-                            gw = (gw & (0xffffffffu >> (8 * (4 - nlo)))) | (g0 << (8 * nlo));
+                            for (int jj = 0; jj < NW4; ++jj) {
+                                uint32_t fw = ld_unaligned_p(fb + 4 * j);
+                                if (j == NW4 - 1) fw &= tail;
+                                int a = kx + 4 * j;
+                                if (a >= N) a -= N;
+                                uint32_t gw = ld_unaligned_p(gb + a);
+                                if (a + 4 > N) {
+                                    const int nlo = N - a;
+                                    gw = (gw & (0xffffffffu >> (8 * (4 - nlo)))) | (g0 << (8 * nlo));
+                                }
+                                if (jj & 1) acc1 = __dp4a(fw, gw, acc1);
+                                else acc0 = __dp4a(fw, gw, acc0);
+                                if (++j == NW4) j = 0;
+                            }
                         }
-                        acc = __dp4a(fw, gw, acc);
-                        if (++j == NW4) j = 0;
                     }
-                    atomicAdd(&ps->candS[c], (int)acc);
+                    const unsigned seg = __match_any_sync(kFull, valid ? c : -1);
+                    const int sum = __reduce_add_sync(seg, (int)(acc0 + acc1));
+                    if (valid && lane == __ffs(seg) - 1) atomicAdd(&ps->candS[c], sum);
+                    c += dc;
+                    y += dy;
+                    if (y >= N) {
+                        y -= N;
+                        ++c;
+                    }
                 }
             }
             group_sync(bar_id);
             if (t < PB && !cs.sdark[grp][t]) {
                 const int a = max(cs.cbase[grp][t], lo), b = min(cs.cend[grp][t], lo + kCandChunk);
                 for (int k = a; k < b; ++k) {
-                    const int sc = ps->candS[k - lo], id = ps->cand[k - lo] & 0xffff;
+                    const int code = ps->cand[k - lo];
+                    const int sc = ps->candS[k - lo], id = ((code >> 8) & 0xff) * N + (code & 0xff);
                     if (sc > best_s || (sc == best_s && id < best_i)) {
                         best_s = sc;
                         best_i = id;

@@ -295,7 +295,7 @@ __device__ __forceinline__ void st_half(uint8_t* p, float v) { *reinterpret_cast
 // Shared state of a CTA's groups (static shared memory).
 struct TcCta {
     uint64_t mbar_mma[kMaxGroups];
-    uint64_t mbar_tma[kMaxGroups];
+    uint64_t mbar_tma[kMaxGroups][2];  // one per window slot
     uint32_t tmem_slot;
     int seg;
     int wsum[kMaxGroups][2 * kMaxPB][2];
@@ -305,10 +305,13 @@ struct TcCta {
     int cend[kMaxGroups][kMaxPB];       // one past its last
     int wtot[kMaxGroups][2][4];         // candidates per warp and surface tile
     uint32_t smaxv[kMaxGroups][kMaxPB];  // ordered value of the approximate peak
-    int2 spoi[kMaxGroups][kMaxPB];
-    const uint8_t* wptr[kMaxGroups][2 * kMaxPB];  // each window's (0, 0): staged box or the image
-    int wrs[kMaxGroups];                // row stride of the windows
-    int wsm[kMaxGroups];                // 1: the windows are the staged boxes (shared memory)
+    // per window slot (a group's batch in work and the next one, staged
+    // while the first runs): POIs, each window's (0, 0) (staged box or the
+    // image), the windows' row stride, 1 when they are the staged boxes
+    int2 spoi[kMaxGroups][2][kMaxPB];
+    const uint8_t* wptr[kMaxGroups][2][2 * kMaxPB];
+    int wrs[kMaxGroups][2];
+    int wsm[kMaxGroups][2];
     int snext[kMaxGroups];
 };
 
@@ -339,10 +342,14 @@ __device__ __forceinline__ void tc_load_tables(uint8_t* sm, const uint4* __restr
 
 // The batches of one group over jobs [job_lo, job_hi) of J, which share the
 // window size of shape s: batch indices [first, nbatch) -- the group's first
-// batch, then the next free one from `counter` plus `counter_base`, taken by
-// thread 0 at the start of a batch so that the atomic's latency is hidden.
-// phase / tphase: the parities of the group's MMA and TMA mbarriers, carried
-// across calls.  Returns false after a bounded wait gave up (err set).
+// batch, then the next free one from `counter` plus `counter_base`, drawn by
+// thread 0 one batch ahead.  The windows are double-buffered: while a batch
+// runs, the next one's POIs are loaded and its windows are staged into the
+// other slot (after the batch's stage-1 MMAs are issued), so a batch starts
+// on windows already in shared memory.
+// phase / tphase: the parities of the group's MMA mbarrier and of its two
+// TMA mbarriers (bits 0 and 1), carried across calls.  Returns false after a
+// bounded wait gave up (err set).
 // REF: the per-reference pass -- stages 1 and 2 of the reference windows,
 // whose spectra (scaled by sqrt(n2) / ||f - mean f||, FP16 pairs) and integer
 // sums go to the job's cache.  Otherwise the per-frame pass: stages 1 and 2 of
@@ -367,95 +374,128 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
     const int n2 = N * N;
     constexpr int K1 = NP;
     uint8_t* gbase = sm + s.tab_bytes + grp * s.group_bytes;
-    uint8_t* wwin = gbase + s.off_win;  // the two one-row TMA boxes: reference at 0, target at utoff
+    // window slots 0 and 1, win_bytes apart: the two one-row TMA boxes,
+    // reference at 0, target at utoff
+    uint8_t* wwin = gbase + s.off_win;
     PeakScratch* ps = reinterpret_cast<PeakScratch*>(gbase + s.off_a13);
     uint64_t* mbar = &cs.mbar_mma[grp];
-    uint64_t* tbar = &cs.mbar_tma[grp];
     const uint32_t tm = cs.tmem_slot + grp * kTmemCols;
     const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
     const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
     const int FS = s.FS;  // cached spectrum: complex values per (POI, ky) row
-    int nxt = 0;
-    for (int batch = first; batch < nbatch; batch = cs.snext[grp]) {
-        if (t == 0) nxt = counter_base + atomicAdd(counter, 1);
-        // the job (image pair, POI set) of this batch: batches of job j are
-        // [batch_begin_j, batch_begin_j + ceil(n_j / PB))
-        int jj = job_lo;
+    // the job (image pair, POI set) of a batch: batches of job j are
+    // [batch_begin_j, batch_begin_j + ceil(n_j / PB))
+    auto job_of = [&](int bt) {
+        int jx = job_lo;
         if (MULTI) {
-            while (jj + 1 < job_hi && batch >= J.job[jj + 1].batch_begin) ++jj;
+            while (jx + 1 < job_hi && bt >= J.job[jx + 1].batch_begin) ++jx;
         }
-        const TcJob& jb = J.job[jj];
-        const Geom& g = jb.g;
-        const int2* __restrict__ poi = jb.poi;
-        const int n_job = jb.n;
-        const int b0 = (batch - jb.batch_begin) * PB;
-        if (t < 2 * kMaxPB * 2) (&cs.wsum[grp][0][0])[t] = 0;
-        if (t < PB) {
-            cs.spoi[grp][t] = (b0 + t < n_job) ? poi[b0 + t] : make_int2(-1, -1);
-            cs.smaxv[grp][t] = 0u;
+        return jx;
+    };
+    // POI t of a batch (t < PB), (-1, -1) past the job's POIs
+    auto batch_poi = [&](int bt) {
+        const TcJob& jx = J.job[job_of(bt)];
+        const int bx0 = (bt - jx.batch_begin) * PB;
+        return bx0 + t < jx.n ? jx.poi[bx0 + t] : make_int2(-1, -1);
+    };
+    // thread 0: a batch's windows into slot sl2, its POIs being in that
+    // slot.  When the POIs lie on one POI row, one [N][uw] TMA box per image
+    // holds all the windows (x aligned down to 16 bytes); otherwise (a batch
+    // across POI rows, POIs off the grid) the windows are read from the
+    // images in global memory.  The per-frame pass also sends the batch's
+    // cached reference spectra towards L2 (epilogue 2 reads them).
+    auto stage_windows = [&](int bt, int sl2) {
+        const TcJob& jx = J.job[job_of(bt)];
+        const Geom& gx = jx.g;
+        uint8_t* wbuf = wwin + sl2 * s.win_bytes;
+        uint64_t* tb = &cs.mbar_tma[grp][sl2];
+        fence_async_smem();  // the slot's earlier generic reads come before the copies' writes
+        int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
+        for (int p = 0; p < PB; ++p) {
+            const int2 pyx = cs.spoi[grp][sl2][p];
+            if (pyx.x < 0) continue;
+            ymin = min(ymin, pyx.x); ymax = max(ymax, pyx.x);
+            xmin = min(xmin, pyx.y); xmax = max(xmax, pyx.y);
         }
-        group_sync(bar_id);
-
-        // ---- phase L1: the windows.  When the batch's POIs lie on one POI row,
-        // one [N][uw] TMA box per image holds all its windows (x aligned down
-        // to 16 bytes); otherwise (a batch across POI rows, POIs off the grid)
-        // the windows are read from the images in global memory
-        if (t == 0) {
-            fence_async_smem();  // the previous batch's generic reads of the windows come first
-            int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
+        const int xau = (xmin - gx.rx) & ~15;
+        const bool uni = jx.uw > 0 && ymin == ymax && xmax - gx.rx + N - xau <= jx.uw;
+        if (uni) {
+            const int y0 = ymin - gx.ry;
+            mbar_expect_tx(tb, (uint32_t)(2 * N * jx.uw));
+            tma_load_2d(wbuf, &jx.maps->ref_u, xau, y0, tb);
+            tma_load_2d(wbuf + jx.utoff, &jx.maps->tar_u, xau, y0, tb);
+            cs.wrs[grp][sl2] = jx.uw;
+            cs.wsm[grp][sl2] = 1;
             for (int p = 0; p < PB; ++p) {
-                const int2 pyx = cs.spoi[grp][p];
-                if (pyx.x < 0) continue;
-                ymin = min(ymin, pyx.x); ymax = max(ymax, pyx.x);
-                xmin = min(xmin, pyx.y); xmax = max(xmax, pyx.y);
+                const int2 pyx = cs.spoi[grp][sl2][p];
+                const int xo = pyx.x < 0 ? 0 : pyx.y - gx.rx - xau;
+                cs.wptr[grp][sl2][2 * p] = wbuf + xo;
+                cs.wptr[grp][sl2][2 * p + 1] = wbuf + jx.utoff + xo;
             }
-            const int xau = (xmin - g.rx) & ~15;
-            const bool uni = jb.uw > 0 && ymin == ymax && xmax - g.rx + N - xau <= jb.uw;
-            if (uni) {
-                const int y0 = ymin - g.ry;
-                mbar_expect_tx(tbar, (uint32_t)(2 * N * jb.uw));
-                tma_load_2d(wwin, &jb.maps->ref_u, xau, y0, tbar);
-                tma_load_2d(wwin + jb.utoff, &jb.maps->tar_u, xau, y0, tbar);
-                cs.wrs[grp] = jb.uw;
-                cs.wsm[grp] = 1;
-                for (int p = 0; p < PB; ++p) {
-                    const int2 pyx = cs.spoi[grp][p];
-                    const int xo = pyx.x < 0 ? 0 : pyx.y - g.rx - xau;
-                    cs.wptr[grp][2 * p] = wwin + xo;
-                    cs.wptr[grp][2 * p + 1] = wwin + jb.utoff + xo;
-                }
-            } else {
-                mbar_expect_tx(tbar, 0u);  // completes the phase: nothing to load
-                cs.wrs[grp] = g.pitch;
-                cs.wsm[grp] = 0;
-                for (int p = 0; p < PB; ++p) {
-                    const int2 pyx = cs.spoi[grp][p];
-                    const size_t o = pyx.x < 0 ? 0 : (size_t)(pyx.x - g.ry) * g.pitch + (pyx.y - g.rx);
-                    cs.wptr[grp][2 * p] = jb.ref + o;
-                    cs.wptr[grp][2 * p + 1] = jb.tar + o;
-                }
+        } else {
+            mbar_expect_tx(tb, 0u);  // completes the phase: nothing to load
+            cs.wrs[grp][sl2] = gx.pitch;
+            cs.wsm[grp][sl2] = 0;
+            for (int p = 0; p < PB; ++p) {
+                const int2 pyx = cs.spoi[grp][sl2][p];
+                const size_t o = pyx.x < 0 ? 0 : (size_t)(pyx.x - gx.ry) * gx.pitch + (pyx.y - gx.rx);
+                cs.wptr[grp][sl2][2 * p] = jx.ref + o;
+                cs.wptr[grp][sl2][2 * p + 1] = jx.tar + o;
             }
         }
         if (!REF) {
-            // the batch's reference spectra towards L2 (epilogue 2 reads them)
-            // and the reference windows' integer sums
-            if (t == 0) {
-                const int np = min(PB, n_job - b0);
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
-                                 reinterpret_cast<uint64_t>(jb.fspec + (size_t)b0 * H * FS)),
-                             "r"((uint32_t)(np * H * FS * 4))
-                             : "memory");
-            }
-            if (t < PB && b0 + t < n_job) {
-                const int2 fsum = jb.fsum[b0 + t];
-                cs.wsum[grp][2 * t][0] = fsum.x;
-                cs.wsum[grp][2 * t][1] = fsum.y;
-            }
+            const int bx0 = (bt - jx.batch_begin) * PB;
+            const int np = min(PB, jx.n - bx0);
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                             reinterpret_cast<uint64_t>(jx.fspec + (size_t)bx0 * H * FS)),
+                         "r"((uint32_t)(np * H * FS * 4))
+                         : "memory");
         }
-        bool ok = mbar_wait(tbar, tphase);
-        tphase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
+    };
+    // a bounded wait gave up: the error flag, and thread 0 lets the next
+    // batch's copies (when staged) land before the group returns
+    auto abort_group = [&](bool pending, int sl2) {
+        if (t == 0) {
+            atomicOr(err, kErrTimeout);
+            if (pending) mbar_wait(&cs.mbar_tma[grp][sl2], (tphase >> sl2) & 1u);
+        }
+    };
+    // prologue: the first batch staged in slot 0, the batch after it drawn
+    // (published after a barrier: the caller's threads may still be reading
+    // the first batch from snext)
+    int cur = first, sl = 0, nxt = 0;
+    if (cur >= nbatch) return true;
+    if (t < PB) cs.spoi[grp][0][t] = batch_poi(cur);
+    if (t == 0) nxt = counter_base + atomicAdd(counter, 1);
+    group_sync(bar_id);
+    if (t == 0) {
+        stage_windows(cur, 0);
+        cs.snext[grp] = nxt;
+    }
+    group_sync(bar_id);
+    int nb = cs.snext[grp];
+    while (cur < nbatch) {
+        const int jj = job_of(cur);
+        const TcJob& jb = J.job[jj];
+        const Geom& g = jb.g;
+        const int n_job = jb.n;
+        const int b0 = (cur - jb.batch_begin) * PB;
+        const bool have_next = nb < nbatch;
+        // loads in flight through the window wait and the A1 build: the next
+        // batch's POIs, this batch's reference window sums (per-frame pass)
+        int2 npoi = make_int2(-1, -1), fsum = make_int2(0, 0);
+        if (t < PB) {
+            if (have_next) npoi = batch_poi(nb);
+            if (!REF && b0 + t < n_job) fsum = jb.fsum[b0 + t];
+        }
+        if (t == 0) nxt = have_next ? counter_base + atomicAdd(counter, 1) : nbatch;  // the batch after nb
+        if (t < 2 * kMaxPB * 2) (&cs.wsum[grp][0][0])[t] = 0;
+        if (t < PB) cs.smaxv[grp][t] = 0u;
+        // this batch's windows (staged one batch earlier)
+        bool ok = mbar_wait(&cs.mbar_tma[grp][sl], (tphase >> sl) & 1u);
+        tphase ^= 1u << sl;
+        if (group_sync_or(bar_id, !ok)) { abort_group(false, sl ^ 1); return false; }
 
         // ---- phase L2: windows -> A1, exact FP16: row (POI, window row y),
         // K = window column x; the reference windows in the per-reference
@@ -470,10 +510,10 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             const int pw = rr / N, y = rr - pw * N;
             const int wi = 2 * pw + (REF ? 0 : 1);
             const bool inb = pw < PB;
-            const bool data = inb && cs.spoi[grp][pw].x >= 0;
+            const bool data = inb && cs.spoi[grp][sl][pw].x >= 0;
             unsigned su = 0u, sq = 0u;
             if (inb) {
-                const uint8_t* src = data ? cs.wptr[grp][wi] + y * cs.wrs[grp] : wwin;
+                const uint8_t* src = data ? cs.wptr[grp][sl][wi] + y * cs.wrs[grp][sl] : wwin;
                 const unsigned sh = 8u * (unsigned)(reinterpret_cast<uintptr_t>(src) & 3);
                 const uint32_t* ws = reinterpret_cast<const uint32_t*>(src - (sh >> 3));
                 uint8_t* a1 = gbase + s.off_a13 + (rr >> 7) * (128 * K1 * 2) + kmaj(rr & 127, 0, K1);
@@ -509,8 +549,16 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 atomicAdd(&cs.wsum[grp][wi][1], gq);
             }
         }
+        if (t < PB) {
+            cs.spoi[grp][sl ^ 1][t] = npoi;  // the next batch's POIs, for its staging below
+            if (!REF && b0 + t < n_job) {
+                cs.wsum[grp][2 * t][0] = fsum.x;
+                cs.wsum[grp][2 * t][1] = fsum.y;
+            }
+        }
         fence_async_smem();
         group_sync(bar_id);
+        const bool pending = have_next;  // from here the next batch's copies may be in flight
 
         // ---- stage 1: D1[(w,y)][(part,kx)] = A1 * B1 (the real DFT along x)
         if (t == 0) {
@@ -526,6 +574,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 }
             }
             mma_commit(mbar);
+            if (have_next) stage_windows(nb, sl ^ 1);  // slot sl ^ 1 was last read by the previous batch
         }
         // per-POI normalisation while the MMAs run: nf = n sum (f - mean)^2 =
         // n sum f^2 - (sum f)^2, exact in integers (likewise ng); the scale of
@@ -541,7 +590,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
+        if (group_sync_or(bar_id, !ok)) { abort_group(pending, sl ^ 1); return false; }
         tc_fence_after();
 
         // ---- epilogue 1: D1 -> A2 (rows (p, kx); K = (y, part) interleaved
@@ -570,21 +619,28 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 uint8_t* rowp = a2 + (data ? p * H : 0) * 16 +
                                 (LO ? (y >> 3) * LB2 + (y & 7) * 2 : (y >> 2) * LB2 + (y & 3) * 4);
                 uint8_t* rowi = a2 + (data ? p * H : 0) * 16 + ((NP + y) >> 3) * LB2 + ((NP + y) & 7) * 2;
+                // TMEM reads three 8-column chunks at a time, one wait each
 #pragma unroll
-                for (int ky0 = 0; ky0 < HP; ky0 += 8) {
-                    float dre[8], dim[8];
-                    tmem_ld8(tm_warp + tile * 2 * HP + ky0, dre);
-                    tmem_ld8(tm_warp + tile * 2 * HP + HP + ky0, dim);
+                for (int cb = 0; cb < HP; cb += 24) {
+                    float dre[24], dim[24];
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        if (cb + 8 * q < HP) {
+                            tmem_ld8(tm_warp + tile * 2 * HP + cb + 8 * q, dre + 8 * q);
+                            tmem_ld8(tm_warp + tile * 2 * HP + HP + cb + 8 * q, dim + 8 * q);
+                        }
+                    }
                     tmem_ld_wait();
                     if (data) {
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            if (ky0 + j < H) {
+                        for (int j = 0; j < 24; ++j) {
+                            const int ky = cb + j;
+                            if (ky < HP && ky < H) {
                                 if (LO) {
-                                    st_half(rowp + (ky0 + j) * 16, dre[j]);
-                                    st_half(rowi + (ky0 + j) * 16, dim[j]);
+                                    st_half(rowp + ky * 16, dre[j]);
+                                    st_half(rowi + ky * 16, dim[j]);
                                 } else {
-                                    *reinterpret_cast<uint32_t*>(rowp + (ky0 + j) * 16) = pack2(dre[j], dim[j]);
+                                    *reinterpret_cast<uint32_t*>(rowp + ky * 16) = pack2(dre[j], dim[j]);
                                 }
                             }
                         }
@@ -646,7 +702,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
+        if (group_sync_or(bar_id, !ok)) { abort_group(pending, sl ^ 1); return false; }
         tc_fence_after();
 
         if (REF) {
@@ -674,6 +730,9 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             tc_fence_before();
             if (t == 0) cs.snext[grp] = nxt;
             group_sync(bar_id);
+            cur = nb;
+            nb = cs.snext[grp];
+            sl ^= 1;
             continue;
         }
 
@@ -780,7 +839,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
+        if (group_sync_or(bar_id, !ok)) { abort_group(pending, sl ^ 1); return false; }
         tc_fence_after();
 
         // ---- epilogue 3: D3 -> A4 (rows (p, v), K = (kx, part) interleaved:
@@ -802,19 +861,27 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
             const int p = rowv ? t / H : 0, ky = rowv ? t - (t / H) * H : 0;
             const float wgt = (ky == 0 || 2 * ky == N) ? 1.f : 2.f;
             uint8_t* rowp = a4 + (p * N) * 16 + (ky >> 2) * LB4 + (ky & 3) * 4;
+            // TMEM reads three 8-column chunks at a time, one wait each
+            // (columns N .. NP-1 are padding)
 #pragma unroll
-            for (int x0 = 0; x0 < NP; x0 += 8) {
-                if (x0 >= N) break;  // columns N .. NP-1 are padding (N is even: N..N+7 too when N % 8)
-                float re[8], im[8];
-                tmem_ld8(tm_warp + x0, re);
-                tmem_ld8(tm_warp + NP + x0, im);
+            for (int cb = 0; cb < NP; cb += 24) {
+                if (cb >= N) break;
+                float re[24], im[24];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (cb + 8 * q < NP) {
+                        tmem_ld8(tm_warp + cb + 8 * q, re + 8 * q);
+                        tmem_ld8(tm_warp + NP + cb + 8 * q, im + 8 * q);
+                    }
+                }
                 tmem_ld_wait();
                 if (rowv) {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (x0 + j < N) {
+                    for (int j = 0; j < 24; ++j) {
+                        const int x = cb + j;
+                        if (x < NP && x < N) {
                             // Zi = -D_i
-                            *reinterpret_cast<uint32_t*>(rowp + (x0 + j) * 16) = pack2(wgt * re[j], -wgt * im[j]);
+                            *reinterpret_cast<uint32_t*>(rowp + x * 16) = pack2(wgt * re[j], -wgt * im[j]);
                         }
                     }
                 }
@@ -841,7 +908,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         ok = mbar_wait(mbar, phase);
         phase ^= 1u;
-        if (group_sync_or(bar_id, !ok)) { if (t == 0) atomicOr(err, kErrTimeout); return false; }
+        if (group_sync_or(bar_id, !ok)) { abort_group(pending, sl ^ 1); return false; }
         tc_fence_after();
 
         // ---- epilogue 4: approximate peak, candidates, exact re-evaluation
@@ -983,8 +1050,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 const int NW4 = s.NW4;
                 const uint32_t tail = (N & 3) ? (0xffffffffu >> (8 * (4 - (N & 3)))) : 0xffffffffu;
                 const int rot = lane % NW4;
-                const int rs = cs.wrs[grp];
-                const bool wsm = cs.wsm[grp] != 0;
+                const int rs = cs.wrs[grp][sl];
+                const bool wsm = cs.wsm[grp][sl] != 0;
                 // task (c, y) = c N + y for thread t, stepped by 128 (all lanes
                 // of a warp take the same number of steps: the warp's sums
                 // per candidate are reduced before one shared atomic each)
@@ -1003,13 +1070,13 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                             // the staged boxes: the circular row product as
                             // two linear segments, f[0, N - kx) g[kx, N) and
                             // f[N - kx, N) g[0, kx)
-                            const uint32_t fb = smem_u32(cs.wptr[grp][2 * p]) + y * rs;
-                            const uint32_t gb = smem_u32(cs.wptr[grp][2 * p + 1]) + yy * rs;
+                            const uint32_t fb = smem_u32(cs.wptr[grp][sl][2 * p]) + y * rs;
+                            const uint32_t gb = smem_u32(cs.wptr[grp][sl][2 * p + 1]) + yy * rs;
                             acc0 = dot_bytes_s(fb, gb + kx, N - kx, acc0);
                             acc1 = dot_bytes_s(fb + N - kx, gb, kx, acc1);
                         } else {
-                            const uint8_t* fb = cs.wptr[grp][2 * p] + y * rs;
-                            const uint8_t* gb = cs.wptr[grp][2 * p + 1] + yy * rs;
+                            const uint8_t* fb = cs.wptr[grp][sl][2 * p] + y * rs;
+                            const uint8_t* gb = cs.wptr[grp][sl][2 * p + 1] + yy * rs;
                             const uint32_t g0 = ld_unaligned_p(gb);
 #pragma unroll 2
                             for (int jj = 0; jj < NW4; ++jj) {
@@ -1079,6 +1146,9 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         if (t == 0) cs.snext[grp] = nxt;
         group_sync(bar_id);
+        cur = nb;
+        nb = cs.snext[grp];
+        sl ^= 1;
     }
     return true;
 }
@@ -1096,7 +1166,8 @@ __device__ __forceinline__ bool tc_setup(TcCta& cs, uint8_t* sm, int groups, uin
     if (threadIdx.x == 0) {
         for (int k = 0; k < groups; ++k) {
             mbar_init(&cs.mbar_mma[k]);
-            mbar_init(&cs.mbar_tma[k]);
+            mbar_init(&cs.mbar_tma[k][0]);
+            mbar_init(&cs.mbar_tma[k][1]);
         }
     }
     tc_fence_before();
@@ -1302,7 +1373,7 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     s.utoff = round_up(N * s.uw, 128);
     s.win_bytes = round_up(s.utoff + N * s.uw + 16, 128);
     s.off_win = region;
-    s.group_bytes = round_up(region + s.win_bytes, 1024);
+    s.group_bytes = round_up(region + 2 * s.win_bytes, 1024);  // two window slots
     // 227 KB per CTA, less the static state (the dynamic part starts 1024-byte aligned)
     const int limit = 227 * 1024 - round_up((int)sizeof(TcCta), 1024);
     s.groups = std::min(kMaxGroups, (limit - o) / s.group_bytes);

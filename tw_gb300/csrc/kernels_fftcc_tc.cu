@@ -399,58 +399,57 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         const int bx0 = (bt - jx.batch_begin) * PB;
         return bx0 + t < jx.n ? jx.poi[bx0 + t] : make_int2(-1, -1);
     };
-    // thread 0: a batch's windows into slot sl2, its POIs being in that
-    // slot.  When the POIs lie on one POI row, one [N][uw] TMA box per image
-    // holds all the windows (x aligned down to 16 bytes); otherwise (a batch
-    // across POI rows, POIs off the grid) the windows are read from the
-    // images in global memory.  The per-frame pass also sends the batch's
-    // cached reference spectra towards L2 (epilogue 2 reads them).
+    // warp 1 (all its lanes): a batch's windows into slot sl2, its POIs
+    // being in that slot.  When the POIs lie on one POI row, one [N][uw] TMA
+    // box per image holds all the windows (x aligned down to 16 bytes);
+    // otherwise (a batch across POI rows, POIs off the grid) the windows are
+    // read from the images in global memory.  The per-frame pass also sends
+    // the batch's cached reference spectra towards L2 (epilogue 2 reads them).
+    // Warp 1 works while thread 0 issues the MMAs.
     auto stage_windows = [&](int bt, int sl2) {
         const TcJob& jx = J.job[job_of(bt)];
         const Geom& gx = jx.g;
         uint8_t* wbuf = wwin + sl2 * s.win_bytes;
         uint64_t* tb = &cs.mbar_tma[grp][sl2];
-        fence_async_smem();  // the slot's earlier generic reads come before the copies' writes
-        int ymin = 0x7fffffff, ymax = -0x7fffffff, xmin = 0x7fffffff, xmax = -0x7fffffff;
-        for (int p = 0; p < PB; ++p) {
-            const int2 pyx = cs.spoi[grp][sl2][p];
-            if (pyx.x < 0) continue;
-            ymin = min(ymin, pyx.x); ymax = max(ymax, pyx.x);
-            xmin = min(xmin, pyx.y); xmax = max(xmax, pyx.y);
-        }
+        const int2 pyx = lane < PB ? cs.spoi[grp][sl2][lane] : make_int2(-1, -1);
+        const bool v = pyx.x >= 0;
+        const int ymin = __reduce_min_sync(kFull, v ? pyx.x : INT_MAX);
+        const int ymax = __reduce_max_sync(kFull, v ? pyx.x : INT_MIN);
+        const int xmin = __reduce_min_sync(kFull, v ? pyx.y : INT_MAX);
+        const int xmax = __reduce_max_sync(kFull, v ? pyx.y : INT_MIN);
         const int xau = (xmin - gx.rx) & ~15;
         const bool uni = jx.uw > 0 && ymin == ymax && xmax - gx.rx + N - xau <= jx.uw;
-        if (uni) {
-            const int y0 = ymin - gx.ry;
-            mbar_expect_tx(tb, (uint32_t)(2 * N * jx.uw));
-            tma_load_2d(wbuf, &jx.maps->ref_u, xau, y0, tb);
-            tma_load_2d(wbuf + jx.utoff, &jx.maps->tar_u, xau, y0, tb);
-            cs.wrs[grp][sl2] = jx.uw;
-            cs.wsm[grp][sl2] = 1;
-            for (int p = 0; p < PB; ++p) {
-                const int2 pyx = cs.spoi[grp][sl2][p];
-                const int xo = pyx.x < 0 ? 0 : pyx.y - gx.rx - xau;
-                cs.wptr[grp][sl2][2 * p] = wbuf + xo;
-                cs.wptr[grp][sl2][2 * p + 1] = wbuf + jx.utoff + xo;
+        if (lane == 0) {
+            fence_async_smem();  // the slot's earlier generic reads come before the copies' writes
+            if (uni) {
+                const int y0 = ymin - gx.ry;
+                mbar_expect_tx(tb, (uint32_t)(2 * N * jx.uw));
+                tma_load_2d(wbuf, &jx.maps->ref_u, xau, y0, tb);
+                tma_load_2d(wbuf + jx.utoff, &jx.maps->tar_u, xau, y0, tb);
+            } else {
+                mbar_expect_tx(tb, 0u);  // completes the phase: nothing to load
             }
-        } else {
-            mbar_expect_tx(tb, 0u);  // completes the phase: nothing to load
-            cs.wrs[grp][sl2] = gx.pitch;
-            cs.wsm[grp][sl2] = 0;
-            for (int p = 0; p < PB; ++p) {
-                const int2 pyx = cs.spoi[grp][sl2][p];
-                const size_t o = pyx.x < 0 ? 0 : (size_t)(pyx.x - gx.ry) * gx.pitch + (pyx.y - gx.rx);
-                cs.wptr[grp][sl2][2 * p] = jx.ref + o;
-                cs.wptr[grp][sl2][2 * p + 1] = jx.tar + o;
+            cs.wrs[grp][sl2] = uni ? jx.uw : gx.pitch;
+            cs.wsm[grp][sl2] = uni ? 1 : 0;
+            if (!REF) {
+                const int bx0 = (bt - jx.batch_begin) * PB;
+                const int np = min(PB, jx.n - bx0);
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
+                                 reinterpret_cast<uint64_t>(jx.fspec + (size_t)bx0 * H * FS)),
+                             "r"((uint32_t)(np * H * FS * 4))
+                             : "memory");
             }
         }
-        if (!REF) {
-            const int bx0 = (bt - jx.batch_begin) * PB;
-            const int np = min(PB, jx.n - bx0);
-            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(
-                             reinterpret_cast<uint64_t>(jx.fspec + (size_t)bx0 * H * FS)),
-                         "r"((uint32_t)(np * H * FS * 4))
-                         : "memory");
+        if (lane < PB) {
+            if (uni) {
+                const int xo = v ? pyx.y - gx.rx - xau : 0;
+                cs.wptr[grp][sl2][2 * lane] = wbuf + xo;
+                cs.wptr[grp][sl2][2 * lane + 1] = wbuf + jx.utoff + xo;
+            } else {
+                const size_t o = v ? (size_t)(pyx.x - gx.ry) * gx.pitch + (pyx.y - gx.rx) : 0;
+                cs.wptr[grp][sl2][2 * lane] = jx.ref + o;
+                cs.wptr[grp][sl2][2 * lane + 1] = jx.tar + o;
+            }
         }
     };
     // a bounded wait gave up: the error flag, and thread 0 lets the next
@@ -469,10 +468,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
     if (t < PB) cs.spoi[grp][0][t] = batch_poi(cur);
     if (t == 0) nxt = counter_base + atomicAdd(counter, 1);
     group_sync(bar_id);
-    if (t == 0) {
-        stage_windows(cur, 0);
-        cs.snext[grp] = nxt;
-    }
+    if (warp == 1) stage_windows(cur, 0);
+    if (t == 0) cs.snext[grp] = nxt;
     group_sync(bar_id);
     int nb = cs.snext[grp];
     while (cur < nbatch) {
@@ -574,8 +571,8 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 }
             }
             mma_commit(mbar);
-            if (have_next) stage_windows(nb, sl ^ 1);  // slot sl ^ 1 was last read by the previous batch
         }
+        if (warp == 1 && have_next) stage_windows(nb, sl ^ 1);  // slot sl ^ 1 was last read by the previous batch
         // per-POI normalisation while the MMAs run: nf = n sum (f - mean)^2 =
         // n sum f^2 - (sum f)^2, exact in integers (likewise ng); the scale of
         // the cached reference spectrum is sqrt(n) / sqrt(nf), of the target's

@@ -1049,15 +1049,15 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                 const int rot = lane % NW4;
                 const int rs = cs.wrs[grp][sl];
                 const bool wsm = cs.wsm[grp][sl] != 0;
-                // task (c, y) = c N + y for thread t, stepped by 128 (all lanes
-                // of a warp take the same number of steps: the warp's sums
-                // per candidate are reduced before one shared atomic each)
-                const int ntask = nc * N, dc = 128 / N, dy = 128 - dc * N;
-                int c = t / N, y = t - (t / N) * N;
-                for (int base = 0; base < ntask; base += 128) {
-                    const bool valid = base + t < ntask;
+                // task (c, y) = y nc + c for thread t, stepped by 128: a
+                // warp's lanes take the candidates of one row side by side
+                // (windows of different POIs: their rows fall in different
+                // banks), one shared atomic per task
+                const int dy = 128 / nc, dc = 128 - dy * nc;
+                int y = t / nc, c = t - (t / nc) * nc;
+                for (; y < N;) {
                     unsigned acc0 = 0u, acc1 = 0u;
-                    if (valid) {
+                    {
                         const int code = ps->cand[c];
                         const int p = code >> 16, ky = (code >> 8) & 0xff, kx = code & 0xff;
                         int yy = y + ky;
@@ -1092,14 +1092,12 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
                             }
                         }
                     }
-                    const unsigned seg = __match_any_sync(kFull, valid ? c : -1);
-                    const int sum = __reduce_add_sync(seg, (int)(acc0 + acc1));
-                    if (valid && lane == __ffs(seg) - 1) atomicAdd(&ps->candS[c], sum);
+                    atomicAdd(&ps->candS[c], (int)(acc0 + acc1));
                     c += dc;
                     y += dy;
-                    if (y >= N) {
-                        y -= N;
-                        ++c;
+                    if (c >= nc) {
+                        c -= nc;
+                        ++y;
                     }
                 }
             }

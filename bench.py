@@ -454,11 +454,11 @@ def _run_gpu(args, world, rank, local, torch):
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
 # profiles/k_icgn_warp_2048_subset41.md and profiles/k_fftcc_tc_2048_subset41.md
-NCU_TRAFFIC = {"k_icgn_warp": 123.86e6 + 6.69e6, "k_fftcc_tc": 9.60e6 + 0.0}
+NCU_TRAFFIC = {"k_icgn_warp": 140.58e6 + 7.22e6, "k_fftcc_tc": 532.43e6 + 5.60e6}
 # from the same IC-GN capture: L1 hit rate of its gathers and the FMA-heavy
 # pipe's share of cycles (the kernel's limiter)
-NCU_ICGN_L1_HIT = 0.891
-NCU_ICGN_FMAHEAVY = 0.680
+NCU_ICGN_L1_HIT = 0.933
+NCU_ICGN_FMAHEAVY = 0.667
 
 
 def fp32_peak(peaks):
@@ -481,8 +481,8 @@ def roofline(g, P, ph, kbar):
     the per-phase CUDA events of the frame.
 
     Binding view (bound / achieved / peak / frac): FP32.  The kernel is
-    limited by the SM's FP32 and integer pipes (ncu: FMA-heavy pipe busy 68 %
-    of cycles, 79 % issue) with its gathers served by L1 (89 % hits); the
+    limited by the SM's FP32 and integer pipes (ncu: FMA-heavy pipe busy 67 %
+    of cycles, 77 % issue) with its gathers served by L1 (93 % hits); the
     credited work is k*S*64 flops per POI (k = mean iterations, S = subset
     pixels; 64 flops per sample and iteration: warp 8, bicubic Horner 30,
     mean/norm 6, residual 4, right-hand side 12, address 4), against the
@@ -490,11 +490,16 @@ def roofline(g, P, ph, kbar):
 
     Secondary views: HBM (the compulsory bytes per launch: the target's 4x4
     neighbourhood table read once, 16 B per ROI pixel; the per-reference
-    gradient image, 4 B per ROI pixel; the target image; per POI the
+    gradient image, float2, 8 B per ROI pixel; the target image; per POI the
     reference cache entry -- statistics 64 B, FP64 inverse Hessian 168 B, flag
     1 B -- the POI 8 B, u/v in 8 B and out 8 B, p6 24 B, iteration count 4 B
-    and flag 1 B); gathers (k*S*20 B per POI through L1/L2); and the tensor
-    view of the FFT-CC kernel (48 N^3 flops per POI)."""
+    and flag 1 B; the subset sample table, 16 B per subset pixel); gathers
+    (k*S*40 B per POI through L1/L2: table entry, gradient and sample-table
+    entry of every sample); and the tensor view of the FFT-CC kernel
+    (48 N^3 flops per POI) with its own HBM bytes (per POI the cached
+    reference spectrum, N/2 + 1 rows of N rounded up to 4 FP16 pairs, and the
+    reference window sums 8 B, the POI 8 B, u, v, ZNCC 12 B and status 1 B;
+    both images once)."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -509,12 +514,13 @@ def roofline(g, P, ph, kbar):
     t_icgn = ph["icgn"] / 1000.0
     t_fftcc = ph["fftcc"] / 1000.0
     per_poi = 64 + 168 + 1 + 8 + 8 + 8 + 24 + 4 + 1
-    bytes_icgn = P * per_poi + (16 + 4) * g.roi_w * g.roi_h + g.img_w * g.img_h
+    bytes_icgn = P * per_poi + (16 + 8) * g.roi_w * g.roi_h + g.img_w * g.img_h + 16 * S
     flops_icgn = kbar * S * 64 * P
     achieved = flops_icgn / t_icgn / 1e12
-    gather = kbar * S * 20 * P
+    gather = kbar * S * 40 * P  # per sample: table entry 16 B, gradient 8 B, sample-table entry 16 B
     flops_fftcc = 48 * N ** 3 * P
     fft_tflops = flops_fftcc / t_fftcc / 1e12
+    bytes_fftcc = fftcc_bytes(g, P)
     return {"kernel": "k_icgn_warp (IC-GN)", "bound": "fp32", "achieved": round(achieved, 3),
             "peak": round(fp32 / 1e12, 2), "unit": "TFLOP/s", "frac": round(achieved * 1e12 / fp32, 4),
             "traffic": NCU_TRAFFIC["k_icgn_warp"], "peak_source": fp32_src,
@@ -530,8 +536,20 @@ def roofline(g, P, ph, kbar):
                                   "achieved_tflops": round(fft_tflops, 2), "peak_tflops": tc,
                                   "frac": round(fft_tflops / tc, 4), "kernel_ms": round(ph["fftcc"], 4),
                                   "traffic": NCU_TRAFFIC["k_fftcc_tc"],
-                                  "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)"},
-            "frame_roofline": frame_roofline(g, P, ph, kbar, peaks, bytes_icgn)}
+                                  "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",
+                                  "hbm_bytes_per_launch": int(bytes_fftcc),
+                                  "hbm_achieved_gbs": round(bytes_fftcc / t_fftcc / 1e9, 1),
+                                  "hbm_frac": round(bytes_fftcc / t_fftcc / 1e9 / hbm, 4)},
+            "frame_roofline": frame_roofline(g, P, ph, kbar, peaks, bytes_icgn + bytes_fftcc)}
+
+
+def fftcc_bytes(g, P):
+    """Algorithmic HBM bytes of one per-frame FFT-CC launch: per POI the
+    cached reference spectrum and window sums, the POI and the outputs; both
+    images once."""
+    N = 2 * g.subset_r
+    spectrum = (N // 2 + 1) * ((N + 3) // 4 * 4) * 4
+    return P * (spectrum + 8 + 8 + 12 + 1) + 2 * g.img_w * g.img_h
 
 
 def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
@@ -539,7 +557,8 @@ def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
     B_compulsory / Peak_HBM) with F_a = 48 N^3 (FFT-CC, credited flops only)
     and F_c = k S 64 (IC-GN); achieved = T_roof / T_measured.  B_compulsory is
     this design's: both images, the neighbourhood table and gradient image,
-    and the per-POI cache and outputs.  (A 64 B/px coefficient LUT and S*28 B
+    the per-POI caches (IC-GN statistics and inverse Hessian, FFT-CC
+    reference spectra) and the outputs.  (A 64 B/px coefficient LUT and S*28 B
     of per-POI reference data, the reference's layout, are never moved here,
     so they are not in the bound.)  Peak_FP32 is not in MEASURED_PEAKS.json:
     it is 128 FP32 lanes x 2 flops per SM and clock at the measured maximum SM
@@ -551,7 +570,7 @@ def frame_roofline(g, P, ph, kbar, peaks, bytes_icgn):
     peak_hbm = peaks.get("hbm_gbs", 6800.0) * 1e9
     t_tc = P * 48 * N ** 3 / peak_tc
     t_fp32 = P * kbar * S * 64 / peak_fp32
-    b_comp = bytes_icgn + 2 * g.img_w * g.img_h  # IC-GN's bytes plus FFT-CC's image reads
+    b_comp = bytes_icgn  # IC-GN's and FFT-CC's bytes
     t_hbm = b_comp / peak_hbm
     t_roof = t_tc + max(t_fp32, t_hbm)
     t_meas = (ph["fftcc"] + ph["prepare"] + ph["icgn"]) / 1000.0

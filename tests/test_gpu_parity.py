@@ -579,3 +579,58 @@ def test_tables_equal_the_oracle(request, case):
     bs_o = O.bspline_lut(pair.tar, g.start_x, g.start_y, g.roi_w, g.roi_h)
     print(case, "B-spline LUT: exact", float((bs == bs_o).mean()), "max diff", float(np.abs(bs - bs_o).max()))
     np.testing.assert_allclose(bs, bs_o, rtol=1e-6, atol=1e-4)
+
+
+@pytest.mark.parametrize("h,w,r,grid", [
+    (160, 300, 20, 5),    # batches of 6 on one POI row: the staged one-row boxes
+    (170, 200, 20, 7),    # 13 POIs per row: batches across POI rows read the images
+    (260, 420, 20, 60),   # a box would be wider than 256 bytes: every batch reads the images
+    (200, 230, 31, 11),   # N = 62, batches of 4, rows of 16 and odd remainders
+])
+def test_fftcc_window_paths(h, w, r, grid):
+    """The tensor-core FFT-CC's window sources: one TMA box pair per batch on
+    one POI row, the images in global memory for batches across POI rows and
+    for grid steps too wide for a box; strict parity with the oracle."""
+    pair, g = synth.small_case(h=h, w=w, r=r, grid=grid, seed=300 + grid)
+    nx, ny, _ = O.num_pois(g.roi_w, g.roi_h, g.subset_r, g.grid, g.margin)
+    assert nx > 0 and ny > 0
+    poi = O.poi_positions(g.start_x, g.start_y, nx, ny, g.margin, g.subset_r, g.grid)
+    u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, poi, r)
+    f = dic.cuFFTCC2D(g.img_w, g.img_h, g.roi_w, g.roi_h, g.start_x, g.start_y, r, r, g.grid, g.grid, g.margin,
+                      g.margin, path=PATH_FAST)
+    U, V, Z = f.InitializeFFTCC(pair.ref)
+    st = np.zeros(f.GetNumPOIs(), np.uint8)
+    f.ComputeFFTCC(U, V, Z, pair.tar, status=st)
+    rep = C.fftcc_parity(pair.ref, pair.tar, poi, r, U.ravel(), V.ravel(), Z.ravel(), u_or, v_or, z_or, st_or)
+    assert (st == st_or).all()
+    assert rep.ok(), (nx, ny, rep)
+
+
+def test_fftcc_batch_mixed_grid_steps():
+    """Frames of one window size but different grid steps in one batched
+    launch: the launch's window region is sized for the first frame's boxes,
+    so a frame whose boxes do not fit reads its windows from the images;
+    every frame equals its single-frame result and the oracle."""
+    cases = [(180, 260, 20, 5, 41), (220, 330, 20, 23, 42), (200, 240, 20, 9, 43)]
+    frames, tars, want, refs = [], [], [], []
+    for h, w, r, grid, seed in cases:
+        pair, g = synth.small_case(h=h, w=w, r=r, grid=grid, seed=seed)
+        fr = dic.DICFrame(params_of(g, PATH_FAST))
+        fr.set_reference(pair.ref)
+        o = fr.alloc_outputs()
+        fr.process(pair.tar, **o)
+        frames.append(fr)
+        tars.append(pair.tar)
+        want.append(o)
+        refs.append((pair, g))
+    b = dic.DICBatch()
+    outs = [fr.alloc_outputs() for fr in frames]
+    b.process(frames, tars, outs)
+    for i, (o, wnt, (pair, g)) in enumerate(zip(outs, want, refs)):
+        for k in wnt:
+            np.testing.assert_array_equal(o[k], wnt[k], err_msg=f"frame {i} {k}")
+        poi = frames[i].poi_positions()
+        u_or, v_or, z_or, st_or = O.fftcc(pair.ref, pair.tar, poi, g.subset_r)
+        sel = st_or == 0
+        assert sel.mean() > 0.9
+        np.testing.assert_allclose(o["zncc"][sel], z_or[sel], atol=3e-5)

@@ -242,7 +242,7 @@ TWDIC_API int twdic_frame_set_guess_mode(twdic_frame* h, int mode);
 TWDIC_API int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll);
 
 /* FFT-CC tile of a frame handle: use_tc (tensor-core kernel), groups (0 = as
- * many 128-thread groups per CTA as fit, 1 to 4 = at most that many),
+ * many 128-thread groups per CTA as fit, 1 to 5 = at most that many),
  * pois_per_group (POIs per group batch, 0 = the most the tiles hold).  No
  * reference counterpart. */
 TWDIC_API int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group);

@@ -873,7 +873,7 @@ int twdic_frame_set_icgn_unroll(twdic_frame* h, int unroll) {
 
 int twdic_frame_set_fftcc_tuning(twdic_frame* h, int use_tc, int groups, int pois_per_group) {
     if (!h) return fail(TWDIC_ERR_INVALID_ARG, "NULL handle");
-    if (groups < 0 || groups > 4 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
+    if (groups < 0 || groups > 5 || pois_per_group < 0) return fail(TWDIC_ERR_INVALID_ARG, "bad FFT-CC tuning");
     h->e.fftcc_tune.use_tc = use_tc;
     h->e.fftcc_tune.groups = groups;
     h->e.fftcc_tune.pois_per_group = pois_per_group;
@@ -930,7 +930,7 @@ bool cached_tuning_valid(const twdic_tuning& c) {
     return valid_icgn_threads(c.icgn_threads) && c.icgn_ctas_per_sm >= 0 && c.icgn_sampler >= kSampWindow &&
            c.icgn_sampler <= kSampNbhd && c.icgn_chunk >= 0 &&
            (c.icgn_unroll == 2 || c.icgn_unroll == 4 || c.icgn_unroll == 8) &&
-           (c.fftcc_use_tc == 0 || c.fftcc_use_tc == 1) && c.fftcc_groups >= 0 && c.fftcc_groups <= 2 &&
+           (c.fftcc_use_tc == 0 || c.fftcc_use_tc == 1) && c.fftcc_groups >= 0 && c.fftcc_groups <= 5 &&
            c.fftcc_pois_per_group >= 0;
 }
 
@@ -1011,7 +1011,7 @@ int twdic_frame_autotune(twdic_frame* h, const uint8_t* tar, int32_t stride, int
     FftccTune best_f = fft0;
     float best_fms = 1e30f;
     if (e.prm.path == TWDIC_PATH_FAST && fftcc_tc_supported(e.g)) {
-        for (int groups : {0, 2, 1}) {
+        for (int groups : {0, 4, 2, 1}) {
             for (int ppg : {0, 2, 1}) {
                 FftccTune c;
                 c.use_tc = 1;

@@ -54,7 +54,8 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kCandChunk = 128;   // exact re-evaluations per pass (all POIs of a group batch)
 constexpr int kMaxPB = 8;         // POIs per batch (upper bound)
-constexpr int kMaxGroups = 4;     // 128-thread groups per CTA (upper bound)
+constexpr int kMaxGroups = 5;     // 128-thread groups per CTA (upper bound; window sizes up to 48)
+constexpr int kSegGroups = 4;     // groups per CTA of the larger windows and of the segmented kernel
 // Candidate window of the approximate correlation surface, in ZNCC units.
 // The exact peak lies within twice the surface's error of the approximate
 // maximum; the largest error measured at any evaluated candidate on the
@@ -63,7 +64,7 @@ constexpr int kMaxGroups = 4;     // 128-thread groups per CTA (upper bound)
 // twiddles, so 0.01 keeps a margin of five or more.
 constexpr float kCandZncc = 0.01f;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kTmemCols = 128;
+constexpr int kTmemCols = 128;  // TMEM columns a group may use (its stride is the shape's tcols)
 constexpr unsigned kWaitLimit = 1u << 24;
 
 // The tensor maps of one image pair: boxes [N rows][uw bytes] holding the
@@ -76,6 +77,7 @@ constexpr int kMaxTcSegs = kMaxTcSegsScratch;    // window sizes per launch (N =
 
 struct TcShape {
     int N, H, HP, NP, PB, tiles1, K4, groups;
+    int tcols;      // TMEM columns per group (96 or 128): the widest accumulator of the four stages
     int uw, utoff;  // one-row boxes: width (0: none for this geometry) and the target box's offset
     int win_bytes;  // a group's window region
     int tiles4;  // 128-row tiles of the surface (stage 4)
@@ -379,7 +381,7 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
     uint8_t* wwin = gbase + s.off_win;
     PeakScratch* ps = reinterpret_cast<PeakScratch*>(gbase + s.off_a13);
     uint64_t* mbar = &cs.mbar_mma[grp];
-    const uint32_t tm = cs.tmem_slot + grp * kTmemCols;
+    const uint32_t tm = cs.tmem_slot + grp * s.tcols;
     const uint32_t tm_warp = tm + ((uint32_t)(warp * 32) << 16);
     const uint32_t gaddr = smem_u32(gbase);
     const uint32_t sbase = smem_u32(sm);
@@ -1191,13 +1193,14 @@ __device__ __forceinline__ void tc_teardown(TcCta& cs, uint32_t tmem_cols) {
 // of every group by position, then the next free one from the launch-wide
 // counter, which evens out the groups' finishing times.
 template <int NP, int HP, bool MULTI, bool LO, bool REF>
-__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
+__global__ void __launch_bounds__(NP <= 48 ? 128 * kMaxGroups : 128 * kSegGroups, 1) k_fftcc_tc(const __grid_constant__ TcJobs J, TcShape s,
                                                                  const uint4* __restrict__ tables, unsigned* err,
                                                                  int* work) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ TcCta cs;
     const int grp = threadIdx.x >> 7;
-    const uint32_t tmem_cols = s.groups == 1 ? 128u : (s.groups == 2 ? 256u : 512u);
+    uint32_t tmem_cols = 32u;  // the groups' columns, allocated as a power of two
+    while (tmem_cols < (uint32_t)(s.groups * s.tcols)) tmem_cols <<= 1;
     tc_load_tables(sm, tables, s.tab_bytes);
     if ((threadIdx.x & 127) == 0) tc_acquire_maps(J, 0, J.njobs);
     if (!tc_setup(cs, sm, s.groups, tmem_cols, err)) return;
@@ -1248,13 +1251,13 @@ __device__ __forceinline__ bool tc_run_segment(const TcJobs& J, const TcSeg& sg,
 // the segment's batches from the segment's counter; when they run out, the
 // CTA moves to the next segment with batches left, until none has.
 template <bool LO>
-__global__ void __launch_bounds__(128 * kMaxGroups, 1) k_fftcc_tc_seg(const __grid_constant__ TcJobs J,
+__global__ void __launch_bounds__(128 * kSegGroups, 1) k_fftcc_tc_seg(const __grid_constant__ TcJobs J,
                                                                      const __grid_constant__ TcSegs S,
                                                                      unsigned* err, int* counters) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ TcCta cs;
     constexpr uint32_t tmem_cols = 512u;
-    if (!tc_setup(cs, sm, kMaxGroups, tmem_cols, err)) return;
+    if (!tc_setup(cs, sm, kSegGroups, tmem_cols, err)) return;
     if ((threadIdx.x & 127) == 0) tc_acquire_maps(J, 0, J.njobs);
     int seg = 0;
     while (seg + 1 < S.nseg && (int)blockIdx.x >= S.seg[seg + 1].cta_begin) ++seg;
@@ -1371,7 +1374,11 @@ bool make_shape(const Geom& g, const FftccTune& tune, TcShape& s) {
     s.group_bytes = round_up(region + 2 * s.win_bytes, 1024);  // two window slots
     // 227 KB per CTA, less the static state (the dynamic part starts 1024-byte aligned)
     const int limit = 227 * 1024 - round_up((int)sizeof(TcCta), 1024);
-    s.groups = std::min(kMaxGroups, (limit - o) / s.group_bytes);
+    // TMEM: each group's widest accumulator (stage 1: tiles x 2 HP, stages 2
+    // and 3: 2 NP, stage 4: tiles x NP), 96 columns up to N = 48, so five
+    // groups share the 512 columns there, four above
+    s.tcols = round_up(std::max(std::max(s.tiles1 * 2 * s.HP, s.tiles4 * s.NP), 2 * s.NP), 32);
+    s.groups = std::min(std::min(kMaxGroups, 512 / s.tcols), (limit - o) / s.group_bytes);
     if (tune.groups > 0) s.groups = std::min(s.groups, tune.groups);  // tuned group count
     if (s.groups < 1) return false;
     s.smem_bytes = o + s.groups * s.group_bytes;
@@ -1580,7 +1587,11 @@ cudaError_t launch_segments(const FftccJob* jobs, int njobs, const FftccTune& tu
         if (S->nseg == 0 || in.g.rx != J->job[S->seg[S->nseg - 1].job_lo].g.rx) {
             if (S->nseg == kMaxTcSegs) return cudaErrorInvalidValue;
             TcSeg& sg = S->seg[S->nseg++];
-            if (!make_shape(in.g, tune, sg.s)) return cudaErrorNotSupported;
+            // at most kSegGroups groups: the segmented kernel holds every window
+            // size's code, and 128 registers keep it free of spills
+            FftccTune ts = tune;
+            if (ts.groups == 0 || ts.groups > kSegGroups) ts.groups = kSegGroups;
+            if (!make_shape(in.g, ts, sg.s)) return cudaErrorNotSupported;
             sg.shape = shape_index(sg.s);
             if (sg.shape < 0) return cudaErrorNotSupported;
             cudaError_t e = tables_for(sg.s, &sg.tables);
@@ -1620,7 +1631,7 @@ cudaError_t launch_segments(const FftccJob* jobs, int njobs, const FftccTune& tu
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(counters, 0, sizeof(int) * kMaxTcSegs, st);
     if (e != cudaSuccess) return e;
-    kern<<<sms, kThreads * kMaxGroups, smem, st>>>(*J, *S, err, counters);
+    kern<<<sms, kThreads * kSegGroups, smem, st>>>(*J, *S, err, counters);
     return cudaGetLastError();
 }
 

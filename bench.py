@@ -454,7 +454,7 @@ def _run_gpu(args, world, rank, local, torch):
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
 # of each kernel on this workload, from the ncu captures summarised in
 # profiles/k_icgn_warp_2048_subset41.md and profiles/k_fftcc_tc_2048_subset41.md
-NCU_TRAFFIC = {"k_icgn_warp": 140.58e6 + 7.22e6, "k_fftcc_tc": 532.43e6 + 5.60e6}
+NCU_TRAFFIC = {"k_icgn_warp": 139.83e6 + 7.27e6, "k_fftcc_tc": 532.76e6 + 5.50e6}
 # from the same IC-GN capture: L1 hit rate of its gathers and the FMA-heavy
 # pipe's share of cycles (the kernel's limiter)
 NCU_ICGN_L1_HIT = 0.933

@@ -23,8 +23,10 @@
 // correlation), with the reference's first-maximum rule.
 // ZNCC is the quotient of the exact integer sums, evaluated in FP32.
 //
-// Up to four groups of 128 threads (one warpgroup each, 128 TMEM columns
-// each) per CTA, one CTA per SM, persistent over batches of POIs; thread 0
+// Up to five groups of 128 threads (one warpgroup each, each with the TMEM
+// columns of its widest accumulator: 96 up to N = 48, then 128, so five groups
+// there and four above) per CTA, one CTA per SM, persistent over batches of
+// POIs; thread 0
 // of a group issues its MMAs, completion is signalled through an mbarrier
 // (bounded wait), the epilogues read TMEM with tcgen05.ld.  The reference
 // windows' spectra are computed once per reference (the per-reference pass)
@@ -1016,11 +1018,10 @@ __device__ __forceinline__ bool tc_group_batches(const TcJobs& J, const TcShape&
         }
         // exact integer correlation of every candidate, kCandChunk slots at a
         // time (any number of candidates: a broad or periodic surface only
-        // takes more chunks), read from the staged windows: tasks (slot, row)
-        // over the group's threads, four products per DP4A, one shared atomic
-        // per task.  Lanes walk the words of their row in a lane-rotated
-        // order, which spreads rows that share shared-memory banks over
-        // different words.  Thread t < PB keeps POI t's best candidate: the
+        // takes more chunks), read from the windows: tasks (slot, row) over
+        // the group's threads, four products per DP4A, one shared atomic per
+        // task (windows read from the images: lanes walk the words of their
+        // row in a lane-rotated order).  Thread t < PB keeps POI t's best candidate: the
         // largest exact sum, the smallest index among equal sums (the
         // reference's first maximum), whatever the chunking.
         int best_s = INT_MIN, best_i = 0;
@@ -1189,7 +1190,7 @@ __device__ __forceinline__ void tc_teardown(TcCta& cs, uint32_t tmem_cols) {
                      "r"(tmem_cols));
 }
 
-// One window size: blockDim = 128 * s.groups (up to four).  The first batch
+// One window size: blockDim = 128 * s.groups (up to five).  The first batch
 // of every group by position, then the next free one from the launch-wide
 // counter, which evens out the groups' finishing times.
 template <int NP, int HP, bool MULTI, bool LO, bool REF>
